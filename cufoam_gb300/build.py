@@ -1,0 +1,78 @@
+"""Build the library in-tree: nvcc, one -gencode for sm_103a, translation
+units compiled in parallel, linked into ``cufoam_gb300/_build/libcufoam_gb300.so``
+(a plain C-ABI shared library: no Python or torch symbols)."""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_NAME = "libcufoam_gb300.so"
+LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
+
+SOURCES = ["capi.cu", "matrix.cu", "solve_fp64.cu", "mixed.cu", "adjoint.cu", "batched.cu"]
+HEADERS = ["internal.h", "device.cuh", "solver_common.cuh"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _flags() -> list[str]:
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                   "-I" + INCLUDE, "-I" + CSRC, "--expt-relaxed-constexpr"]
+
+
+def _newest(paths: list[str]) -> float:
+    return max(os.path.getmtime(p) for p in paths)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "cufoam_gb300.h")]
+    hdr_time = _newest(hdrs)
+    objs = []
+    jobs = []
+    for src in SOURCES:
+        sp = os.path.join(CSRC, src)
+        op = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
+        objs.append(op)
+        if force or not os.path.exists(op) or os.path.getmtime(op) < max(os.path.getmtime(sp), hdr_time):
+            jobs.append((sp, op))
+
+    def compile_one(job):
+        sp, op = job
+        tmp = op + f".tmp{os.getpid()}"
+        cmd = [nvcc()] + _flags() + ["-c", sp, "-o", tmp]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {sp}:\n{r.stdout}\n{r.stderr}")
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout + r.stderr)
+        os.replace(tmp, op)
+
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            list(ex.map(compile_one, jobs))
+    if jobs or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < _newest(objs):
+        tmp = LIB_PATH + f".tmp{os.getpid()}"
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

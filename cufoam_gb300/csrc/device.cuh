@@ -1,0 +1,259 @@
+// device.cuh -- device building blocks shared by the solver kernels:
+//   * the reference's reduction tree (gis/SparseSystem/kernels.h:153-199)
+//     and a single-pass "last block finishes" grid reduction,
+//   * warp-staged CSR row products with the reference's 8-lane summation
+//     order (gis/SparseSystem/kernels.h:206-237).
+#pragma once
+
+#include "internal.h"
+
+namespace cf {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// Iterate this thread's rows in the reference's grid-stride order: thread
+// s = block*256 + tid handles rows s, s + G*256, ...  All lanes of a warp
+// iterate together (chunk base is warp-uniform), which the staging needs.
+#define CF_FOR_CHUNKS(base, n)                                                   \
+    for (int base = blockIdx.x * kBlock + (threadIdx.x & ~31); base < (n);      \
+         base += gridDim.x * kBlock)
+
+// Grid-stride over single elements with the same thread->index mapping.
+#define CF_FOR_ELEMS(i, n)                                                        \
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < (n); i += gridDim.x * kBlock)
+
+template <class T> __device__ __forceinline__ T ld_cg(const T *p) { return __ldcg(p); }
+
+// Block tree over NV per-thread values in the reference's order: strides
+// 128 and 64 through shared memory, then 32..1 inside warp 0 (the shuffle
+// tree adds lane i+s into lane i exactly like the warp-synchronous steps).
+// Result valid in thread 0.
+template <int NV, class T>
+__device__ __forceinline__ void block_tree(T (&v)[NV], T *sm)
+{
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) sm[i * kBlock + tid] = v[i];
+    __syncthreads();
+    if (tid < 128) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) sm[i * kBlock + tid] = sm[i * kBlock + tid] + sm[i * kBlock + tid + 128];
+    }
+    __syncthreads();
+    if (tid < 64) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) sm[i * kBlock + tid] = sm[i * kBlock + tid] + sm[i * kBlock + tid + 64];
+    }
+    __syncthreads();
+    if (tid < 32) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            T x = sm[i * kBlock + tid] + sm[i * kBlock + tid + 32];
+            x = x + __shfl_down_sync(kFull, x, 16);
+            x = x + __shfl_down_sync(kFull, x, 8);
+            x = x + __shfl_down_sync(kFull, x, 4);
+            x = x + __shfl_down_sync(kFull, x, 2);
+            x = x + __shfl_down_sync(kFull, x, 1);
+            v[i] = x;
+        }
+    }
+}
+
+// Single-pass grid reduction.  Every block publishes its NV partials; the
+// block that arrives last sums them in a fixed order (sequentially in block
+// order for the reference order, else a strided sum + block tree), so the
+// result is deterministic.  Returns true in the last block, where `out`
+// holds the totals (in thread 0).  The arrival counter is reset for the
+// next launch.  No block ever waits for another.
+template <int NV, class T>
+__device__ __forceinline__ bool grid_reduce(T (&acc)[NV], T *partials, int stride,
+                                            uint32_t *counter, bool ref_order, T (&out)[NV])
+{
+    __shared__ T sm[NV * kBlock];
+    __shared__ bool s_last;
+    block_tree<NV, T>(acc, sm);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) partials[i * stride + blockIdx.x] = acc[i];
+        __threadfence();
+        const uint32_t ticket = atomicAdd(counter, 1u);
+        s_last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    const int G = gridDim.x;
+    if (ref_order) {
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int i = 0; i < NV; ++i) {
+                T s = T(0);
+                for (int b = 0; b < G; ++b) s += ld_cg(partials + i * stride + b);
+                out[i] = s;
+            }
+        }
+    } else {
+        T v[NV];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            T s = T(0);
+            for (int b = threadIdx.x; b < G; b += kBlock) s += ld_cg(partials + i * stride + b);
+            v[i] = s;
+        }
+        __syncthreads();
+        block_tree<NV, T>(v, sm);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int i = 0; i < NV; ++i) out[i] = v[i];
+        }
+    }
+    if (threadIdx.x == 0) *counter = 0u;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// CSR row products
+// ---------------------------------------------------------------------------
+// Per-warp staging area in dynamic shared memory: values, then columns.
+template <class V>
+__host__ __device__ __forceinline__ size_t stage_bytes_per_warp(int cap)
+{
+    return (size_t)(cap + 8) * sizeof(V) + (size_t)(cap + 8) * sizeof(int32_t);
+}
+
+template <class V>
+struct Chunk {
+    int rs, re;        // this lane's row [rs, re)
+    int ov, oc;        // staging origins (element index of slot 0); -1 = not staged
+    const V *sv;
+    const int32_t *sc;
+};
+
+// Load the CSR entries of rows [base, base+32) into this warp's staging area
+// with 16-byte vector loads (fully coalesced), or leave them in global
+// memory when the chunk does not fit.  The arrays must be readable 16 bytes
+// past nnz (the matrix allocations are padded).
+template <class V>
+__device__ __forceinline__ Chunk<V> stage_chunk(const int32_t *__restrict__ ro,
+                                                const int32_t *__restrict__ col,
+                                                const V *__restrict__ val, int n, int base,
+                                                int cap, V *sv, int32_t *sc)
+{
+    const int lane = threadIdx.x & 31;
+    const int row = base + lane;
+    Chunk<V> c;
+    c.rs = __ldg(ro + (row < n ? row : n));
+    int nxt = __shfl_down_sync(kFull, c.rs, 1);
+    const int last = __ldg(ro + (base + 32 < n ? base + 32 : n));
+    c.re = (lane == 31) ? last : nxt;
+    const int eb = __shfl_sync(kFull, c.rs, 0);
+    const int ee = last;
+    c.sv = sv;
+    c.sc = sc;
+    if (cap <= 0 || ee - eb > cap) {
+        c.ov = -1;
+        c.oc = -1;
+        return c;
+    }
+    constexpr int VPER = 16 / sizeof(V);
+    const int av = eb & ~(VPER - 1);
+    for (int i = av + lane * VPER; i < ee; i += 32 * VPER) {
+        if (sizeof(V) == 8) {
+            const double2 t = __ldg(reinterpret_cast<const double2 *>(val + i));
+            double *d = reinterpret_cast<double *>(sv) + (i - av);
+            d[0] = t.x;
+            d[1] = t.y;
+        } else {
+            const float4 t = __ldg(reinterpret_cast<const float4 *>(val + i));
+            float *d = reinterpret_cast<float *>(sv) + (i - av);
+            d[0] = t.x;
+            d[1] = t.y;
+            d[2] = t.z;
+            d[3] = t.w;
+        }
+    }
+    const int ac = eb & ~3;
+    for (int i = ac + lane * 4; i < ee; i += 128) {
+        const int4 t = __ldg(reinterpret_cast<const int4 *>(col + i));
+        int32_t *d = sc + (i - ac);
+        d[0] = t.x;
+        d[1] = t.y;
+        d[2] = t.z;
+        d[3] = t.w;
+    }
+    __syncwarp();
+    c.ov = av;
+    c.oc = ac;
+    return c;
+}
+
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+__device__ __forceinline__ double add_t(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_t(float a, float b) { return __fadd_rn(a, b); }
+
+// ((t0+t4)+(t2+t6)) + ((t1+t5)+(t3+t7)): the reference's 8-lane tree
+template <class V>
+__device__ __forceinline__ V tree8(const V (&t)[8])
+{
+    return add_t(add_t(add_t(t[0], t[4]), add_t(t[2], t[6])), add_t(add_t(t[1], t[5]), add_t(t[3], t[7])));
+}
+
+// sum_j a_ij * g(j) for this lane's row in the reference's order: lane l of
+// 8 accumulates entries rs+l, rs+l+8, ... with FMA, then
+// ((t0+t4)+(t2+t6)) + ((t1+t5)+(t3+t7)).
+template <class V, class G>
+__device__ __forceinline__ V row_product(const Chunk<V> &c, const int32_t *__restrict__ col,
+                                         const V *__restrict__ val, G g)
+{
+    V t[8];
+    if (c.ov >= 0) {
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+            V acc = V(0);
+            for (int j = c.rs + l; j < c.re; j += 8) acc = fma_t(c.sv[j - c.ov], g(c.sc[j - c.oc]), acc);
+            t[l] = acc;
+        }
+    } else {
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+            V acc = V(0);
+            for (int j = c.rs + l; j < c.re; j += 8) acc = fma_t(__ldg(val + j), g(__ldg(col + j)), acc);
+            t[l] = acc;
+        }
+    }
+    return tree8(t);
+}
+
+// Two products over the same pattern (A and A^T values share row_offsets
+// and column indices for LDU matrices): the column index is read once.
+template <class V, class G1, class G2>
+__device__ __forceinline__ void row_product2(const Chunk<V> &c, const int32_t *__restrict__ col,
+                                             const V *__restrict__ val1, const V *__restrict__ val2,
+                                             G1 g1, G2 g2, V &y1, V &y2)
+{
+    V t[8], u[8];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+        V a1 = V(0), a2 = V(0);
+        for (int j = c.rs + l; j < c.re; j += 8) {
+            const int cc = (c.oc >= 0) ? c.sc[j - c.oc] : __ldg(col + j);
+            const V v1 = (c.ov >= 0) ? c.sv[j - c.ov] : __ldg(val1 + j);
+            a1 = fma_t(v1, g1(cc), a1);
+            a2 = fma_t(__ldg(val2 + j), g2(cc), a2);
+        }
+        t[l] = a1;
+        u[l] = a2;
+    }
+    y1 = tree8(t);
+    y2 = tree8(u);
+}
+
+// Finish a device-driven loop iteration: set the graph's while condition.
+__device__ __forceinline__ void set_loop_condition(const SolveArgs *a, bool cont)
+{
+    if (a->use_cond) cudaGraphSetConditional(a->cond, cont ? 1u : 0u);
+}
+
+} // namespace cf

@@ -1,0 +1,235 @@
+// internal.h -- host/device structures shared by the library's translation
+// units.  Nothing here is part of the C ABI (include/cufoam_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "cufoam_gb300.h"
+
+namespace cf {
+
+// ---------------------------------------------------------------------------
+// errors: thrown inside the library, turned into cf_status at the C ABI
+// ---------------------------------------------------------------------------
+struct Error {
+    cf_status status;
+    std::string msg;
+};
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char *what, const char *file, int line);
+
+#define CF_CUDA(call)                                                   \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) ::cf::throw_cuda(e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define CF_CHECK_LAUNCH() CF_CUDA(cudaGetLastError())
+
+inline void require(bool ok, cf_status st, const std::string &msg)
+{
+    if (!ok) throw Error{st, msg};
+}
+
+// ---------------------------------------------------------------------------
+// device-side solver state (one per context, reused by every solve)
+// ---------------------------------------------------------------------------
+struct DevState {
+    double rho0, rho1;   // CG / BiCG inner products
+    double xi;           // CG / BiCG step length
+    double theta;        // BiCG direction update factor
+    double omega;        // MR / MRJacobi / JMR / MRS step, Richardson relaxation
+    double norm;         // latest ||r||_2 as recorded by the reference
+    double norm0;        // initial ||r||_2
+    double tol;          // absolute stopping threshold (tolerance * normFactor)
+    double tolerance;    // relative tolerance as given (tolerance_)
+    double rel_tol;      // relTol_ (0 = off)
+    double nf;           // normFactor
+    double int_bound;    // BiCG breakdown bound
+    double pow_inv;      // power method: 1 / ||x2||
+    double lambda_max;   // power method eigenvalue estimate
+    double diag_abs_min; // min |a_ii|
+    double xbar;         // normFactor: mean of psi
+    double scale;        // mixed: residual scaling
+    int32_t k;           // completed iterations
+    int32_t done;        // loop finished
+    int32_t status;      // cf_status of the loop
+    int32_t max_steps;   // iteration limit (INT_MAX when unlimited)
+    int32_t min_steps;   // minIter_
+    int32_t x_pending;   // CG/BiCG: x += xi * p not yet applied
+    int32_t hist_cap;    // capacity of the device history
+    int32_t body_count;  // loop-guard counter (device-driven loops)
+    int32_t pow_step;    // power method step counter
+    int32_t flags;
+    uint32_t counters[16];
+};
+
+enum CounterSlot {
+    SLOT_A = 0, SLOT_B, SLOT_C, SLOT_D, SLOT_NF1, SLOT_NF2, SLOT_INIT, SLOT_POW, SLOT_MISC
+};
+
+constexpr int kMaxNV = 3;       // reductions per kernel
+constexpr int kBlock = 256;     // threads per block (the reference's BLOCK_SIZE)
+constexpr int kWarps = kBlock / 32;
+
+// Everything a solver kernel needs, resident in device memory so that one
+// instantiated CUDA graph serves any matrix and any vectors.
+struct SolveArgs {
+    // matrix (CSR produced by ldu2csr; valT = A^T values on the same pattern)
+    int32_t n;
+    int32_t stage_cap;         // staged nnz per warp (0 = no staging)
+    const int32_t *ro;
+    const int32_t *col;
+    const double *val;
+    const double *valT;
+    const float *val32;
+    const float *valT32;
+    const double *diag;        // a_ii
+    const double *dinv;        // 1 / a_ii
+    const double *dinv_sqrt;   // sqrt(1 / a_ii)
+    // vectors (FP64)
+    double *x;                 // psi (in/out)
+    const double *b;           // source
+    double *r[2];
+    double *p[2];
+    double *q;
+    double *rs;
+    double *ps[2];
+    double *qs;
+    double *w[2];
+    // vectors (FP32, mixed precision inner solve)
+    float *fx, *fr, *fp[2], *fq, *frs, *fps[2], *fqs, *fb;
+    // reductions / state
+    double *partials;          // [kMaxNV][partial_stride]
+    float *partials32;
+    int32_t partial_stride;
+    int32_t ref_order;         // reduce in the reference's order
+    DevState *st;
+    DevState *st_in;           // inner (FP32) solve of the mixed-precision loop
+    double *hist;
+    unsigned long long cond;   // cudaGraphConditionalHandle of the running loop
+    int32_t use_cond;
+    int32_t power_steps;       // Richardson: power-method steps
+    const volatile int32_t *abort_flag; // host-mapped flag: stop the loop (time limit)
+};
+
+// ---------------------------------------------------------------------------
+// host objects
+// ---------------------------------------------------------------------------
+struct DeviceBuffer {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    void ensure(size_t nbytes);   // grow-only
+    void release();
+    ~DeviceBuffer() { release(); }
+    template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+struct GraphKey {
+    int solver, precision, reduction, stage_cap, phase;
+    bool operator<(const GraphKey &o) const
+    {
+        return std::tie(solver, precision, reduction, stage_cap, phase) <
+               std::tie(o.solver, o.precision, o.reduction, o.stage_cap, o.phase);
+    }
+};
+
+struct GraphEntry {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long cond = 0;
+};
+
+struct Context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    int max_threads_sm = 0;
+    int ref_grid = 0;          // the reference's LaunchConfig grid on this GPU
+    size_t l2_bytes = 0;
+    std::string last_error;
+    bool graphs_ok = true;
+
+    // workspace (grow-only, reused by every solve)
+    DeviceBuffer vec[24];
+    DeviceBuffer partials, partials32, hist, state, state_in, args;
+    SolveArgs *h_args = nullptr;   // pinned
+    DevState *h_state = nullptr;   // pinned
+    DevState *h_state_in = nullptr; // pinned
+    int32_t *h_abort = nullptr;    // pinned, mapped
+    int32_t *d_abort = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ev_mid = nullptr;
+    std::vector<cudaEvent_t> prof_events;
+    std::map<GraphKey, GraphEntry> graphs;
+
+    int fast_grid(const void *kernel, size_t dyn_smem) const;
+    ~Context();
+};
+
+struct Matrix {
+    Context *ctx = nullptr;
+    int32_t n = 0, nf = 0;
+    int64_t nnz = 0;
+    int32_t max_chunk = 0;     // max nnz over 32-row chunks
+    // CSR (reference layout) + transpose values on the same pattern
+    DeviceBuffer ro, col, val, valT, val32, valT32;
+    // LDU copy (for value updates, the transpose and adjoint scatter)
+    DeviceBuffer diag, lower, upper, la, ua, losort, lstart, ostart;
+    DeviceBuffer dinv, dinv_sqrt;
+    bool have_valT = false, have_32 = false, have_T32 = false;
+    double diag_abs_min = 0.0;
+    bool have_dmin = false;
+};
+
+// ---------------------------------------------------------------------------
+// entry points between translation units
+// ---------------------------------------------------------------------------
+Context *context_create(int device);
+void context_bind(Context *ctx);
+void upload(Context *ctx, void *dst, const void *src, size_t bytes, int memory);
+void download(Context *ctx, void *dst, const void *src, size_t bytes, int memory);
+
+Matrix *matrix_create(Context *ctx, const cf_ldu_view &v);
+void matrix_update_values(Matrix *m, const double *diag, const double *lower,
+                          const double *upper, int memory);
+void matrix_ensure_transpose(Matrix *m);
+void matrix_ensure_fp32(Matrix *m, bool transpose);
+void matrix_ensure_dmin(Matrix *m);
+void ldu2csr_into(Context *ctx, const cf_ldu_view &v, int32_t *ro, int32_t *col,
+                  double *val, int memory);
+
+int stage_cap_for(const Matrix *m);
+void spmv(Matrix *m, bool transpose, const double *x, double *y);
+double norm_factor(Matrix *m, const double *b, const double *x, int norm_type, bool ref_order);
+void solve(Matrix *m, int solver, const cf_controls &c, const double *b, double *x,
+           cf_perf *perf);
+
+struct Batch;
+Batch *batch_create(Context *ctx, int n_systems, const cf_ldu_view *views);
+void batch_destroy(Batch *B);
+void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, double *x_io,
+                 int memory, const cf_batch_config *cfg, cf_batch_result *results, float *ms_out);
+int64_t batch_rows(const Batch *B);
+int batch_systems(const Batch *B);
+int64_t batch_offset(const Batch *B, int s);
+
+void adjoint_gradients(Matrix *m, const double *lam, const double *x, double *d_diag,
+                       double *d_lower, double *d_upper);
+
+struct MixedResult {
+    int inner_iterations = 0;
+    int outer = 0;
+    int status = CF_OK;
+};
+bool mixed_supported(int solver);
+void mixed_prepare(Context *ctx, Matrix *m, int solver, SolveArgs &A);
+MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c, SolveArgs *d_args,
+                      int cap, bool use_graph);
+
+} // namespace cf

@@ -1,0 +1,526 @@
+// matrix.cu -- device LDU -> CSR conversion and matrix objects.
+//
+// The CSR layout is exactly the reference's getSparseCSRMat
+// (gis/ldu2csr.h:7-40): row c = [lower coefficients of the faces whose
+// neighbour is c, in losort order] [diag c] [upper coefficients of the faces
+// owned by c, in face order].  Row offsets follow from the addressing
+// without a scan: row_offsets[c] = losortStart[c] + c + ownerStart[c]
+// (relative to the first entries), which is the reference's running count.
+#include "device.cuh"
+
+#include <cmath>
+
+namespace cf {
+
+// ---------------------------------------------------------------------------
+// addressing validation / construction
+// ---------------------------------------------------------------------------
+enum AddrError { ADDR_RANGE = 1, ADDR_ORDER = 2, ADDR_START = 4, ADDR_COUNT = 8 };
+
+__global__ void k_check_faces(int n, int nf, const int32_t *__restrict__ la,
+                              const int32_t *__restrict__ ua, int *err)
+{
+    CF_FOR_ELEMS(f, nf) {
+        const int o = la[f], u = ua[f];
+        if (o < 0 || o >= n || u < 0 || u >= n) atomicOr(err, ADDR_RANGE);
+        else if (u <= o) atomicOr(err, ADDR_ORDER);
+        if (f > 0 && la[f - 1] > o) atomicOr(err, ADDR_ORDER);
+    }
+}
+
+// Caller-provided losort/losortStart/ownerStart: ranges and monotonicity.
+__global__ void k_check_given(int n, int nf, const int32_t *__restrict__ losort,
+                              const int32_t *__restrict__ ls, const int32_t *__restrict__ os,
+                              int *err)
+{
+    CF_FOR_ELEMS(i, nf) {
+        if (losort[i] < 0 || losort[i] >= nf) atomicOr(err, ADDR_RANGE);
+    }
+    CF_FOR_ELEMS(c, n + 1) {
+        if (ls[c] < 0 || ls[c] > nf || os[c] < 0 || os[c] > nf) atomicOr(err, ADDR_START);
+        if (c < n && (ls[c + 1] < ls[c] || os[c + 1] < os[c])) atomicOr(err, ADDR_START);
+    }
+}
+
+// ownerStart[c] = first face whose owner is >= c (faces sorted by owner).
+__global__ void k_owner_start(int n, int nf, const int32_t *__restrict__ la, int32_t *os)
+{
+    CF_FOR_ELEMS(c, n + 1) {
+        int lo = 0, hi = nf;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(la + mid) < c) lo = mid + 1;
+            else hi = mid;
+        }
+        os[c] = lo;
+    }
+}
+
+__global__ void k_count_neighbours(int nf, const int32_t *__restrict__ ua, int32_t *cnt)
+{
+    CF_FOR_ELEMS(f, nf) atomicAdd(cnt + ua[f], 1);
+}
+
+// Exclusive scan of m int32 values, three kernels: per-block inclusive scan
+// with block totals, a single-block scan of the totals, then the fix-up.
+constexpr int kScanBlock = 1024;
+
+__device__ __forceinline__ int block_inclusive_scan(int v, int *sm)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) sm[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        int w = (lane < (int)(blockDim.x >> 5)) ? sm[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, w, o);
+            if (lane >= o) w += t;
+        }
+        sm[lane] = w;
+    }
+    __syncthreads();
+    if (warp > 0) v += sm[warp - 1];
+    __syncthreads();
+    return v;
+}
+
+__global__ void k_scan_blocks(int m, const int32_t *__restrict__ in, int32_t *out, int32_t *sums)
+{
+    __shared__ int sm[32];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const int v = (i < m) ? in[i] : 0;
+    const int inc = block_inclusive_scan(v, sm);
+    if (i < m) out[i] = inc - v; // exclusive within the block
+    if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = inc;
+}
+
+__global__ void k_scan_sums(int nb, int32_t *sums)
+{
+    __shared__ int sm[32];
+    const int per = (nb + kScanBlock - 1) / kScanBlock;
+    const int b0 = threadIdx.x * per;
+    int local = 0;
+    for (int j = 0; j < per && b0 + j < nb; ++j) local += sums[b0 + j];
+    const int inc = block_inclusive_scan(local, sm);
+    int run = inc - local;
+    for (int j = 0; j < per && b0 + j < nb; ++j) {
+        const int t = sums[b0 + j];
+        sums[b0 + j] = run;
+        run += t;
+    }
+}
+
+__global__ void k_scan_add(int m, int32_t *out, const int32_t *__restrict__ sums)
+{
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < m) out[i] += sums[blockIdx.x];
+}
+
+// Place every face in its neighbour's losort segment (arbitrary order inside
+// the segment), then sort each segment by face index: the result is the
+// stable order of OpenFOAM's losort.
+__global__ void k_losort_place(int nf, const int32_t *__restrict__ ua,
+                               const int32_t *__restrict__ ls, int32_t *cursor, int32_t *losort)
+{
+    CF_FOR_ELEMS(f, nf) {
+        const int u = ua[f];
+        const int pos = ls[u] + atomicAdd(cursor + u, 1);
+        losort[pos] = f;
+    }
+}
+
+__global__ void k_losort_sort(int n, const int32_t *__restrict__ ls, int32_t *losort)
+{
+    CF_FOR_ELEMS(c, n) {
+        const int b = ls[c], e = ls[c + 1];
+        for (int i = b + 1; i < e; ++i) {
+            const int v = losort[i];
+            int j = i - 1;
+            while (j >= b && losort[j] > v) {
+                losort[j + 1] = losort[j];
+                --j;
+            }
+            losort[j + 1] = v;
+        }
+    }
+}
+
+__global__ void k_row_offsets(int n, const int32_t *__restrict__ ls, const int32_t *__restrict__ os,
+                              int32_t *ro)
+{
+    const int l0 = ls[0], o0 = os[0];
+    CF_FOR_ELEMS(c, n + 1) ro[c] = (ls[c] - l0) + c + (os[c] - o0);
+}
+
+// One thread per cell, in the reference's entry order.  `col` may be null
+// (value-only refresh); `lower`/`upper` swapped gives A^T on the same
+// pattern (faces are structurally symmetric).
+__global__ void k_fill_csr(int n, const int32_t *__restrict__ ls, const int32_t *__restrict__ os,
+                           const int32_t *__restrict__ losort, const int32_t *__restrict__ la,
+                           const int32_t *__restrict__ ua, const double *__restrict__ diag,
+                           const double *__restrict__ lower, const double *__restrict__ upper,
+                           const int32_t *__restrict__ ro, int32_t *col, double *val)
+{
+    CF_FOR_ELEMS(c, n) {
+        int e = ro[c];
+        for (int idx = ls[c]; idx < ls[c + 1]; ++idx) {
+            const int face = losort[idx];
+            if (col) col[e] = la[face];
+            val[e] = lower[face];
+            ++e;
+        }
+        if (col) col[e] = c;
+        val[e] = diag[c];
+        ++e;
+        for (int face = os[c]; face < os[c + 1]; ++face) {
+            if (col) col[e] = ua[face];
+            val[e] = upper[face];
+            ++e;
+        }
+    }
+}
+
+__global__ void k_max_chunk(int n, const int32_t *__restrict__ ro, int *out)
+{
+    int m = 0;
+    for (int base = (blockIdx.x * blockDim.x + threadIdx.x) * 32; base < n;
+         base += gridDim.x * blockDim.x * 32) {
+        const int top = base + 32 < n ? base + 32 : n;
+        const int c = ro[top] - ro[base];
+        m = c > m ? c : m;
+    }
+    atomicMax(out, m);
+}
+
+__global__ void k_diag_derived(int n, const double *__restrict__ diag, double *dinv,
+                               double *dinv_sqrt)
+{
+    // FindDiagInv / FindDiagInvSqrt (gis/SparseSystem/kernels.h:563-603)
+    CF_FOR_ELEMS(c, n) {
+        const double inv = 1.0 / diag[c];
+        dinv[c] = inv;
+        dinv_sqrt[c] = sqrt(inv);
+    }
+}
+
+__global__ void k_to_f32(int64_t m, const double *__restrict__ src, float *dst)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+         i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+
+__global__ void k_min_abs(int n, const double *__restrict__ v, double *out_bits_as_u64)
+{
+    // min |v| (order independent); non-negative doubles order like their bits
+    double m = INFINITY;
+    CF_FOR_ELEMS(i, n) m = fmin(m, fabs(v[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_down_sync(kFull, m, o));
+    if ((threadIdx.x & 31) == 0)
+        atomicMin(reinterpret_cast<unsigned long long *>(out_bits_as_u64),
+                  (unsigned long long)__double_as_longlong(m));
+}
+
+// Plain y = A x with the reference's row order (SpMv, SolverSingleGPU.h:173-184).
+__global__ void __launch_bounds__(kBlock) k_spmv(int n, int cap, const int32_t *__restrict__ ro,
+                                                 const int32_t *__restrict__ col,
+                                                 const double *__restrict__ val,
+                                                 const double *__restrict__ x, double *y)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5;
+    unsigned char *area = smem + warp * stage_bytes_per_warp<double>(cap);
+    double *sv = reinterpret_cast<double *>(area);
+    int32_t *sc = reinterpret_cast<int32_t *>(area + (size_t)(cap + 8) * sizeof(double));
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv, sc);
+        const int row = base + (threadIdx.x & 31);
+        const double v = row_product<double>(ch, col, val, [&](int c) { return __ldg(x + c); });
+        if (row < n) y[row] = v;
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static int grid_for(Context *ctx, int64_t work, int per_block = kBlock)
+{
+    int64_t g = (work + per_block - 1) / per_block;
+    const int64_t cap = (int64_t)ctx->sm_count * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+static void exclusive_scan(Context *ctx, int m, const int32_t *in, int32_t *out, DeviceBuffer &tmp)
+{
+    const int nb = (m + kScanBlock - 1) / kScanBlock;
+    tmp.ensure(sizeof(int32_t) * (size_t)(nb + 1));
+    k_scan_blocks<<<nb, kScanBlock, 0, ctx->stream>>>(m, in, out, tmp.as<int32_t>());
+    CF_CHECK_LAUNCH();
+    k_scan_sums<<<1, kScanBlock, 0, ctx->stream>>>(nb, tmp.as<int32_t>());
+    CF_CHECK_LAUNCH();
+    k_scan_add<<<nb, kScanBlock, 0, ctx->stream>>>(m, out, tmp.as<int32_t>());
+    CF_CHECK_LAUNCH();
+}
+
+static int read_flag(Context *ctx, const int *d_flag)
+{
+    int h = 0;
+    CF_CUDA(cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return h;
+}
+
+// Copies the LDU arrays to `m`, validates and completes the addressing,
+// builds the CSR.  When `out_*` are given the CSR is written there instead.
+static void build_from_ldu(Context *ctx, Matrix *m, const cf_ldu_view &v)
+{
+    const int n = v.n_cells, nf = v.n_faces;
+    require(n >= 0 && nf >= 0, CF_BAD_INPUT, "negative matrix size");
+    require((int64_t)n + 2 * (int64_t)nf < (int64_t)INT32_MAX - 16, CF_BAD_INPUT,
+            "matrix too large for 32-bit CSR offsets");
+    require(n == 0 || v.diag, CF_BAD_INPUT, "diag is null");
+    require(nf == 0 || (v.lower && v.upper && v.lower_addr && v.upper_addr), CF_BAD_INPUT,
+            "face arrays are null");
+    const bool given = v.losort || v.losort_start || v.owner_start;
+    require(!given || (v.losort && v.losort_start && v.owner_start), CF_BAD_INPUT,
+            "losort, losort_start and owner_start must be given together");
+    m->n = n;
+    m->nf = nf;
+    m->nnz = (int64_t)n + 2 * (int64_t)nf;
+    const size_t pad = 4;
+    m->diag.ensure(sizeof(double) * (n + pad));
+    m->lower.ensure(sizeof(double) * (nf + pad));
+    m->upper.ensure(sizeof(double) * (nf + pad));
+    m->la.ensure(sizeof(int32_t) * (nf + pad));
+    m->ua.ensure(sizeof(int32_t) * (nf + pad));
+    m->losort.ensure(sizeof(int32_t) * (nf + pad));
+    m->lstart.ensure(sizeof(int32_t) * (n + 1 + pad));
+    m->ostart.ensure(sizeof(int32_t) * (n + 1 + pad));
+    upload(ctx, m->diag.ptr, v.diag, sizeof(double) * n, v.memory);
+    upload(ctx, m->lower.ptr, v.lower, sizeof(double) * nf, v.memory);
+    upload(ctx, m->upper.ptr, v.upper, sizeof(double) * nf, v.memory);
+    upload(ctx, m->la.ptr, v.lower_addr, sizeof(int32_t) * nf, v.memory);
+    upload(ctx, m->ua.ptr, v.upper_addr, sizeof(int32_t) * nf, v.memory);
+
+    DeviceBuffer flag, tmp, cnt;
+    flag.ensure(sizeof(int) * 4);
+    CF_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int) * 4, ctx->stream));
+    int *d_err = flag.as<int>();
+    const int gf = grid_for(ctx, nf > 0 ? nf : 1);
+    const int gc = grid_for(ctx, (int64_t)n + 1);
+    if (nf > 0) {
+        k_check_faces<<<gf, kBlock, 0, ctx->stream>>>(n, nf, m->la.as<int32_t>(), m->ua.as<int32_t>(), d_err);
+        CF_CHECK_LAUNCH();
+    }
+    if (given) {
+        upload(ctx, m->losort.ptr, v.losort, sizeof(int32_t) * nf, v.memory);
+        upload(ctx, m->lstart.ptr, v.losort_start, sizeof(int32_t) * (n + 1), v.memory);
+        upload(ctx, m->ostart.ptr, v.owner_start, sizeof(int32_t) * (n + 1), v.memory);
+        k_check_given<<<gc, kBlock, 0, ctx->stream>>>(n, nf, m->losort.as<int32_t>(),
+                                                      m->lstart.as<int32_t>(), m->ostart.as<int32_t>(), d_err);
+        CF_CHECK_LAUNCH();
+    } else {
+        k_owner_start<<<gc, kBlock, 0, ctx->stream>>>(n, nf, m->la.as<int32_t>(), m->ostart.as<int32_t>());
+        CF_CHECK_LAUNCH();
+    }
+    int err = read_flag(ctx, d_err);
+    require(err == 0, CF_BAD_INPUT,
+            std::string("invalid LDU addressing:") + ((err & ADDR_RANGE) ? " index out of range" : "") +
+                ((err & ADDR_ORDER) ? " faces not sorted by owner or not upper-triangular" : "") +
+                ((err & ADDR_START) ? " bad losortStart/ownerStart" : ""));
+    if (!given) {
+        cnt.ensure(sizeof(int32_t) * (size_t)(n + 1));
+        CF_CUDA(cudaMemsetAsync(cnt.ptr, 0, sizeof(int32_t) * (size_t)(n + 1), ctx->stream));
+        if (nf > 0) {
+            k_count_neighbours<<<gf, kBlock, 0, ctx->stream>>>(nf, m->ua.as<int32_t>(), cnt.as<int32_t>());
+            CF_CHECK_LAUNCH();
+        }
+        exclusive_scan(ctx, n + 1, cnt.as<int32_t>(), m->lstart.as<int32_t>(), tmp);
+        CF_CUDA(cudaMemsetAsync(cnt.ptr, 0, sizeof(int32_t) * (size_t)(n + 1), ctx->stream));
+        if (nf > 0) {
+            k_losort_place<<<gf, kBlock, 0, ctx->stream>>>(nf, m->ua.as<int32_t>(), m->lstart.as<int32_t>(),
+                                                           cnt.as<int32_t>(), m->losort.as<int32_t>());
+            CF_CHECK_LAUNCH();
+            k_losort_sort<<<gc, kBlock, 0, ctx->stream>>>(n, m->lstart.as<int32_t>(), m->losort.as<int32_t>());
+            CF_CHECK_LAUNCH();
+        }
+    }
+    m->ro.ensure(sizeof(int32_t) * (n + 1 + pad));
+    k_row_offsets<<<gc, kBlock, 0, ctx->stream>>>(n, m->lstart.as<int32_t>(), m->ostart.as<int32_t>(),
+                                                   m->ro.as<int32_t>());
+    CF_CHECK_LAUNCH();
+    // the counts must describe exactly n + 2F entries
+    int32_t last = 0;
+    CF_CUDA(cudaMemcpyAsync(&last, m->ro.as<int32_t>() + n, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    CF_CUDA(cudaStreamSynchronize(ctx->stream));
+    require((int64_t)last == m->nnz, CF_BAD_INPUT,
+            "losortStart/ownerStart do not describe n + 2*nFaces entries");
+    m->col.ensure(sizeof(int32_t) * (m->nnz + pad));
+    m->val.ensure(sizeof(double) * (m->nnz + pad));
+    // zero the padding read by 16-byte vector loads past nnz
+    CF_CUDA(cudaMemsetAsync(m->col.as<int32_t>() + m->nnz, 0, sizeof(int32_t) * pad, ctx->stream));
+    CF_CUDA(cudaMemsetAsync(m->val.as<double>() + m->nnz, 0, sizeof(double) * pad, ctx->stream));
+    if (n > 0) {
+        k_fill_csr<<<gc, kBlock, 0, ctx->stream>>>(n, m->lstart.as<int32_t>(), m->ostart.as<int32_t>(),
+                                                   m->losort.as<int32_t>(), m->la.as<int32_t>(),
+                                                   m->ua.as<int32_t>(), m->diag.as<double>(),
+                                                   m->lower.as<double>(), m->upper.as<double>(),
+                                                   m->ro.as<int32_t>(), m->col.as<int32_t>(),
+                                                   m->val.as<double>());
+        CF_CHECK_LAUNCH();
+    }
+    // staging capacity: max nnz over 32-row chunks
+    CF_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
+    if (n > 0) {
+        k_max_chunk<<<grid_for(ctx, (n + 31) / 32), kBlock, 0, ctx->stream>>>(n, m->ro.as<int32_t>(), d_err);
+        CF_CHECK_LAUNCH();
+    }
+    m->max_chunk = read_flag(ctx, d_err);
+    m->dinv.ensure(sizeof(double) * (n + pad));
+    m->dinv_sqrt.ensure(sizeof(double) * (n + pad));
+    if (n > 0) {
+        k_diag_derived<<<gc, kBlock, 0, ctx->stream>>>(n, m->diag.as<double>(), m->dinv.as<double>(),
+                                                       m->dinv_sqrt.as<double>());
+        CF_CHECK_LAUNCH();
+    }
+    m->have_valT = m->have_32 = m->have_T32 = m->have_dmin = false;
+}
+
+Matrix *matrix_create(Context *ctx, const cf_ldu_view &v)
+{
+    Matrix *m = new Matrix();
+    m->ctx = ctx;
+    try {
+        build_from_ldu(ctx, m, v);
+    } catch (...) {
+        delete m;
+        throw;
+    }
+    return m;
+}
+
+void matrix_update_values(Matrix *m, const double *diag, const double *lower, const double *upper,
+                          int memory)
+{
+    Context *ctx = m->ctx;
+    require(diag && (m->nf == 0 || (lower && upper)), CF_BAD_INPUT, "null coefficient array");
+    upload(ctx, m->diag.ptr, diag, sizeof(double) * m->n, memory);
+    upload(ctx, m->lower.ptr, lower, sizeof(double) * m->nf, memory);
+    upload(ctx, m->upper.ptr, upper, sizeof(double) * m->nf, memory);
+    const int gc = grid_for(ctx, (int64_t)m->n + 1);
+    if (m->n > 0) {
+        k_fill_csr<<<gc, kBlock, 0, ctx->stream>>>(m->n, m->lstart.as<int32_t>(), m->ostart.as<int32_t>(),
+                                                   m->losort.as<int32_t>(), m->la.as<int32_t>(),
+                                                   m->ua.as<int32_t>(), m->diag.as<double>(),
+                                                   m->lower.as<double>(), m->upper.as<double>(),
+                                                   m->ro.as<int32_t>(), nullptr, m->val.as<double>());
+        CF_CHECK_LAUNCH();
+        k_diag_derived<<<gc, kBlock, 0, ctx->stream>>>(m->n, m->diag.as<double>(), m->dinv.as<double>(),
+                                                       m->dinv_sqrt.as<double>());
+        CF_CHECK_LAUNCH();
+    }
+    m->have_valT = m->have_32 = m->have_T32 = m->have_dmin = false;
+}
+
+// A^T values on A's pattern: the same fill with lower and upper swapped.
+// Equals the reference's Transpose (Thrust stable sort by column,
+// SolverSingleGPU.h:33-71) because row c of A^T lists A[i][c] by ascending i.
+void matrix_ensure_transpose(Matrix *m)
+{
+    if (m->have_valT) return;
+    Context *ctx = m->ctx;
+    m->valT.ensure(sizeof(double) * (m->nnz + 4));
+    CF_CUDA(cudaMemsetAsync(m->valT.as<double>() + m->nnz, 0, sizeof(double) * 4, ctx->stream));
+    if (m->n > 0) {
+        k_fill_csr<<<grid_for(ctx, (int64_t)m->n + 1), kBlock, 0, ctx->stream>>>(
+            m->n, m->lstart.as<int32_t>(), m->ostart.as<int32_t>(), m->losort.as<int32_t>(),
+            m->la.as<int32_t>(), m->ua.as<int32_t>(), m->diag.as<double>(), m->upper.as<double>(),
+            m->lower.as<double>(), m->ro.as<int32_t>(), nullptr, m->valT.as<double>());
+        CF_CHECK_LAUNCH();
+    }
+    m->have_valT = true;
+}
+
+void matrix_ensure_fp32(Matrix *m, bool transpose)
+{
+    Context *ctx = m->ctx;
+    if (!transpose && m->have_32) return;
+    if (transpose && m->have_T32) return;
+    if (transpose) matrix_ensure_transpose(m);
+    DeviceBuffer &dst = transpose ? m->valT32 : m->val32;
+    const double *src = transpose ? m->valT.as<double>() : m->val.as<double>();
+    dst.ensure(sizeof(float) * (m->nnz + 4));
+    CF_CUDA(cudaMemsetAsync(dst.as<float>() + m->nnz, 0, sizeof(float) * 4, ctx->stream));
+    if (m->nnz > 0) {
+        k_to_f32<<<grid_for(ctx, m->nnz), kBlock, 0, ctx->stream>>>(m->nnz, src, dst.as<float>());
+        CF_CHECK_LAUNCH();
+    }
+    (transpose ? m->have_T32 : m->have_32) = true;
+}
+
+// FindDiagAbsMin (SolverSingleGPU.h:686-720): min |a_ii|.
+void matrix_ensure_dmin(Matrix *m)
+{
+    if (m->have_dmin) return;
+    Context *ctx = m->ctx;
+    DeviceBuffer b;
+    b.ensure(sizeof(double));
+    const double inf = INFINITY;
+    CF_CUDA(cudaMemcpyAsync(b.ptr, &inf, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    if (m->n > 0) {
+        k_min_abs<<<grid_for(ctx, m->n), kBlock, 0, ctx->stream>>>(m->n, m->diag.as<double>(), b.as<double>());
+        CF_CHECK_LAUNCH();
+    }
+    double h = 0;
+    CF_CUDA(cudaMemcpyAsync(&h, b.ptr, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CF_CUDA(cudaStreamSynchronize(ctx->stream));
+    m->diag_abs_min = h;
+    m->have_dmin = true;
+}
+
+void ldu2csr_into(Context *ctx, const cf_ldu_view &v, int32_t *ro, int32_t *col, double *val,
+                  int memory)
+{
+    Matrix tmp;
+    tmp.ctx = ctx;
+    build_from_ldu(ctx, &tmp, v);
+    download(ctx, ro, tmp.ro.ptr, sizeof(int32_t) * (size_t)(tmp.n + 1), memory);
+    download(ctx, col, tmp.col.ptr, sizeof(int32_t) * (size_t)tmp.nnz, memory);
+    download(ctx, val, tmp.val.ptr, sizeof(double) * (size_t)tmp.nnz, memory);
+    CF_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+int stage_cap_for(const Matrix *m)
+{
+    // stage a warp's rows when they fit a modest per-warp buffer
+    if (m->max_chunk <= 256) return 256;
+    if (m->max_chunk <= 1024) return 1024;
+    return 0;
+}
+
+void spmv(Matrix *m, bool transpose, const double *x, double *y)
+{
+    Context *ctx = m->ctx;
+    if (transpose) matrix_ensure_transpose(m);
+    if (m->n == 0) return;
+    const int cap = stage_cap_for(m);
+    const size_t smem = cap > 0 ? kWarps * stage_bytes_per_warp<double>(cap) : 0;
+    if (smem > 48 * 1024)
+        CF_CUDA(cudaFuncSetAttribute(k_spmv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int g = ctx->fast_grid((const void *)k_spmv, smem);
+    k_spmv<<<g, kBlock, smem, ctx->stream>>>(m->n, cap, m->ro.as<int32_t>(), m->col.as<int32_t>(),
+                                             transpose ? m->valT.as<double>() : m->val.as<double>(), x, y);
+    CF_CHECK_LAUNCH();
+}
+
+} // namespace cf

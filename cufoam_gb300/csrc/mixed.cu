@@ -1,0 +1,471 @@
+// mixed.cu -- mixed-precision solves: FP32 matrix values, FP32 Krylov
+// vectors and FP32 accumulation in the inner solver, inside an FP64
+// iterative-refinement loop that owns the true residual b - A x, the
+// normFactor and the stopping test.
+//
+// Outer step j:  r = b - A x (FP64);  solve A d = r / ||r|| in FP32 to a
+// relative tolerance eta (CG, BiCG or MR, same fused kernels as FP64 with
+// float data);  x += ||r|| d (FP64).  The loop stops when the FP64 residual
+// reaches tolerance * normFactor, so the answer carries the FP64 tolerance.
+// FP32 halves the bytes of every vector stream and cuts the matrix from 12
+// to 8 bytes per entry.
+#include "solver_common.cuh"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+
+namespace cf {
+
+// ---------------------------------------------------------------------------
+// FP64 pieces of the outer loop
+// ---------------------------------------------------------------------------
+// x += s * d with s = ||r|| of the residual the inner system was scaled by.
+__global__ void __launch_bounds__(kBlock) k_mx_correct(const SolveArgs *__restrict__ a)
+{
+    const int n = a->n;
+    const double s = ld_cg(&a->st->norm);
+    const float *d = a->fx;
+    double *x = a->x;
+    CF_FOR_ELEMS(i, n) x[i] = fma_t(s, (double)d[i], x[i]);
+}
+
+// r = b - A x, ||r|| (FP64); records the outer step.
+__global__ void __launch_bounds__(kBlock) k_mx_residual(const SolveArgs *__restrict__ a)
+{
+    const int n = a->n, cap = a->stage_cap;
+    CF_STAGE(double, cap);
+    const int32_t *ro = a->ro, *col = a->col;
+    const double *val = a->val, *x = a->x, *b = a->b;
+    double *r = a->r[0];
+    double acc[1] = {0.0};
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const int row = base + (threadIdx.x & 31);
+        const double t = row_product<double>(ch, col, val, [&](int c) { return x[c]; });
+        if (row < n) {
+            const double ri = b[row] - t;
+            r[row] = ri;
+            acc[0] = fma_t(ri, ri, acc[0]);
+        }
+        __syncwarp();
+    }
+    double tot[1];
+    if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &a->st->counters[SLOT_MISC],
+                               false, tot) && threadIdx.x == 0) {
+        DevState *st = a->st;
+        const double norm = sqrt(tot[0]);
+        const int k = st->k + 1; // outer steps
+        st->k = k;
+        st->norm = norm;
+        if (a->hist && k < st->hist_cap) a->hist[k] = norm;
+        if (!isfinite(norm)) {
+            st->done = 1;
+            st->status = CF_NONFINITE;
+        } else if (norm <= st->tol) {
+            st->done = 1;
+            st->status = CF_OK;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 inner solve
+// ---------------------------------------------------------------------------
+// r32 = float(r64 / ||r64||), d = 0 (, r*32 = r32 for BiCG); inner state.
+__global__ void __launch_bounds__(kBlock) k_mx_setup(const SolveArgs *__restrict__ a, int bicg)
+{
+    const int n = a->n;
+    DevState *si = a->st_in;
+    const double inv = 1.0 / ld_cg(&a->st->norm);
+    const double *r64 = a->r[0];
+    float *fr = a->fr, *fd = a->fx, *frs = a->frs;
+    float acc[1] = {0.f};
+    CF_FOR_ELEMS(i, n) {
+        const float v = (float)(r64[i] * inv);
+        fr[i] = v;
+        fd[i] = 0.f;
+        if (bicg) frs[i] = v;
+        acc[0] = fma_t(v, v, acc[0]);
+    }
+    float tot[1];
+    if (grid_reduce<1, float>(acc, a->partials32, a->partial_stride, &si->counters[SLOT_INIT], false,
+                              tot) && threadIdx.x == 0) {
+        const float rr = tot[0];
+        const double norm0 = sqrtf(rr);
+        si->rho0 = rr;
+        si->rho1 = 0.0;
+        si->norm0 = norm0;
+        si->norm = norm0;
+        si->tol = si->tolerance * norm0;
+        si->k = 0;
+        si->x_pending = 0;
+        si->body_count = 0;
+        const bool finite = isfinite(norm0);
+        bool cont = finite && si->max_steps >= 1 && (bicg || norm0 > si->tol);
+        si->done = cont ? 0 : 1;
+        si->status = finite ? CF_OK : CF_NONFINITE;
+    }
+}
+
+// CG: K1 p = r + beta p_old (on the fly), q = A32 p, (p, q); deferred d update
+__global__ void __launch_bounds__(kBlock) k_mx_cg_spmv(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st_in;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n, cap = a->stage_cap;
+    CF_STAGE(float, cap);
+    const int k = ld_cg(&st->k) + 1;
+    const bool first = (k == 1);
+    const float beta = first ? 0.f : (float)ld_cg(&st->rho0) / (float)ld_cg(&st->rho1);
+    const float xi_prev = (float)ld_cg(&st->xi);
+    const bool xpend = ld_cg(&st->x_pending) != 0;
+    const float *pin = a->fp[(k + 1) & 1];
+    float *pout = a->fp[k & 1];
+    const float *r = a->fr;
+    float *d = a->fx, *q = a->fq;
+    const int32_t *ro = a->ro, *col = a->col;
+    const float *val = a->val32;
+    auto g = [&](int c) { return first ? r[c] : fma_t(beta, pin[c], r[c]); };
+    float acc[1] = {0.f};
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<float> ch = stage_chunk<float>(ro, col, val, n, base, cap, sv_, sc_);
+        const int row = base + (threadIdx.x & 31);
+        const float y = row_product<float>(ch, col, val, g);
+        if (row < n) {
+            const float pi = g(row);
+            pout[row] = pi;
+            q[row] = y;
+            if (xpend) d[row] = fma_t(xi_prev, pin[row], d[row]);
+            acc[0] = fma_t(pi, y, acc[0]);
+        }
+        __syncwarp();
+    }
+    float tot[1];
+    if (grid_reduce<1, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
+                              tot) && threadIdx.x == 0) {
+        st->xi = (float)st->rho0 / tot[0];
+        st->x_pending = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_mx_cg_update(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st_in;
+    CF_EXIT_IF_DONE(a, st, true);
+    const int n = a->n;
+    const float xi = (float)ld_cg(&st->xi);
+    float *r = a->fr;
+    const float *q = a->fq;
+    float acc[1] = {0.f};
+    CF_FOR_ELEMS(i, n) {
+        const float ri = fma_t(-xi, q[i], r[i]);
+        r[i] = ri;
+        acc[0] = fma_t(ri, ri, acc[0]);
+    }
+    float tot[1];
+    if (grid_reduce<1, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_B], false,
+                              tot) && threadIdx.x == 0) {
+        st->rho1 = st->rho0;
+        st->rho0 = tot[0];
+        st->x_pending = 1;
+        finish_step(a, st, sqrtf(tot[0]));
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_mx_flush(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st_in;
+    if (!ld_cg(&st->x_pending)) return;
+    const int n = a->n;
+    const int k = ld_cg(&st->k);
+    const float xi = (float)ld_cg(&st->xi);
+    const float *p = a->fp[k & 1];
+    float *d = a->fx;
+    CF_FOR_ELEMS(i, n) d[i] = fma_t(xi, p[i], d[i]);
+}
+
+// BiCG: q = A32 p and q* = A32^T p* over the shared pattern
+__global__ void __launch_bounds__(kBlock) k_mx_bicg_spmv(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st_in;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n, cap = a->stage_cap;
+    CF_STAGE(float, cap);
+    const int k = ld_cg(&st->k) + 1;
+    const bool first = (k == 1);
+    const float theta = (float)ld_cg(&st->theta);
+    const float xi_prev = (float)ld_cg(&st->xi);
+    const bool xpend = ld_cg(&st->x_pending) != 0;
+    const float *pin = a->fp[(k + 1) & 1], *psin = a->fps[(k + 1) & 1];
+    float *pout = a->fp[k & 1], *psout = a->fps[k & 1];
+    const float *r = a->fr, *rs = a->frs;
+    float *d = a->fx, *q = a->fq, *qs = a->fqs;
+    const int32_t *ro = a->ro, *col = a->col;
+    const float *val = a->val32, *valT = a->valT32;
+    auto gp = [&](int c) { return first ? r[c] : fma_t(theta, pin[c], r[c]); };
+    auto gps = [&](int c) { return first ? rs[c] : fma_t(theta, psin[c], rs[c]); };
+    float acc[1] = {0.f};
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<float> ch = stage_chunk<float>(ro, col, val, n, base, cap, sv_, sc_);
+        const int row = base + (threadIdx.x & 31);
+        float y1, y2;
+        row_product2<float>(ch, col, val, valT, gp, gps, y1, y2);
+        if (row < n) {
+            const float pi = gp(row), psi = gps(row);
+            pout[row] = pi;
+            psout[row] = psi;
+            q[row] = y1;
+            qs[row] = y2;
+            if (xpend) d[row] = fma_t(xi_prev, pin[row], d[row]);
+            acc[0] = fma_t(psi, y1, acc[0]);
+        }
+        __syncwarp();
+    }
+    float tot[1];
+    if (grid_reduce<1, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
+                              tot) && threadIdx.x == 0) {
+        const float xi = (float)st->rho0 / tot[0];
+        st->x_pending = 0;
+        const double bound = st->int_bound;
+        if (!(xi > -bound && xi < bound) && isfinite(xi)) {
+            st->xi = xi;
+        } else {
+            st->done = 1;
+            st->status = isfinite(xi) ? CF_BREAKDOWN : CF_NONFINITE;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_mx_bicg_update(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st_in;
+    CF_EXIT_IF_DONE(a, st, true);
+    const int n = a->n;
+    const float xi = (float)ld_cg(&st->xi);
+    float *r = a->fr, *rs = a->frs;
+    const float *q = a->fq, *qs = a->fqs;
+    float acc[2] = {0.f, 0.f};
+    CF_FOR_ELEMS(i, n) {
+        const float ri = fma_t(-xi, q[i], r[i]);
+        const float rsi = fma_t(-xi, qs[i], rs[i]);
+        r[i] = ri;
+        rs[i] = rsi;
+        acc[0] = fma_t(ri, ri, acc[0]);
+        acc[1] = fma_t(ri, rsi, acc[1]);
+    }
+    float tot[2];
+    if (grid_reduce<2, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_B], false,
+                              tot) && threadIdx.x == 0) {
+        const double norm = sqrtf(tot[0]);
+        const int k = st->k + 1;
+        st->k = k;
+        st->norm = norm;
+        st->x_pending = 1;
+        bool cont = true;
+        int status = CF_NOT_CONVERGED;
+        if (norm < st->tol) { cont = false; status = CF_OK; }
+        else if (k >= st->max_steps) { cont = false; }
+        else if (!isfinite(norm)) { cont = false; status = CF_NONFINITE; }
+        st->body_count += 1;
+        if (st->body_count > k + 2 || (a->abort_flag && *a->abort_flag)) { cont = false; status = CF_TIMEOUT; }
+        if (cont) {
+            st->rho1 = st->rho0;
+            st->rho0 = tot[1];
+            st->theta = (float)st->rho0 / (float)st->rho1;
+        } else {
+            st->done = 1;
+            st->status = status;
+        }
+        set_loop_condition(a, cont);
+    }
+}
+
+// MR: K1 y = A32 r, (r, y), (y, y); K2 d += w r, r -= w y
+__global__ void __launch_bounds__(kBlock) k_mx_mr_spmv(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st_in;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n, cap = a->stage_cap;
+    CF_STAGE(float, cap);
+    const float *r = a->fr;
+    float *y = a->fq;
+    const int32_t *ro = a->ro, *col = a->col;
+    const float *val = a->val32;
+    float acc[2] = {0.f, 0.f};
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<float> ch = stage_chunk<float>(ro, col, val, n, base, cap, sv_, sc_);
+        const int row = base + (threadIdx.x & 31);
+        const float v = row_product<float>(ch, col, val, [&](int c) { return r[c]; });
+        if (row < n) {
+            y[row] = v;
+            acc[0] = fma_t(r[row], v, acc[0]);
+            acc[1] = fma_t(v, v, acc[1]);
+        }
+        __syncwarp();
+    }
+    float tot[2];
+    if (grid_reduce<2, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
+                              tot) && threadIdx.x == 0)
+        st->omega = tot[0] / tot[1];
+}
+
+__global__ void __launch_bounds__(kBlock) k_mx_mr_update(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st_in;
+    CF_EXIT_IF_DONE(a, st, true);
+    const int n = a->n;
+    const float w = (float)ld_cg(&st->omega);
+    float *r = a->fr, *d = a->fx;
+    const float *y = a->fq;
+    float acc[1] = {0.f};
+    CF_FOR_ELEMS(i, n) {
+        d[i] = fma_t(w, r[i], d[i]);
+        const float ri = fma_t(-w, y[i], r[i]);
+        r[i] = ri;
+        acc[0] = fma_t(ri, ri, acc[0]);
+    }
+    float tot[1];
+    if (grid_reduce<1, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_B], false,
+                              tot) && threadIdx.x == 0)
+        finish_step(a, st, sqrtf(tot[0]));
+}
+
+// ---------------------------------------------------------------------------
+// host driver of the refinement loop
+// ---------------------------------------------------------------------------
+static Kernels inner_kernels(int solver)
+{
+    Kernels k;
+    k.value_bytes = sizeof(float);
+    switch (solver) {
+    case CF_CG: k.k1 = (const void *)k_mx_cg_spmv; k.k1_spmv = true; k.k2 = (const void *)k_mx_cg_update; break;
+    case CF_BICG: k.k1 = (const void *)k_mx_bicg_spmv; k.k1_spmv = true; k.k2 = (const void *)k_mx_bicg_update; break;
+    case CF_MR: k.k1 = (const void *)k_mx_mr_spmv; k.k1_spmv = true; k.k2 = (const void *)k_mx_mr_update; break;
+    default: break;
+    }
+    return k;
+}
+
+bool mixed_supported(int solver) { return solver == CF_CG || solver == CF_BICG || solver == CF_MR; }
+
+void mixed_prepare(Context *ctx, Matrix *m, int solver, SolveArgs &A)
+{
+    require(mixed_supported(solver), CF_UNSUPPORTED,
+            "mixed precision is implemented for CG, BiCG and MR");
+    const bool tr = A.val != m->val.as<double>(); // transposed solve
+    matrix_ensure_fp32(m, false);
+    if (solver == CF_BICG || tr) matrix_ensure_fp32(m, true);
+    const size_t fb = sizeof(float) * ((size_t)m->n + 16);
+    for (int i = 14; i < 24; ++i) ctx->vec[i].ensure(fb);
+    const int stride = std::max(ctx->ref_grid, ctx->sm_count * 8);
+    ctx->partials32.ensure(sizeof(float) * kMaxNV * (size_t)stride);
+    ctx->state_in.ensure(sizeof(DevState));
+    A.val32 = m->val32.as<float>();
+    A.valT32 = m->have_T32 ? m->valT32.as<float>() : nullptr;
+    if (tr) std::swap(A.val32, A.valT32);
+    A.fx = ctx->vec[14].as<float>();
+    A.fr = ctx->vec[15].as<float>();
+    A.fp[0] = ctx->vec[16].as<float>();
+    A.fp[1] = ctx->vec[17].as<float>();
+    A.fq = ctx->vec[18].as<float>();
+    A.frs = ctx->vec[19].as<float>();
+    A.fps[0] = ctx->vec[20].as<float>();
+    A.fps[1] = ctx->vec[21].as<float>();
+    A.fqs = ctx->vec[22].as<float>();
+    A.partials32 = ctx->partials32.as<float>();
+    A.st_in = ctx->state_in.as<DevState>();
+}
+
+// Runs after the FP64 normFactor and initial residual (st holds ||r_0||,
+// tol = tolerance * normFactor).  Returns the total inner iterations.
+MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c, SolveArgs *d_args,
+                      int cap, bool use_graph_in)
+{
+    MixedResult res;
+    SolveArgs &A = *ctx->h_args;
+    void *args1[] = {&d_args};
+    const Kernels kk = inner_kernels(solver);
+    bool use_graph = use_graph_in;
+    GraphEntry *ge = nullptr;
+    if (use_graph) {
+        try {
+            ge = loop_graph(ctx, kk, solver, CF_PREC_MIXED, cap, false, d_args);
+        } catch (const Error &) {
+            ctx->graphs_ok = false;
+            use_graph = false;
+        }
+    }
+    if (use_graph) {
+        // the loop handle travels in the device-resident arguments
+        A.use_cond = 1;
+        A.cond = ge->cond;
+        CF_CUDA(cudaMemcpyAsync(d_args, &A, sizeof(SolveArgs), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CF_CUDA(cudaMemcpyAsync(ctx->h_state, A.st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+    CF_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int64_t max_total = c.max_iter <= 0 ? INT_MAX : c.max_iter;
+    const int max_outer = c.mixed_max_outer > 0 ? c.mixed_max_outer : 50;
+    const double eta = (c.mixed_inner_rtol > 0 && c.mixed_inner_rtol < 1) ? c.mixed_inner_rtol : 1e-4;
+    double prev_norm = ctx->h_state->norm;
+    int64_t total = 0;
+    int outer = 0;
+    int status = ctx->h_state->done ? ctx->h_state->status : CF_NOT_CONVERGED;
+    DevState &SI = *ctx->h_state_in;
+    while (!ctx->h_state->done && outer < max_outer && total < max_total) {
+        SI = DevState{};
+        SI.tolerance = eta;
+        SI.max_steps = (int)std::min<int64_t>(max_total - total, INT_MAX);
+        SI.int_bound = c.bicg_int_bound;
+        SI.hist_cap = 0;
+        CF_CUDA(cudaMemcpyAsync(A.st_in, &SI, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
+        int bicg = solver == CF_BICG ? 1 : 0;
+        void *a2[] = {&d_args, &bicg};
+        launch(ctx, ctx->stream, (const void *)k_mx_setup,
+               launch_cfg(ctx, (const void *)k_mx_setup, false, cap, false), a2);
+        if (use_graph) {
+            CF_CUDA(cudaGraphLaunch(ge->exec, ctx->stream));
+        } else {
+            for (;;) {
+                for (int i = 0; i < 16; ++i) launch_body(ctx, ctx->stream, kk, cap, false, d_args);
+                CF_CUDA(cudaMemcpyAsync(&SI, A.st_in, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+                CF_CUDA(cudaStreamSynchronize(ctx->stream));
+                if (SI.done) break;
+            }
+        }
+        if (solver != CF_MR)
+            launch(ctx, ctx->stream, (const void *)k_mx_flush,
+                   launch_cfg(ctx, (const void *)k_mx_flush, false, cap, false), args1);
+        launch(ctx, ctx->stream, (const void *)k_mx_correct,
+               launch_cfg(ctx, (const void *)k_mx_correct, false, cap, false), args1);
+        launch(ctx, ctx->stream, (const void *)k_mx_residual,
+               launch_cfg(ctx, (const void *)k_mx_residual, true, cap, false), args1);
+        CF_CUDA(cudaMemcpyAsync(&SI, A.st_in, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+        CF_CUDA(cudaMemcpyAsync(ctx->h_state, A.st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+        CF_CUDA(cudaStreamSynchronize(ctx->stream));
+        total += SI.k;
+        ++outer;
+        const double nrm = ctx->h_state->norm;
+        if (ctx->h_state->done) {
+            status = ctx->h_state->status;
+            break;
+        }
+        if (SI.status == CF_NONFINITE || !(nrm < prev_norm)) {
+            // the FP32 inner solve stopped making progress on the FP64 residual
+            status = (SI.status == CF_NONFINITE) ? CF_NONFINITE : CF_NOT_CONVERGED;
+            break;
+        }
+        if (SI.status == CF_BREAKDOWN && SI.k == 0) {
+            status = CF_BREAKDOWN;
+            break;
+        }
+        prev_norm = nrm;
+    }
+    if (!ctx->h_state->done && status == CF_NOT_CONVERGED) status = CF_NOT_CONVERGED;
+    res.inner_iterations = (int)std::min<int64_t>(total, INT_MAX);
+    res.outer = outer;
+    res.status = ctx->h_state->done ? ctx->h_state->status : status;
+    return res;
+}
+
+} // namespace cf

@@ -1,0 +1,158 @@
+// solver_common.cuh -- pieces shared by the FP64 and mixed-precision solver
+// translation units: per-warp staging declaration, loop bookkeeping run by
+// the last block of a reduction, and the host-side launch / CUDA-graph
+// helpers of the device-driven iteration loop.
+#pragma once
+
+#include "device.cuh"
+
+namespace cf {
+
+// shared-memory staging area of this warp (declared in every SpMV kernel)
+#define CF_STAGE(V, cap)                                                              \
+    extern __shared__ __align__(16) unsigned char smem_raw_[];                        \
+    unsigned char *area_ = smem_raw_ + (threadIdx.x >> 5) * stage_bytes_per_warp<V>(cap); \
+    V *sv_ = reinterpret_cast<V *>(area_);                                            \
+    int32_t *sc_ = reinterpret_cast<int32_t *>(area_ + (size_t)((cap) + 8) * sizeof(V))
+
+// ---------------------------------------------------------------------------
+// loop bookkeeping (thread 0 of the last block)
+// ---------------------------------------------------------------------------
+static __device__ __noinline__ void finish_init(const SolveArgs *a, DevState *st, double rr, bool bicg)
+{
+    const double norm0 = sqrt(rr);
+    st->rho0 = rr;
+    st->rho1 = 0.0;
+    st->norm0 = norm0;
+    st->norm = norm0;
+    if (a->hist && st->hist_cap > 0) a->hist[0] = norm0;
+    double tol = st->tol;
+    if (st->rel_tol > 0.0) tol = fmax(tol, st->rel_tol * norm0);
+    st->tol = tol;
+    st->k = 0;
+    st->x_pending = 0;
+    st->body_count = 0;
+    const bool finite = isfinite(norm0);
+    bool cont = st->max_steps >= 1;
+    if (!bicg) cont = cont && (norm0 > tol || st->min_steps > 0);
+    if (!finite) cont = false;
+    st->done = cont ? 0 : 1;
+    st->status = !finite ? CF_NONFINITE : (norm0 > tol ? CF_NOT_CONVERGED : CF_OK);
+}
+
+// One step of a `while (k++ <= max_steps && norm_r > error)` / CG `for`
+// loop: record ||r|| and decide whether another step runs.
+static __device__ __noinline__ void finish_step(const SolveArgs *a, DevState *st, double norm)
+{
+    const int k = st->k + 1;
+    st->k = k;
+    st->norm = norm;
+    if (a->hist && k < st->hist_cap) a->hist[k] = norm;
+    const bool finite = isfinite(norm);
+    bool cont = finite && k < st->max_steps && (norm > st->tol || k < st->min_steps);
+    int status = !finite ? CF_NONFINITE : (norm > st->tol ? CF_NOT_CONVERGED : CF_OK);
+    st->body_count += 1;
+    if (st->body_count > k + 2 || (a->abort_flag && *a->abort_flag)) {
+        cont = false;
+        status = CF_TIMEOUT;
+    }
+    if (!cont) {
+        st->done = 1;
+        st->status = status;
+    }
+    set_loop_condition(a, cont);
+}
+
+// A body kernel that finds the loop already finished ends the graph loop.
+#define CF_EXIT_IF_DONE(a, st, is_last_kernel)                                  \
+    if (ld_cg(&(st)->done)) {                                                   \
+        if ((is_last_kernel) && blockIdx.x == 0 && threadIdx.x == 0)            \
+            set_loop_condition(a, false);                                       \
+        return;                                                                 \
+    }
+
+
+// ---------------------------------------------------------------------------
+// host-side launch helpers
+// ---------------------------------------------------------------------------
+struct Kernels {
+    const void *k1 = nullptr;    // first body kernel
+    const void *k2 = nullptr;    // second body kernel (may be null)
+    bool k1_spmv = false, k2_spmv = false;
+    size_t value_bytes = sizeof(double);
+};
+
+struct Launch {
+    int grid;
+    size_t smem;
+};
+
+static Launch launch_cfg(Context *ctx, const void *kern, bool is_spmv, int cap, bool ref_order,
+                         size_t value_bytes = sizeof(double))
+{
+    Launch l;
+    l.smem = (is_spmv && cap > 0) ? kWarps * ((size_t)(cap + 8) * (value_bytes + sizeof(int32_t))) : 0;
+    if (l.smem > 48 * 1024)
+        CF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.smem));
+    l.grid = ref_order ? ctx->ref_grid : ctx->fast_grid(kern, l.smem);
+    return l;
+}
+
+static void launch(Context *ctx, cudaStream_t s, const void *kern, const Launch &l, void **args)
+{
+    CF_CUDA(cudaLaunchKernel(kern, dim3(l.grid), dim3(kBlock), args, l.smem, s));
+}
+
+static void launch_body(Context *ctx, cudaStream_t s, const Kernels &kk, int cap, bool ref,
+                        SolveArgs *d_args)
+{
+    void *args[] = {&d_args};
+    launch(ctx, s, kk.k1, launch_cfg(ctx, kk.k1, kk.k1_spmv, cap, ref, kk.value_bytes), args);
+    if (kk.k2) launch(ctx, s, kk.k2, launch_cfg(ctx, kk.k2, kk.k2_spmv, cap, ref, kk.value_bytes), args);
+}
+
+static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int precision, int cap,
+                              bool ref, SolveArgs *d_args)
+{
+    GraphKey key{solver, precision, ref ? 1 : 0, cap, 0};
+    auto it = ctx->graphs.find(key);
+    if (it != ctx->graphs.end()) return &it->second;
+    GraphEntry ge;
+    cudaStream_t cs = nullptr;
+    try {
+        CF_CUDA(cudaGraphCreate(&ge.graph, 0));
+        cudaGraphConditionalHandle h = 0;
+        CF_CUDA(cudaGraphConditionalHandleCreate(&h, ge.graph, 1, cudaGraphCondAssignDefault));
+        ge.cond = (unsigned long long)h;
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        CF_CUDA(cudaGraphAddNode(&node, ge.graph, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        CF_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        CF_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal));
+        launch_body(ctx, cs, kk, cap, ref, d_args);
+        cudaGraph_t out = nullptr;
+        CF_CUDA(cudaStreamEndCapture(cs, &out));
+        CF_CUDA(cudaStreamDestroy(cs));
+        cs = nullptr;
+        CF_CUDA(cudaGraphInstantiate(&ge.exec, ge.graph, 0));
+    } catch (...) {
+        if (cs) {
+            cudaGraph_t junk = nullptr;
+            cudaStreamEndCapture(cs, &junk);
+            cudaStreamDestroy(cs);
+        }
+        if (ge.exec) cudaGraphExecDestroy(ge.exec);
+        if (ge.graph) cudaGraphDestroy(ge.graph);
+        cudaGetLastError();
+        throw;
+    }
+    return &(ctx->graphs[key] = ge);
+}
+
+} // namespace cf

@@ -1,0 +1,257 @@
+/*
+ * cufoam_gb300.h -- C ABI of the GB300 sparse-solve library.
+ *
+ * This is the drop-in boundary for the reference's solver library
+ * (libGIS.so, gis/gis.h:1-95) and for the host work its OpenFOAM plugins do
+ * before calling it (gis/ldu2csr.h:7-40, cuFoam<X>/cuFoam<X>.C).  Every
+ * function is extern "C", takes plain pointers and sizes, never exits the
+ * process and never throws: failures come back as a cf_status plus a
+ * message from cf_context_last_error().
+ *
+ * Pointers tagged with a `memory` argument/field are host pointers when it
+ * is CF_MEM_HOST and device pointers (on the context's device) when it is
+ * CF_MEM_DEVICE.  All device memory the library needs is owned by the
+ * context or the matrix; nothing is allocated per solver iteration.
+ *
+ * Thread safety: one context may be used by one host thread at a time.
+ * Work is ordered on the context's CUDA stream (cf_context_set_stream).
+ */
+#ifndef CUFOAM_GB300_H
+#define CUFOAM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CF_ABI_VERSION 1
+
+typedef enum cf_status {
+    CF_OK = 0,
+    CF_NOT_CONVERGED = 1, /* max_iter reached with the residual above tolerance */
+    CF_BREAKDOWN = 2,     /* BiCG: |xi| < int_bound (SolverSingleGPU.h:629-630) */
+    CF_NONFINITE = 3,     /* a NaN/Inf residual or scalar stopped the loop */
+    CF_BAD_INPUT = 4,     /* invalid sizes, addressing or arguments */
+    CF_CUDA_ERROR = 5,    /* a CUDA runtime call failed (message has details) */
+    CF_TIMEOUT = 6,       /* the device loop guard or the time limit stopped the solve */
+    CF_NO_DEVICE = 7,     /* no usable CUDA device */
+    CF_UNSUPPORTED = 8,   /* option combination not implemented */
+    CF_OUT_OF_MEMORY = 9
+} cf_status;
+
+/* Solver selection: the eight cuFoam plugins (fvSolution `solver cuFoamX;`). */
+typedef enum cf_solver {
+    CF_CG = 0,         /* cuFoamCG         -> gis.h:11-17  CG */
+    CF_BICG = 1,       /* cuFoamBiCG       -> gis.h:28-36  BiCG(A, At) */
+    CF_JACOBI = 2,     /* cuFoamJacobi     -> gis.h:56-62  Jacobi */
+    CF_MR = 3,         /* cuFoamMR         -> gis.h:48-54  MR */
+    CF_MRJACOBI = 4,   /* cuFoamMRJacobi   -> gis.h:64-70  MRJacobi */
+    CF_MRS = 5,        /* cuFoamMRS        -> gis.h:80-87  MRS with invM = D^-1 */
+    CF_JMR = 6,        /* cuFoamJMR        -> gis.h:72-78  JMR */
+    CF_RICHARDSON = 7  /* cuFoamRichardson -> gis.h:38-46  Richardson */
+} cf_solver;
+
+enum { CF_MEM_HOST = 0, CF_MEM_DEVICE = 1 };
+
+/* Arithmetic of the solve. */
+enum {
+    CF_PREC_FP64 = 0,  /* FP64 values, vectors and reductions (the reference's) */
+    CF_PREC_MIXED = 1  /* FP32 matrix/vectors/accumulation inside an FP64
+                          iterative-refinement loop (CG, BiCG, MR only) */
+};
+
+/* Reduction order of dot products in FP64 solves. */
+enum {
+    CF_REDUCE_FAST = 0,      /* deterministic tree over an occupancy-sized grid */
+    CF_REDUCE_REFERENCE = 1  /* the reference's order on this GPU: grid =
+                                maxThreadsPerSM/256 * SMs blocks of 256,
+                                sequential sum of block partials; gives the
+                                reference algorithm's exact bits */
+};
+
+/* normFactor flavour reported in cf_perf and used for the tolerance. */
+enum {
+    CF_NORM_REFERENCE_L2 = 0, /* gis/gis.cu:106-123 (the reference's) */
+    CF_NORM_OPENFOAM_L1 = 1   /* OpenFOAM's lduMatrix::normFactor (sum of |.|) */
+};
+
+typedef struct cf_context cf_context;
+typedef struct cf_matrix cf_matrix;
+
+/* An OpenFOAM lduMatrix: n_cells diagonal entries, n_faces lower/upper
+ * coefficients, owner (lowerAddr) / neighbour (upperAddr) per face, faces
+ * sorted by owner with owner < neighbour.  losort, losort_start and
+ * owner_start are lduAddressing's losortAddr/losortStartAddr/ownerStartAddr;
+ * pass NULL for all three to have them computed on the device. */
+typedef struct cf_ldu_view {
+    int32_t n_cells;
+    int32_t n_faces;
+    const double *diag;
+    const double *lower;
+    const double *upper;
+    const int32_t *lower_addr;
+    const int32_t *upper_addr;
+    const int32_t *losort;
+    const int32_t *losort_start;
+    const int32_t *owner_start;
+    int32_t memory;
+} cf_ldu_view;
+
+typedef struct cf_controls {
+    double tolerance;        /* tolerance_ (absolute, in normFactor units) */
+    double rel_tol;          /* relTol_; 0 = ignore (the reference ignores it) */
+    int32_t max_iter;        /* maxIter_; <= 0 means unlimited, as the reference */
+    int32_t min_iter;        /* minIter_; 0 = none (the reference ignores it) */
+    int32_t precision;       /* CF_PREC_* */
+    int32_t reduction;       /* CF_REDUCE_* (FP64 only) */
+    int32_t memory;          /* where source and psi live: CF_MEM_* */
+    int32_t norm_type;       /* CF_NORM_* */
+    double bicg_int_bound;   /* BiCG breakdown bound, default 1e-10 */
+    double richardson_omega; /* 0 = estimate by the power method (default) */
+    int32_t power_max_steps; /* power-method steps for Richardson, default 30 */
+    int32_t mixed_max_outer; /* mixed: refinement sweeps limit, default 50 */
+    double mixed_inner_rtol; /* mixed: inner FP32 relative tolerance, default 1e-4 */
+    double *history;         /* optional HOST buffer: absolute ||r||_2 per step */
+    int32_t history_capacity;
+    int32_t use_graph;       /* 1 (default): device-driven loop in a CUDA graph */
+    double time_limit_s;     /* > 0: stop with CF_TIMEOUT after this wall time */
+    int32_t profile_kernels; /* 1: host-driven loop with CUDA events around every
+                                body kernel; fills cf_perf.kernel_ms */
+    int32_t transpose;       /* 1: solve A^T psi = source (the adjoint system) */
+    int32_t reserved[6];
+} cf_controls;
+
+/* solverPerformance plus diagnostics. */
+typedef struct cf_perf {
+    double initial_residual;     /* ||r_0|| / normFactor  (OpenFOAM convention) */
+    double final_residual;       /* ||r_end|| / normFactor */
+    double initial_residual_abs; /* ||r_0||_2, what libGIS records */
+    double final_residual_abs;
+    double norm_factor;
+    double true_residual;        /* FP64 ||b - A x|| / normFactor at exit */
+    double omega;                /* Richardson: relaxation factor used */
+    double solve_ms;             /* device time of the solve (CUDA events) */
+    int32_t n_iterations;        /* solver steps (inner steps for mixed) */
+    int32_t n_outer;             /* mixed: refinement sweeps */
+    int32_t status;              /* cf_status of the solve */
+    int32_t history_length;      /* entries written to controls->history */
+    /* with profile_kernels: summed device time and launch count of
+       [0] the SpMV body kernel, [1] the update body kernel,
+       [2] set-up (normFactor, power method, initial residual) */
+    double kernel_ms[3];
+    int32_t kernel_launches[3];
+    int32_t reserved[7];
+} cf_perf;
+
+typedef struct cf_device_info {
+    int32_t device;
+    int32_t sm_count;
+    int32_t cc_major, cc_minor;
+    int32_t max_threads_per_sm;
+    int32_t reference_grid;      /* the reference's LaunchConfig grid here */
+    int64_t l2_bytes;
+    int64_t global_mem_bytes;
+    char name[128];
+} cf_device_info;
+
+/* ---- library / context ------------------------------------------------- */
+int32_t cf_abi_version(void);
+const char *cf_status_string(int32_t status);
+/* Name of a plugin ("cuFoamCG", "CG", ...) -> cf_solver.  Mirrors the
+ * run-time selection by name in fvSolution (cuFoamCG/cuFoamCG.C:11-15). */
+cf_status cf_solver_from_name(const char *name, int32_t *solver);
+void cf_controls_init(cf_controls *c);
+
+cf_status cf_context_create(int32_t device, cf_context **out);
+void cf_context_destroy(cf_context *ctx);
+cf_status cf_context_set_stream(cf_context *ctx, void *cuda_stream);
+const char *cf_context_last_error(const cf_context *ctx);
+cf_status cf_device_query(cf_context *ctx, cf_device_info *out);
+
+/* ---- matrices ---------------------------------------------------------- */
+/* Uploads an LDU matrix and converts it on the device to the reference's
+ * CSR (replaces getSparseCSRMat, gis/ldu2csr.h:7-40, plus the
+ * SingleGPU::SparseCSR upload, gis/SparseSystem/SparseSingleGPU.h:51-80). */
+cf_status cf_matrix_create_ldu(cf_context *ctx, const cf_ldu_view *ldu, cf_matrix **out);
+/* New coefficients, same addressing (time-step / Ux,Uy,Uz reuse). */
+cf_status cf_matrix_update_values(cf_matrix *m, const double *diag, const double *lower,
+                                  const double *upper, int32_t memory);
+void cf_matrix_destroy(cf_matrix *m);
+cf_status cf_matrix_shape(const cf_matrix *m, int32_t *n_rows, int32_t *n_faces, int64_t *nnz);
+/* CSR arrays of A (transpose = 0) or A^T (transpose = 1; the reference's
+ * Transpose, gis/gis.h:10-11).  row_offsets[n+1], cols[nnz], vals[nnz]. */
+cf_status cf_matrix_export_csr(cf_matrix *m, int32_t transpose, int32_t *row_offsets,
+                               int32_t *cols, double *vals, int32_t memory);
+
+/* One-shot device ldu2csr into caller buffers (gis/ldu2csr.h:7-40). */
+cf_status cf_ldu2csr(cf_context *ctx, const cf_ldu_view *ldu, int32_t *row_offsets,
+                     int32_t *cols, double *vals, int32_t memory);
+
+/* ---- operations -------------------------------------------------------- */
+/* y = A x (transpose = 0) or A^T x, with the reference's row summation
+ * (SpMv, SolverSingleGPU.h:173-184). */
+cf_status cf_spmv(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t memory);
+/* normFactor(source, psi) (gis/gis.cu:106-123 for CF_NORM_REFERENCE_L2). */
+cf_status cf_norm_factor(cf_matrix *m, const double *source, const double *psi,
+                         int32_t memory, int32_t norm_type, int32_t reduction, double *out);
+/* cuFoam<X>::solve(psi, source): normFactor, then the solver at
+ * tolerance*normFactor, psi updated in place, performance in *perf.
+ * (cuFoamCG/cuFoamCG.C:38-90 and its seven siblings.) */
+cf_status cf_solve(cf_matrix *m, int32_t solver, const cf_controls *controls,
+                   const double *source, double *psi, cf_perf *perf);
+
+/* Gradient of a loss L through A x = b with respect to the LDU
+ * coefficients, from the forward solution x and the adjoint solution
+ * lambda of A^T lambda = dL/dx (solve with controls.transpose = 1):
+ * d_diag[i] = -lambda_i x_i, d_upper[f] = -lambda_owner x_neighbour,
+ * d_lower[f] = -lambda_neighbour x_owner (dL/dsource is lambda itself).
+ * Any output may be NULL.  No counterpart in the reference, which has no
+ * differentiable path; it is the backward of the torch.autograd.Function
+ * in cufoam_gb300/autograd.py. */
+cf_status cf_adjoint_gradients(cf_matrix *m, const double *lambda, const double *x,
+                               double *d_diag, double *d_lower, double *d_upper,
+                               int32_t memory);
+
+/* ---- batched solves ---------------------------------------------------- */
+/* Many independent LDU systems, each with n_rhs right-hand sides sharing its
+ * matrix (OpenFOAM solves Ux, Uy, Uz with one matrix, calling solve() per
+ * component), solved by CG in ONE persistent kernel launch inside a CUDA
+ * graph.  No counterpart in the reference, whose plugins solve one system
+ * and one component per call (cuFoamCG/cuFoamCG.C:38-90). */
+typedef struct cf_batch cf_batch;
+
+typedef struct cf_batch_config {
+    int32_t cluster_size;   /* CTAs cooperating on one system: 1, 2, 4, 8 (0 = 4) */
+    int32_t threads;        /* threads per CTA: 128, 256, 512 (0 = 256) */
+    int32_t order;          /* 0 = largest system first, 1 = given order */
+    int32_t max_clusters;   /* 0 = one full wave */
+    int32_t reserved[4];
+} cf_batch_config;
+
+typedef struct cf_batch_result {
+    double initial_residual; /* normalised by normFactor */
+    double final_residual;
+    double norm_factor;
+    int32_t n_iterations;
+    int32_t status;
+} cf_batch_result;
+
+cf_status cf_batch_create(cf_context *ctx, int32_t n_systems, const cf_ldu_view *systems,
+                          cf_batch **out);
+void cf_batch_destroy(cf_batch *b);
+/* total rows and, if row_offsets is not NULL, each system's first row in
+ * the batch vectors (length n_systems). */
+cf_status cf_batch_shape(const cf_batch *b, int32_t *n_systems, int64_t *total_rows,
+                         int64_t *row_offsets);
+/* sources / psi: [total_rows][n_rhs] (the n_rhs components of a cell are
+ * adjacent), psi updated in place; results[n_systems * n_rhs].  solver must
+ * be CF_CG and controls->precision CF_PREC_FP64. */
+cf_status cf_batch_solve(cf_batch *b, int32_t solver, const cf_controls *controls,
+                         const cf_batch_config *config, int32_t n_rhs, const double *sources,
+                         double *psi, cf_batch_result *results, double *device_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CUFOAM_GB300_H */

@@ -1,0 +1,68 @@
+"""Build recipe for the CPU oracle (test infrastructure only).
+
+* ``oracle/_build/liboracle.so`` -- the plain-C restatement (oracle.c),
+  compiled with ``-ffp-contract=off`` so it gives the same bits on x86 and
+  Arm, with OpenMP for the timed CPU baseline.
+* ``oracle/_ref/libref_ldu2csr.so`` -- the reference's own
+  ``gis/ldu2csr.h`` compiled from its source file against the
+  ``refstub/lduMatrix.H`` stand-in.  Built only where the reference sources
+  are mounted; the committed golden fixtures carry its outputs elsewhere.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+REF_DIR = os.path.join(HERE, "_ref")
+ORACLE_SO = os.path.join(BUILD_DIR, "liboracle.so")
+REF_LDU2CSR_SO = os.path.join(REF_DIR, "libref_ldu2csr.so")
+REFERENCE_ROOT = os.environ.get("CUFOAM_REFERENCE_ROOT", "/root/reference")
+
+
+def _stale(target: str, sources: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build_oracle(force: bool = False) -> str:
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "oracle.h")]
+    if force or _stale(ORACLE_SO, srcs):
+        tmp = ORACLE_SO + f".tmp{os.getpid()}"
+        subprocess.check_call([
+            "gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp",
+            "-ffp-contract=off", "-Wall", srcs[0], "-o", tmp, "-lm"])
+        os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_ref_ldu2csr(force: bool = False) -> str | None:
+    """Compile gis/ldu2csr.h from the reference sources, if they exist."""
+    gis = os.path.join(REFERENCE_ROOT, "gis")
+    hdr = os.path.join(gis, "ldu2csr.h")
+    if not os.path.exists(hdr):
+        return REF_LDU2CSR_SO if os.path.exists(REF_LDU2CSR_SO) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    drv = os.path.join(HERE, "refstub", "ref_ldu2csr.cpp")
+    stub = os.path.join(HERE, "refstub", "lduMatrix.H")
+    if force or _stale(REF_LDU2CSR_SO, [drv, stub, hdr]):
+        tmp = REF_LDU2CSR_SO + f".tmp{os.getpid()}"
+        subprocess.check_call([
+            "g++", "-O2", "-std=c++14", "-fPIC", "-shared",
+            "-I" + gis, "-I" + os.path.join(HERE, "refstub"), drv, "-o", tmp])
+        os.replace(tmp, REF_LDU2CSR_SO)
+    return REF_LDU2CSR_SO
+
+
+def build_all(force: bool = False) -> None:
+    build_oracle(force)
+    build_ref_ldu2csr(force)
+
+
+if __name__ == "__main__":
+    build_all(force=True)
+    print(ORACLE_SO)

@@ -1,0 +1,66 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); runs through the C ABI")
+
+
+def _have_gpu() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+HAVE_GPU = _have_gpu()
+
+
+def pytest_collection_modifyitems(config, items):
+    if HAVE_GPU:
+        return
+    skip = pytest.mark.skip(reason="no CUDA device")
+    for item in items:
+        if "gpu" in item.keywords:
+            item.add_marker(skip)
+
+
+def load_ldu2csr_cases():
+    import oracle as O
+    z = np.load(os.path.join(GOLDEN, "ldu2csr_cases.npz"))
+    out = {}
+    for name in z["__names__"]:
+        name = str(name)
+        g = lambda k: z[f"{name}/{k}"]
+        L = O.LDU(int(g("n")[0]), g("diag"), g("lower"), g("upper"), g("lower_addr"),
+                  g("upper_addr"))
+        L._addr = (g("losort"), g("losort_start"), g("owner_start"))
+        ref = O.CSR(g("ref_row_offsets"), g("ref_cols"), g("ref_vals"))
+        out[name] = (L, ref)
+    return out
+
+
+@pytest.fixture(scope="session")
+def ldu2csr_cases():
+    return load_ldu2csr_cases()
+
+
+@pytest.fixture(scope="session")
+def ctx():
+    import cufoam_gb300 as cf
+    return cf.default_context()
+
+
+@pytest.fixture(scope="session")
+def ref_grid(ctx):
+    return ctx.device_info()["reference_grid"]

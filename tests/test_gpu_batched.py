@@ -1,0 +1,69 @@
+"""Batched persistent-cluster CG: every (system, right-hand side) pair must
+match an independent FP64 solve of the same system (iteration count within
+one, final relative residual within 1e-12, true residual at tolerance)."""
+import numpy as np
+import pytest
+
+import cufoam_gb300 as cf
+import oracle as O
+from cufoam_gb300.batch import BatchSolver, c4_systems
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_batch(n_systems=12, seed=11):
+    systems, sizes = c4_systems(n_systems, seed=seed, lo=6, hi=14)
+    rhs = [np.stack([O.uniform(100 * s + j, L.n) for j in range(3)]) for s, L in enumerate(systems)]
+    return systems, rhs
+
+
+@pytest.mark.parametrize("config", [(1, 256, 0), (2, 128, 0), (4, 256, 0), (8, 512, 0), (4, 256, 1)])
+def test_batched_matches_independent_solves(ctx, config):
+    systems, rhs = _small_batch()
+    tol, maxit = 1e-8, 5000
+    B = BatchSolver(systems, n_rhs=3, context=ctx)
+    x, results, ms = B.solve(rhs, tolerance=tol, max_iter=maxit, config=config)
+    xs = B.unpack(x)
+    for s, L in enumerate(systems):
+        A = O.ldu2csr(L)
+        for j in range(3):
+            res = results[s * 3 + j]
+            want = O.plugin_solve(O.CG, L, rhs[s][j], np.zeros(L.n), tol, maxit)
+            assert abs(res["n_iterations"] - want.n_iterations) <= 1, (s, j)
+            assert abs(res["final_residual"] - want.final_residual) <= 1e-12
+            assert res["status"] == 0
+            assert abs(res["norm_factor"] - want.norm_factor) <= 1e-13 * want.norm_factor
+            true_rel = O.true_residual_norm(A, rhs[s][j], xs[s][j]) / res["norm_factor"]
+            assert true_rel <= 2 * tol
+
+
+def test_batched_graph_and_direct_launch_agree(ctx):
+    systems, rhs = _small_batch(6, seed=3)
+    B = BatchSolver(systems, n_rhs=3, context=ctx)
+    x1, r1, _ = B.solve(rhs, tolerance=1e-9, max_iter=3000, use_graph=True)
+    x2, r2, _ = B.solve(rhs, tolerance=1e-9, max_iter=3000, use_graph=False)
+    assert np.array_equal(x1, x2)
+    assert [r["n_iterations"] for r in r1] == [r["n_iterations"] for r in r2]
+
+
+def test_batched_device_tensors_and_max_iter(ctx):
+    import torch
+    systems, rhs = _small_batch(5, seed=5)
+    B = BatchSolver(systems, n_rhs=3, context=ctx)
+    b = torch.from_numpy(B.pack(rhs)).cuda()
+    x, res, _ = B.solve(b, tolerance=1e-14, max_iter=7)
+    torch.cuda.synchronize()
+    assert all(r["n_iterations"] == 7 and r["status"] == 1 for r in res)
+    assert x.is_cuda
+
+
+def test_autotuner_picks_and_caches(ctx, tmp_path, monkeypatch):
+    monkeypatch.setenv("CUFOAM_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    systems, rhs = _small_batch(8, seed=9)
+    B = BatchSolver(systems, n_rhs=3, context=ctx)
+    cands = [(1, 256, 0), (4, 256, 0)]
+    cfg, entry = B.tune(rhs, tolerance=1e-8, max_iter=2000, candidates=cands)
+    assert cfg in cands and len(entry["timings_ms"]) == 2
+    B2 = BatchSolver(systems, n_rhs=3, context=ctx)
+    cfg2, _ = B2.tune(rhs, tolerance=1e-8, max_iter=2000, candidates=cands)
+    assert cfg2 == cfg  # served from the cache

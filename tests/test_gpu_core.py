@@ -1,0 +1,277 @@
+"""GPU parity tests through the C ABI: device ldu2csr against the reference's
+own CSR (golden fixtures), SpMV / normFactor / all eight solvers against the
+oracle.  In the reference reduction order the GPU must reproduce the
+oracle's bits exactly; in the fast order the final relative residuals agree
+within 1e-12 and the iteration counts within one."""
+import numpy as np
+import pytest
+
+import cufoam_gb300 as cf
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL_RES_TOL = 1e-12   # |final relative residual (GPU) - (oracle)|
+
+
+def _matrix(ctx, L, with_addressing=False):
+    return cf.LduMatrix.from_ldu(L, ctx, with_addressing=with_addressing)
+
+
+# ---------------------------------------------------------------------------
+# ldu2csr
+# ---------------------------------------------------------------------------
+def test_ldu2csr_bit_exact_vs_reference(ctx, ldu2csr_cases):
+    for name, (L, ref) in ldu2csr_cases.items():
+        for given in (False, True):
+            M = _matrix(ctx, L, with_addressing=given)
+            ro, cols, vals = M.to_csr()
+            assert np.array_equal(ro, ref.row_offsets), (name, given)
+            assert np.array_equal(cols, ref.cols), (name, given)
+            assert vals.tobytes() == ref.vals.tobytes(), (name, given)
+            # A^T on the same pattern == ldu2csr of the swapped LDU
+            rot, colt, valt = M.to_csr(transpose=True)
+            T = O.ldu2csr(L.transposed())
+            assert np.array_equal(rot, T.row_offsets) and np.array_equal(colt, T.cols)
+            assert valt.tobytes() == T.vals.tobytes(), name
+            M.close()
+
+
+def test_ldu2csr_from_device_tensors(ctx):
+    import torch
+    L = O.grid_lognormal(9, 7, 5, 31)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(L, k))).cuda()
+           for k in ("diag", "lower", "upper", "lower_addr", "upper_addr")}
+    M = cf.LduMatrix(L.n, dev["diag"], dev["lower"], dev["upper"], dev["lower_addr"],
+                     dev["upper_addr"], context=ctx)
+    ro, cols, vals = M.to_csr()
+    R = O.ldu2csr(L)
+    assert np.array_equal(ro, R.row_offsets) and np.array_equal(cols, R.cols)
+    assert vals.tobytes() == R.vals.tobytes()
+
+
+def test_update_values_keeps_pattern(ctx):
+    L = O.grid_lognormal(8, 6, 4, 1)
+    L2 = O.grid_lognormal(8, 6, 4, 2)
+    M = _matrix(ctx, L)
+    M.update_values(L2.diag, L2.lower, L2.upper)
+    ro, cols, vals = M.to_csr()
+    assert vals.tobytes() == O.ldu2csr(L2).vals.tobytes()
+
+
+def test_bad_addressing_is_rejected(ctx):
+    d = np.ones(3)
+    v = np.ones(2)
+    bad = [
+        (np.array([1, 0], np.int32), np.array([2, 2], np.int32)),   # owners not sorted
+        (np.array([0, 1], np.int32), np.array([0, 2], np.int32)),   # owner == neighbour
+        (np.array([0, 1], np.int32), np.array([1, 3], np.int32)),   # out of range
+    ]
+    for la, ua in bad:
+        with pytest.raises(cf.CufoamError) as e:
+            cf.LduMatrix(3, d, v, v, la, ua, context=ctx)
+        assert e.value.status == 4
+    # losortStart covering one face fewer than n_faces: the entry count would
+    # not be n + 2F, which the reference's fixed-size CSR cannot hold
+    la, ua = np.array([0, 1], np.int32), np.array([1, 2], np.int32)
+    with pytest.raises(cf.CufoamError) as e:
+        cf.LduMatrix(3, d, v, v, la, ua, losort=np.array([0, 1], np.int32),
+                     losort_start=np.array([0, 0, 1, 1], np.int32),
+                     owner_start=np.array([0, 1, 2, 2], np.int32), context=ctx)
+    assert e.value.status == 4
+    # out-of-range losort entry
+    with pytest.raises(cf.CufoamError):
+        cf.LduMatrix(3, d, v, v, la, ua, losort=np.array([0, 5], np.int32),
+                     losort_start=np.array([0, 0, 1, 2], np.int32),
+                     owner_start=np.array([0, 1, 2, 2], np.int32), context=ctx)
+
+
+# ---------------------------------------------------------------------------
+# SpMV and normFactor
+# ---------------------------------------------------------------------------
+def _star_ldu(n):
+    """Cell 0 coupled to every other cell: one row of n entries (longer
+    than a warp's staging buffer) plus short rows."""
+    la = np.zeros(n - 1, np.int32)
+    ua = np.arange(1, n, dtype=np.int32)
+    rng = np.random.default_rng(5)
+    return O.LDU(n, rng.standard_normal(n) + 10, rng.standard_normal(n - 1),
+                 rng.standard_normal(n - 1), la, ua)
+
+
+@pytest.mark.parametrize("case", ["c1", "lognormal", "convdiff", "star", "permuted"])
+def test_spmv_bit_exact(ctx, case):
+    L = {"c1": lambda: O.grid_const(64, 64, 1),
+         "lognormal": lambda: O.grid_lognormal(20, 17, 9, 3),
+         "convdiff": lambda: O.grid_convdiff(16, 15, 14, 4)[0],
+         "star": lambda: _star_ldu(3000),
+         "permuted": lambda: O.permute_ldu(O.grid_lognormal(11, 10, 9, 6), O.permutation(6, 990)),
+         }[case]()
+    M = _matrix(ctx, L)
+    x = O.uniform(7, L.n)
+    A = O.ldu2csr(L)
+    assert M.spmv(x).tobytes() == O.ref_spmv(A, x).tobytes()
+    T = O.ldu2csr(L.transposed())
+    assert M.spmv(x, transpose=True).tobytes() == O.ref_spmv(T, x).tobytes()
+
+
+def test_norm_factor(ctx, ref_grid):
+    L = O.grid_lognormal(17, 13, 11, 8)
+    A = O.ldu2csr(L)
+    M = _matrix(ctx, L)
+    b = O.uniform(1, L.n)
+    for psi in (np.zeros(L.n), O.uniform(2, L.n, 0.0, 3.0)):
+        want = O.norm_factor(A, b, psi, ref_grid)
+        assert M.norm_factor(b, psi, reduction="reference") == want
+        assert abs(M.norm_factor(b, psi) - want) <= 1e-14 * want
+    # OpenFOAM's L1 normFactor
+    psi = O.uniform(2, L.n, 0.0, 3.0)
+    Ad = A.dense() if L.n < 3000 else None
+    rs = np.array([A.vals[A.row_offsets[i]:A.row_offsets[i + 1]].sum() for i in range(L.n)])
+    xbar = psi.mean()
+    want = np.abs(O.ref_spmv(A, psi) - rs * xbar).sum() + np.abs(b - rs * xbar).sum() + 1e-20
+    assert abs(M.norm_factor(b, psi, norm_type="openfoam") - want) <= 1e-12 * want
+    del Ad
+
+
+# ---------------------------------------------------------------------------
+# solvers
+# ---------------------------------------------------------------------------
+CASES = {
+    "c1": (lambda: O.grid_const(64, 64, 1), 1e-6, 40000),
+    "lognormal3d": (lambda: O.grid_lognormal(12, 10, 8, 2), 1e-8, 40000),
+}
+
+
+def _problem(case, kind):
+    make, tol, maxit = CASES[case]
+    L = make()
+    if kind == O.BICG and case == "lognormal3d":
+        L = O.grid_convdiff(12, 10, 8, 3)[0]
+    b = O.uniform(3, L.n)
+    return L, b, tol, maxit
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("name", list(O.SOLVER_NAMES))
+def test_solver_reference_order_is_bit_exact(ctx, ref_grid, name, case):
+    kind = O.SOLVER_NAMES[name]
+    L, b, tol, maxit = _problem(case, kind)
+    want = O.plugin_solve(kind, L, b, np.zeros(L.n), tol, maxit, grid=ref_grid)
+    M = _matrix(ctx, L)
+    psi = np.zeros(L.n)
+    s = cf.New("p", M, {"solver": "cuFoam" + name, "tolerance": tol, "maxIter": maxit,
+                        "reduction": "reference"})
+    perf = s.solve(psi, b, history=maxit + 1)
+    assert perf.n_iterations == want.n_iterations
+    assert perf.norm_factor == want.norm_factor
+    assert perf.history.tobytes() == want.history.tobytes()
+    assert psi.tobytes() == want.psi.tobytes()
+    assert perf.initial_residual == want.initial_residual
+    assert perf.final_residual == want.final_residual
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("name", list(O.SOLVER_NAMES))
+def test_solver_fast_order_parity(ctx, name, case):
+    """Fast reduction order: a different (deterministic) summation order, so
+    Krylov residuals drift apart at rounding level late in the solve; the
+    iteration count agrees within one, the early history within 1e-12
+    (relative to the initial residual), both runs reach the tolerance, and
+    the GPU answer's true residual meets it."""
+    kind = O.SOLVER_NAMES[name]
+    L, b, tol, maxit = _problem(case, kind)
+    want = O.plugin_solve(kind, L, b, np.zeros(L.n), tol, maxit)
+    M = _matrix(ctx, L)
+    psi = np.zeros(L.n)
+    perf = cf._TABLE["cuFoam" + name]("p", M, {"tolerance": tol, "maxIter": maxit}).solve(
+        psi, b, history=maxit + 1)
+    assert abs(perf.n_iterations - want.n_iterations) <= 1
+    assert abs(perf.norm_factor - want.norm_factor) <= 1e-14 * want.norm_factor
+    h0 = want.history[0]
+    early = min(10, len(want.history), len(perf.history))
+    assert np.all(np.abs(perf.history[:early] - want.history[:early]) <= REL_RES_TOL * h0)
+    if want.final_residual <= tol:
+        assert perf.converged and perf.final_residual <= tol
+    A = O.ldu2csr(L)
+    if kind == O.JMR:  # JMR stops on the D^-1/2-scaled residual
+        r = b - O.ref_spmv(A, psi)
+        true_rel = np.linalg.norm(r / np.sqrt(L.diag)) / perf.norm_factor
+    else:
+        true_rel = O.true_residual_norm(A, b, psi) / perf.norm_factor
+    assert true_rel <= 1.5 * tol
+
+
+def test_graph_and_host_loop_agree(ctx):
+    L = O.grid_lognormal(16, 16, 8, 4)
+    b = O.uniform(5, L.n)
+    M = _matrix(ctx, L)
+    out = []
+    for g in (1, 0):
+        psi = np.zeros(L.n)
+        p = cf.cuFoamCG("p", M, {"tolerance": 1e-9, "maxIter": 5000, "useGraph": g,
+                                 "reduction": "reference"}).solve(psi, b, history=5001)
+        out.append((psi, p))
+    assert out[0][0].tobytes() == out[1][0].tobytes()
+    assert out[0][1].history.tobytes() == out[1][1].history.tobytes()
+
+
+def test_nonzero_initial_guess_and_device_tensors(ctx, ref_grid):
+    import torch
+    L = O.grid_lognormal(14, 12, 10, 7)
+    b = O.uniform(8, L.n)
+    x0 = O.uniform(9, L.n, -0.5, 0.5)
+    want = O.plugin_solve(O.CG, L, b, x0, 1e-9, 5000, grid=ref_grid)
+    M = _matrix(ctx, L)
+    psi = torch.from_numpy(x0.copy()).cuda()
+    src = torch.from_numpy(b).cuda()
+    perf = cf.cuFoamCG("p", M, {"tolerance": 1e-9, "maxIter": 5000,
+                                "reduction": "reference"}).solve(psi, src)
+    torch.cuda.synchronize()
+    assert perf.n_iterations == want.n_iterations
+    assert psi.cpu().numpy().tobytes() == want.psi.tobytes()
+
+
+def test_status_codes(ctx):
+    L = O.grid_const(32, 32, 1)
+    b = O.uniform(1, L.n)
+    M = _matrix(ctx, L)
+    p = cf.cuFoamJacobi("p", M, {"tolerance": 1e-12, "maxIter": 25}).solve(np.zeros(L.n), b)
+    assert p.n_iterations == 25 and p.status == 1 and not p.converged
+    p = cf.cuFoamCG("p", M, {"tolerance": 1e-6, "maxIter": 1000}).solve(np.zeros(L.n), b)
+    assert p.status == 0 and p.converged
+    bad = b.copy()
+    bad[7] = np.nan
+    p = cf.cuFoamCG("p", M, {"tolerance": 1e-6, "maxIter": 100}).solve(np.zeros(L.n), bad)
+    assert p.status == 3 and p.n_iterations == 0
+    # BiCG breakdown: |xi| < 1e-10 on the first step (SolverSingleGPU.h:629-630)
+    L3 = O.LDU(2, np.array([1e12, 1e12]), np.array([0.0]), np.array([0.0]),
+               np.array([0], np.int32), np.array([1], np.int32))
+    M3 = _matrix(ctx, L3)
+    psi = np.zeros(2)
+    p = cf.cuFoamBiCG("p", M3, {"tolerance": 1e-30, "maxIter": 10}).solve(psi, np.ones(2))
+    assert p.status == 2 and p.n_iterations == 0 and np.all(psi == 0)
+
+
+def test_time_limit_stops_loop(ctx):
+    L = O.grid_lognormal(48, 48, 48, 3)
+    b = O.uniform(1, L.n)
+    M = _matrix(ctx, L)
+    for g in (1, 0):
+        p = cf.cuFoamJacobi("p", M, {"tolerance": 1e-15, "maxIter": 10_000_000, "useGraph": g,
+                                     "timeLimit": 0.05}).solve(np.zeros(L.n), b)
+        assert p.status == 6
+        assert 0 < p.n_iterations < 10_000_000
+
+
+def test_repeated_solves_reuse_workspace(ctx):
+    L = O.grid_lognormal(10, 9, 8, 1)
+    M = _matrix(ctx, L)
+    b = O.uniform(2, L.n)
+    res = []
+    for _ in range(3):
+        psi = np.zeros(L.n)
+        res.append(cf.cuFoamMR("p", M, {"tolerance": 1e-8, "maxIter": 20000}).solve(psi, b))
+        res[-1].psi = psi
+    assert all(r.n_iterations == res[0].n_iterations for r in res)
+    assert all(r.psi.tobytes() == res[0].psi.tobytes() for r in res)

@@ -1,0 +1,60 @@
+"""Mixed precision (FP32 inner solve, FP64 iterative refinement): every
+result must reach the FP64 tolerance on the true residual, and its error
+against the FP64 oracle solution is stated and bounded."""
+import numpy as np
+import pytest
+
+import cufoam_gb300 as cf
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _true_rel(L, b, x, nf):
+    return O.true_residual_norm(O.ldu2csr(L), b, x) / nf
+
+
+@pytest.mark.parametrize("name,make", [
+    ("BiCG", lambda: O.grid_convdiff(32, 30, 28, 4, 10.0)[0]),
+    ("MR", lambda: O.grid_convdiff(20, 18, 16, 5, 10.0)[0]),
+    ("CG", lambda: O.grid_lognormal(32, 30, 28, 6)),
+])
+def test_mixed_reaches_fp64_tolerance(ctx, name, make):
+    L = make()
+    b = O.uniform(7, L.n)
+    tol = 1e-10
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    psi = np.zeros(L.n)
+    perf = cf._TABLE["cuFoam" + name]("p", M, {"tolerance": tol, "maxIter": 200000,
+                                              "precision": "mixed"}).solve(psi, b, history=64)
+    assert perf.status == 0, perf.status_name
+    assert perf.n_outer >= 2
+    assert perf.final_residual <= tol
+    true_rel = _true_rel(L, b, psi, perf.norm_factor)
+    assert true_rel <= tol
+    # error against the FP64 oracle solution at the same tolerance
+    want = O.plugin_solve(O.SOLVER_NAMES[name], L, b, np.zeros(L.n), tol, 200000)
+    err = np.linalg.norm(psi - want.psi) / np.linalg.norm(want.psi)
+    assert err < 1e-6, err
+    # history: FP64 residual per refinement sweep, decreasing
+    h = perf.history
+    assert h.shape[0] == perf.n_outer + 1
+    assert np.all(np.diff(h) < 0)
+
+
+def test_mixed_unsupported_solvers_are_refused(ctx):
+    L = O.grid_lognormal(8, 8, 8, 1)
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    with pytest.raises(cf.CufoamError) as e:
+        cf.cuFoamJacobi("p", M, {"precision": "mixed"}).solve(np.zeros(L.n), np.ones(L.n))
+    assert e.value.status == 8
+
+
+def test_mixed_respects_max_iter(ctx):
+    L = O.grid_lognormal(24, 24, 24, 2)
+    b = O.uniform(3, L.n)
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    perf = cf.cuFoamCG("p", M, {"tolerance": 1e-12, "maxIter": 30,
+                                "precision": "mixed"}).solve(np.zeros(L.n), b)
+    assert perf.n_iterations <= 30
+    assert perf.status == 1

@@ -1,0 +1,247 @@
+"""CPU tests of the oracle: pinned to the reference's own ldu2csr (golden
+fixtures made by the reference code compiled from source), generator bytes
+pinned across hosts, solvers cross-checked against dense direct solves."""
+import hashlib
+import json
+import math
+import os
+
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import GOLDEN
+
+
+def test_oracle_ldu2csr_matches_reference_golden(ldu2csr_cases):
+    assert len(ldu2csr_cases) >= 8
+    for name, (L, ref) in ldu2csr_cases.items():
+        A = O.ldu2csr(L)
+        assert np.array_equal(A.row_offsets, ref.row_offsets), name
+        assert np.array_equal(A.cols, ref.cols), name
+        assert A.vals.tobytes() == ref.vals.tobytes(), name
+
+
+def test_oracle_addressing_matches_golden(ldu2csr_cases):
+    for name, (L, _) in ldu2csr_cases.items():
+        fresh = O.ldu_addressing(L.n, L.lower_addr, L.upper_addr)
+        for a, b in zip(fresh, L._addr):
+            assert np.array_equal(a, b), name
+        numpy_side = O.LDU(L.n, L.diag, L.lower, L.upper, L.lower_addr, L.upper_addr).addressing()
+        for a, b in zip(numpy_side, L._addr):
+            assert np.array_equal(a, b), name
+
+
+def test_reference_ldu2csr_rebuilt_here_agrees(ldu2csr_cases):
+    if not O.ref_ldu2csr_available():
+        pytest.skip("reference sources not mounted")
+    for name, (L, ref) in ldu2csr_cases.items():
+        R = O.ref_ldu2csr(L)
+        assert np.array_equal(R.row_offsets, ref.row_offsets), name
+        assert R.vals.tobytes() == ref.vals.tobytes(), name
+
+
+def test_generator_bytes_pinned():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gen_golden", os.path.join(GOLDEN, "gen_golden.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    want = json.load(open(os.path.join(GOLDEN, "generator_checksums.json")))
+    got = {k: hashlib.sha256(np.ascontiguousarray(v).tobytes()).hexdigest()
+           for k, v in gen.generator_inputs().items()}
+    assert got == want
+
+
+def test_addressing_semantics():
+    # losort is a stable sort of faces by neighbour; starts are lower bounds
+    L = O.grid_const(5, 4, 3)
+    ls, lst, ost = L.addressing()
+    nbr = L.upper_addr[ls]
+    assert np.all(np.diff(nbr) >= 0)
+    for c in range(L.n):
+        seg = ls[lst[c]:lst[c + 1]]
+        assert np.all(L.upper_addr[seg] == c)
+        assert np.all(np.diff(seg) > 0)
+        assert np.all(L.lower_addr[ost[c]:ost[c + 1]] == c)
+    with pytest.raises(ValueError):
+        O.ldu_addressing(3, np.array([1, 0], np.int32), np.array([2, 2], np.int32))
+    with pytest.raises(ValueError):
+        O.ldu_addressing(3, np.array([1], np.int32), np.array([1], np.int32))
+
+
+def test_grid_sizes_match_configs():
+    assert O.grid_addressing(64, 64, 1)[0].shape[0] == 8064
+    assert O.n_faces(128, 128, 128) == 6_242_304
+    assert O.n_faces(256, 256, 256) == 50_135_040
+    assert O.n_faces(96, 96, 96) == 2_626_560
+
+
+def test_elementary_functions():
+    from cufoam_gb300 import workloads as W
+    L = W.lib()
+    for x in np.linspace(-30, 30, 301):
+        assert abs(L.wl_exp(x) / math.exp(x) - 1) < 5e-15
+        assert abs(L.wl_sin(x) - math.sin(x)) < 5e-15
+        assert abs(L.wl_cos(x) - math.cos(x)) < 5e-15
+    for x in np.geomspace(1e-300, 1e300, 301):
+        assert abs(L.wl_log(x) - math.log(x)) <= 5e-15 * max(1.0, abs(math.log(x)))
+
+
+def test_numpy_addressing_matches_oracle_restatement():
+    for L in (O.grid_const(7, 5, 3), O.grid_convdiff(6, 5, 4, 2)[0],
+              O.permute_ldu(O.grid_lognormal(5, 4, 3, 1), O.permutation(2, 60))):
+        mine = L.addressing()
+        ref = O.ldu_addressing(L.n, L.lower_addr, L.upper_addr)
+        for a, b in zip(mine, ref):
+            assert np.array_equal(a, b)
+
+
+def test_lognormal_and_convdiff_properties():
+    L = O.grid_lognormal(6, 5, 4, 3)
+    A = O.ldu2csr(L).dense()
+    assert np.allclose(A, A.T)
+    assert np.all(np.linalg.eigvalsh(A) > 0)
+    # diagonal = |off-diagonal| row sum (+ positive wall terms on wall cells)
+    off = np.abs(A - np.diag(np.diag(A))).sum(1)
+    assert np.all(np.diag(A) >= off * (1 - 1e-14))
+    n_off = (np.abs(A) > 0).sum(1) - 1
+    assert np.all(np.diag(A)[n_off < 6] > off[n_off < 6])
+    cd, stats = O.grid_convdiff(6, 5, 4, 4, pe_max=10.0)
+    B = O.ldu2csr(cd).dense()
+    assert not np.allclose(B, B.T)
+    assert abs(stats["pe_max"] - 10.0) < 1e-12
+    # M-matrix: positive diagonal, non-positive off-diagonals, weak row dominance
+    assert np.all(np.diag(B) > 0)
+    assert np.all(B - np.diag(np.diag(B)) <= 0)
+    assert np.all(np.diag(B) - np.abs(B - np.diag(np.diag(B))).sum(1) > -1e-9)
+
+
+def test_permute_ldu_is_similarity():
+    L = O.grid_lognormal(4, 3, 3, 5)
+    perm = O.permutation(3, L.n)
+    P = O.permute_ldu(L, perm)
+    A = O.ldu2csr(L).dense()
+    B = O.ldu2csr(P).dense()
+    Pm = np.zeros((L.n, L.n))
+    Pm[perm, np.arange(L.n)] = 1.0
+    assert np.allclose(Pm @ A @ Pm.T, B)
+
+
+def test_norm_factor_zero_psi_is_source_norm():
+    L = O.grid_const(16, 16, 1)
+    A = O.ldu2csr(L)
+    b = O.uniform(1, L.n)
+    nf = O.norm_factor(A, b, np.zeros(L.n))
+    assert nf == O.ref_dot(b, b) ** 0.5 + 1e-20
+
+
+def fma(a, b, c):
+    """Correctly rounded a*b + c (exact rational arithmetic)."""
+    return float(Fraction(float(a)) * Fraction(float(b)) + Fraction(float(c)))
+
+
+def test_ref_spmv_row_order():
+    # rows longer than 8 exercise the 8-lane FMA accumulation
+    L = O.grid_const(3, 3, 1)
+    A = O.ldu2csr(L)
+    x = O.uniform(3, L.n)
+    assert np.allclose(O.ref_spmv(A, x), A.dense() @ x, rtol=1e-14, atol=1e-14)
+    rng = np.random.default_rng(0)
+    n = 12
+    ro = np.arange(0, n * n + 1, n, dtype=np.int32)
+    cols = np.tile(np.arange(n, dtype=np.int32), n)
+    vals = rng.standard_normal(n * n)
+    D = O.CSR(ro, cols, vals)
+    x = rng.standard_normal(n)
+    y = O.ref_spmv(D, x)
+    row = vals[:n]
+    t = [0.0] * 8
+    for l in range(8):
+        acc = 0.0
+        for j in range(l, n, 8):
+            acc = fma(row[j], x[j], acc)
+        t[l] = acc
+    want = ((t[0] + t[4]) + (t[2] + t[6])) + ((t[1] + t[5]) + (t[3] + t[7]))
+    assert y[0] == want
+
+
+@pytest.mark.parametrize("name", list(O.SOLVER_NAMES))
+def test_oracle_solvers_converge_to_direct_solution(name):
+    kind = O.SOLVER_NAMES[name]
+    L = O.grid_lognormal(8, 7, 1, 21) if kind != O.BICG else O.grid_convdiff(8, 7, 1, 22)[0]
+    A = O.ldu2csr(L)
+    b = O.uniform(2, L.n)
+    x0 = np.zeros(L.n)
+    r = O.plugin_solve(kind, L, b, x0, 1e-10, 200000)
+    xd = np.linalg.solve(A.dense(), b)
+    assert r.final_residual <= 1e-10 * (2.0 if kind == O.JMR else 1.0) or r.n_iterations == 200000
+    assert np.linalg.norm(r.psi - xd) / np.linalg.norm(xd) < 1e-7
+    assert r.history.shape[0] == r.n_iterations + 1
+    assert abs(O.true_residual_norm(A, b, r.psi) - np.linalg.norm(b - A.dense() @ r.psi)) < 1e-12
+
+
+def test_cg_iteration_count_c1():
+    L = O.grid_const(64, 64, 1)
+    b = O.uniform(1, L.n)
+    r = O.plugin_solve(O.CG, L, b, np.zeros(L.n), 1e-6, 10000)
+    assert 150 <= r.n_iterations <= 180
+    assert r.final_residual <= 1e-6
+
+
+def test_bicg_breakdown_detected():
+    # A = [[0,1],[1,0]]: (p*, A p) = 2 r0 r1 = 0 for r0 = (1, 0) -> xi = inf
+    # is not a breakdown (|xi| large); use a tiny rho instead: b = (1e-6, 0)
+    L = O.LDU(2, np.array([0.0, 0.0]), np.array([1.0]), np.array([1.0]),
+              np.array([0], np.int32), np.array([1], np.int32))
+    A = O.ldu2csr(L)
+    At = O.ldu2csr(L.transposed())
+    b = np.array([1e-6, 1e-6])
+    r = O.solve(O.BICG, A, b, np.zeros(2), 1e-30, 10, At=At)
+    # xi = (r,r*)/(p*,Ap) = 2e-12 / 2e-12 = 1: no breakdown; then converges
+    assert not r.breakdown
+    b2 = np.array([1e-6, -1e-6])
+    r2 = O.solve(O.BICG, A, b2, np.zeros(2), 1e-30, 10, At=At)
+    # (p*, A p) = -2e-12, xi = -1: fine too; a real breakdown needs |xi| < 1e-10
+    L3 = O.LDU(2, np.array([1e12, 1e12]), np.array([0.0]), np.array([0.0]),
+               np.array([0], np.int32), np.array([1], np.int32))
+    A3 = O.ldu2csr(L3)
+    r3 = O.solve(O.BICG, A3, np.array([1.0, 1.0]), np.zeros(2), 1e-30, 10, At=O.ldu2csr(L3.transposed()))
+    assert r3.breakdown and r3.n_iterations == 0
+    assert r2.n_iterations >= 1
+
+
+def test_richardson_omega_matches_eigen_estimate():
+    L = O.grid_lognormal(6, 6, 1, 8)
+    A = O.ldu2csr(L)
+    b = O.uniform(3, L.n)
+    r = O.solve(O.RICHARDSON, A, b, np.zeros(L.n), 1e-8 * np.linalg.norm(b), 100000)
+    lmax = np.linalg.eigvalsh(A.dense()).max()
+    assert abs(r.lambda_max - lmax) / lmax < 0.05
+    assert r.diag_abs_min == np.abs(L.diag).min()
+    assert r.omega == 2.0 / (r.lambda_max + r.diag_abs_min)
+
+
+def test_mrs_equals_mrjacobi_in_exact_arithmetic():
+    L = O.grid_lognormal(7, 6, 1, 9)
+    b = O.uniform(4, L.n)
+    a = O.plugin_solve(O.MRS, L, b, np.zeros(L.n), 1e-8, 50000)
+    c = O.plugin_solve(O.MRJACOBI, L, b, np.zeros(L.n), 1e-8, 50000)
+    assert a.n_iterations == c.n_iterations
+    assert np.array_equal(a.history, c.history)
+
+
+def test_max_iter_cap_and_loop_semantics():
+    L = O.grid_const(16, 16, 1)
+    b = O.uniform(1, L.n)
+    for kind in (O.CG, O.MR, O.JACOBI, O.RICHARDSON, O.BICG):
+        r = O.plugin_solve(kind, L, b, np.zeros(L.n), 1e-14, 7)
+        assert r.n_iterations == 7 and r.history.shape[0] == 8
+    # already converged: no step, except BiCG which always takes one
+    x = np.linalg.solve(O.ldu2csr(L).dense(), b)
+    for kind in (O.CG, O.MR, O.JACOBI):
+        r = O.plugin_solve(kind, L, b, x, 1e-3, 7)
+        assert r.n_iterations == 0
+    r = O.plugin_solve(O.BICG, L, b, x, 1e-3, 7)
+    assert r.n_iterations == 1
