@@ -47,16 +47,22 @@ def spmv_bytes(n: int, nnz: int) -> int:
     return 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
 
 
-def cg_k1_bytes(n: int, nnz: int) -> int:
-    """k_cg_spmv: matrix, r and p_old read, p and q written, x read+written."""
-    return 12 * nnz + 4 * (n + 1) + 48 * n
+def cg_spmv_bytes(n: int, nnz: int) -> int:
+    """k_f_cg_spmv: matrix, p read (gathered, counted once), q written."""
+    return spmv_bytes(n, nnz)
+
+
+def cg_iteration_bytes(n: int, nnz: int) -> int:
+    """One CG step of the default schedule: prep (r, p, x read; p, x
+    written), spmv (q = A p), update (q, r read; r written)."""
+    return 40 * n + cg_spmv_bytes(n, nnz) + 24 * n
 
 
 def solve_bytes(n: int, nnz: int, iters: int) -> int:
     matrix = 12 * nnz + 4 * (n + 1)
     setup = 8 * n + (matrix + 16 * n) + (matrix + 24 * n)     # nf_sum, nf_dist, res_init
-    per_iter = cg_k1_bytes(n, nnz) + 24 * n                     # K1 + K2 (r, q read, r write)
-    first = per_iter - 16 * n                                   # no pending x update in step 1
+    per_iter = cg_iteration_bytes(n, nnz)
+    first = per_iter - 24 * n                                   # step 1: p = r, no x update
     flush = 24 * n
     if iters == 0:
         return setup
@@ -164,8 +170,7 @@ def cpu_baseline(L, b, iters: int):
     dt = time.perf_counter() - t0
     nf_time_share = 0  # normFactor is not part of the sample
     del nf_time_share
-    bytes_ = (12 * A.nnz + 4 * (A.n + 1) + 24 * A.n) + r.n_iterations * (
-        cg_k1_bytes(A.n, A.nnz) + 24 * A.n)
+    bytes_ = (12 * A.nnz + 4 * (A.n + 1) + 24 * A.n) + r.n_iterations * cg_iteration_bytes(A.n, A.nnz)
     return bytes_ / dt / 1e9, O.get_threads(), dt, r.n_iterations
 
 
@@ -185,7 +190,7 @@ def run_reference(args):
         t0 = time.perf_counter()
         O.solve(O.CG, A, b, x0, 0.0, sample)
         times.append(time.perf_counter() - t0)
-    bytes_step = (12 * A.nnz + 4 * (A.n + 1) + 24 * A.n) + sample * (cg_k1_bytes(A.n, A.nnz) + 24 * A.n)
+    bytes_step = (12 * A.nnz + 4 * (A.n + 1) + 24 * A.n) + sample * cg_iteration_bytes(A.n, A.nnz)
     total = sum(times)
     value = bytes_step * args.steps / total / 1e9
     cores = O.get_threads()
@@ -264,7 +269,7 @@ def run_ours(args):
         ms = float(t.item())
     bytes_total = sum(solve_bytes(n, nnz, k) for k in its) * world
     value = bytes_total / (ms * 1e-3) / 1e9
-    launches = sum(5 + 2 * k for k in its)  # nf_sum, nf_dist, res_init, 2/iter, flush, clear
+    launches = sum(5 + 3 * k for k in its)  # nf_sum, nf_dist, res_init, 3/iter, flush, clear
 
     # ---- e2e through the public API with pinned host buffers -------------
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -300,24 +305,25 @@ def run_ours(args):
     prof = cf.cuFoamCG("p", M, {"tolerance": TOL, "maxIter": MAX_ITER,
                                 "profileKernels": 1})
     pp = prof.solve(psi, src)
-    raw = pp  # SolverPerformance exposes kernel timings via the raw struct below
-    k1_ms = raw.kernel_ms[0] / max(raw.kernel_launches[0], 1)
-    k2_ms = raw.kernel_ms[1] / max(raw.kernel_launches[1], 1)
+    k1_ms = pp.kernel_ms[0] / max(pp.kernel_launches[0], 1)
+    k2_ms = pp.kernel_ms[1] / max(pp.kernel_launches[1], 1)
+    k0_ms = pp.kernel_ms[2] / max(pp.kernel_launches[2], 1)
     peak, peak_kind = measured_hbm_peak()
-    k1_gbs = cg_k1_bytes(n, nnz) / (k1_ms * 1e-3) / 1e9
+    k1_gbs = cg_spmv_bytes(n, nnz) / (k1_ms * 1e-3) / 1e9
     k2_gbs = 24 * n / (k2_ms * 1e-3) / 1e9
+    k0_gbs = 40 * n / (k0_ms * 1e-3) / 1e9
 
     # ---- plain SpMV (y = A x) with CUDA events ---------------------------
     x = torch.from_numpy(W.uniform(5, n)).to(f"cuda:{device}")
     for _ in range(3):
-        M.spmv(x)
+        M.spmv(x, row_order="fast")
     torch.cuda.synchronize()
     reps = 50
     s0 = torch.cuda.Event(enable_timing=True)
     s1 = torch.cuda.Event(enable_timing=True)
     s0.record(stream)
     for _ in range(reps):
-        M.spmv(x)
+        M.spmv(x, row_order="fast")
     s1.record(stream)
     torch.cuda.synchronize()
     spmv_ms = s0.elapsed_time(s1) / reps
@@ -341,13 +347,14 @@ def run_ours(args):
         "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": round(1e3 * e_dt / len(e_its), 3)},
-        "roofline": {"bound": "hbm", "kernel": "k_cg_spmv", "achieved": round(k1_gbs, 1),
+        "roofline": {"bound": "hbm", "kernel": "k_f_cg_spmv", "achieved": round(k1_gbs, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(k1_gbs / peak, 4),
                      "peak_source": peak_kind,
-                     "bytes_per_launch": cg_k1_bytes(n, nnz),
+                     "bytes_per_launch": cg_spmv_bytes(n, nnz),
                      "us_per_launch": round(k1_ms * 1e3, 2),
-                     "traffic": profiled_traffic("k_cg_spmv_poisson128.md")},
-        "kernels": {"k_cg_update_gbs": round(k2_gbs, 1), "k_cg_update_us": round(k2_ms * 1e3, 2),
+                     "traffic": profiled_traffic("k_f_cg_spmv_poisson128.md")},
+        "kernels": {"k_f_cg_update_gbs": round(k2_gbs, 1), "k_f_cg_update_us": round(k2_ms * 1e3, 2),
+                    "k_f_cg_prep_gbs": round(k0_gbs, 1), "k_f_cg_prep_us": round(k0_ms * 1e3, 2),
                     "spmv_gbs": round(spmv_gbs, 1), "spmv_us": round(spmv_ms * 1e3, 2),
                     "spmv_frac": round(spmv_gbs / peak, 4)},
         "cpu_baseline": {"value": round(base_gbs, 3), "unit": "GB/s", "cores": cores, "kind": "port",
@@ -380,7 +387,7 @@ def run_profile(args):
         perf = s.solve(psi, src)
     x = torch.from_numpy(W.uniform(5, L.n)).cuda()
     for _ in range(5):
-        M.spmv(x)
+        M.spmv(x, row_order="fast")
     torch.cuda.synchronize()
     print(f"profile run ok: {perf.n_iterations} iterations")
     return 0

@@ -205,7 +205,9 @@ class LduMatrix:
                        "cf_matrix_export_csr")
         return ro, cols, vals
 
-    def spmv(self, x, transpose: bool = False):
+    def spmv(self, x, transpose: bool = False, row_order: str = "reference"):
+        """y = A x (or A^T x); row_order "reference" sums rows in the
+        reference's 8-lane order, "fast" as one FMA chain."""
         px, mx, kx = _ptr(x, np.float64, "x")
         if mx == _capi.CF_MEM_DEVICE:
             import torch
@@ -214,7 +216,8 @@ class LduMatrix:
         else:
             y = np.empty(self.n)
             py = y.ctypes.data
-        self.ctx.check(self._lib.cf_spmv(self._h, int(transpose), px, py, mx), "cf_spmv")
+        self.ctx.check(self._lib.cf_spmv(self._h, int(transpose), px, py, mx, _REDUCE[row_order]),
+                       "cf_spmv")
         return y
 
     def norm_factor(self, source, psi, norm_type: str = "reference",
@@ -269,8 +272,8 @@ class SolverPerformance:
     omega: float = 0.0
     n_outer: int = 0
     history: np.ndarray | None = field(default=None, repr=False)
-    kernel_ms: tuple = (0.0, 0.0, 0.0)
-    kernel_launches: tuple = (0, 0, 0)
+    kernel_ms: tuple = (0.0, 0.0, 0.0, 0.0)        # spmv, update, prep, set-up
+    kernel_launches: tuple = (0, 0, 0, 0)
 
     @property
     def status_name(self) -> str:

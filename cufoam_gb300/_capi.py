@@ -49,8 +49,8 @@ class cf_perf(C.Structure):
                 ("omega", C.c_double), ("solve_ms", C.c_double),
                 ("n_iterations", C.c_int32), ("n_outer", C.c_int32),
                 ("status", C.c_int32), ("history_length", C.c_int32),
-                ("kernel_ms", C.c_double * 3), ("kernel_launches", C.c_int32 * 3),
-                ("reserved", C.c_int32 * 7)]
+                ("kernel_ms", C.c_double * 4), ("kernel_launches", C.c_int32 * 4),
+                ("reserved", C.c_int32 * 6)]
 
 
 class cf_device_info(C.Structure):
@@ -109,7 +109,7 @@ def load(build_if_missing: bool = True):
                                         C.POINTER(C.c_int64)]),
         "cf_matrix_export_csr": (C.c_int32, [P, C.c_int32, P, P, P, C.c_int32]),
         "cf_ldu2csr": (C.c_int32, [P, C.POINTER(cf_ldu_view), P, P, P, C.c_int32]),
-        "cf_spmv": (C.c_int32, [P, C.c_int32, P, P, C.c_int32]),
+        "cf_spmv": (C.c_int32, [P, C.c_int32, P, P, C.c_int32, C.c_int32]),
         "cf_norm_factor": (C.c_int32, [P, P, P, C.c_int32, C.c_int32, C.c_int32,
                                        C.POINTER(C.c_double)]),
         "cf_solve": (C.c_int32, [P, C.c_int32, C.POINTER(cf_controls), P, P,

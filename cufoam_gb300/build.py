@@ -16,7 +16,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libcufoam_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
-SOURCES = ["capi.cu", "matrix.cu", "solve_fp64.cu", "mixed.cu", "adjoint.cu", "batched.cu"]
+SOURCES = ["capi.cu", "matrix.cu", "solve_fp64.cu", "solve_fast.cu", "mixed.cu", "adjoint.cu", "batched.cu"]
 HEADERS = ["internal.h", "device.cuh", "solver_common.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -35,6 +35,30 @@ def _flags() -> list[str]:
 
 def _newest(paths: list[str]) -> float:
     return max(os.path.getmtime(p) for p in paths)
+
+
+PLUGIN_DIR = os.path.join(HERE, "plugin")
+PLUGIN_LIB = os.path.join(BUILD_DIR, "libcufoam_plugin_minifoam.so")
+
+
+def build_plugin(force: bool = False) -> str:
+    """The OpenFOAM plugin sources compiled against the minifoam stand-in,
+    plus the harness that drives them (linked to the C-ABI library)."""
+    srcs = [os.path.join(PLUGIN_DIR, "cuFoamGB300.C"),
+            os.path.join(PLUGIN_DIR, "minifoam", "minifoam_harness.C")]
+    deps = srcs + [os.path.join(PLUGIN_DIR, "cuFoamGB300.H"),
+                   os.path.join(PLUGIN_DIR, "minifoam", "lduMatrix.H"),
+                   os.path.join(INCLUDE, "cufoam_gb300.h"), LIB_PATH]
+    if force or not os.path.exists(PLUGIN_LIB) or os.path.getmtime(PLUGIN_LIB) < _newest(deps):
+        tmp = PLUGIN_LIB + f".tmp{os.getpid()}"
+        cmd = ["g++", "-O2", "-std=c++14", "-shared", "-fPIC", "-Wall",
+               "-I" + os.path.join(PLUGIN_DIR, "minifoam"), "-I" + INCLUDE] + srcs + \
+              ["-L" + BUILD_DIR, "-lcufoam_gb300", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"plugin build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, PLUGIN_LIB)
+    return PLUGIN_LIB
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -71,6 +95,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB_PATH)
+    build_plugin(force)
     return LIB_PATH
 
 

@@ -360,7 +360,8 @@ cf_status cf_ldu2csr(cf_context *ctx, const cf_ldu_view *ldu, int32_t *row_offse
     return guarded(ctx, [&] { cf::ldu2csr_into(ctx->impl, *ldu, row_offsets, cols, vals, memory); });
 }
 
-cf_status cf_spmv(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t memory)
+cf_status cf_spmv(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t memory,
+                  int32_t row_order)
 {
     if (!m || !x || !y) return CF_BAD_INPUT;
     return guarded(m->owner, [&] {
@@ -376,7 +377,7 @@ cf_status cf_spmv(cf_matrix *m, int32_t transpose, const double *x, double *y, i
             dx = c->vec[0].as<double>();
             dy = c->vec[1].as<double>();
         }
-        cf::spmv(mm, transpose != 0, dx, dy);
+        cf::spmv(mm, transpose != 0, dx, dy, row_order == CF_REDUCE_REFERENCE);
         if (memory == CF_MEM_HOST) cf::download(c, y, dy, sizeof(double) * mm->n, CF_MEM_HOST);
         CF_CUDA(cudaStreamSynchronize(c->stream));
     });

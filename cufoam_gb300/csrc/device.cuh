@@ -250,6 +250,38 @@ __device__ __forceinline__ void row_product2(const Chunk<V> &c, const int32_t *_
     y2 = tree8(u);
 }
 
+// sum_j a_ij * g(j) as one FMA chain in entry order: one FP64 instruction
+// per entry, the least work per row (the fast reduction order).
+template <class V, class G>
+__device__ __forceinline__ V row_chain(const Chunk<V> &c, const int32_t *__restrict__ col,
+                                       const V *__restrict__ val, G g)
+{
+    V acc = V(0);
+    if (c.ov >= 0) {
+        for (int j = c.rs; j < c.re; ++j) acc = fma_t(c.sv[j - c.ov], g(c.sc[j - c.oc]), acc);
+    } else {
+        for (int j = c.rs; j < c.re; ++j) acc = fma_t(__ldg(val + j), g(__ldg(col + j)), acc);
+    }
+    return acc;
+}
+
+// Two FMA chains over the same pattern (A and A^T values).
+template <class V, class G1, class G2>
+__device__ __forceinline__ void row_chain2(const Chunk<V> &c, const int32_t *__restrict__ col,
+                                           const V *__restrict__ val1, const V *__restrict__ val2,
+                                           G1 g1, G2 g2, V &y1, V &y2)
+{
+    V a1 = V(0), a2 = V(0);
+    for (int j = c.rs; j < c.re; ++j) {
+        const int cc = (c.oc >= 0) ? c.sc[j - c.oc] : __ldg(col + j);
+        const V v1 = (c.ov >= 0) ? c.sv[j - c.ov] : __ldg(val1 + j);
+        a1 = fma_t(v1, g1(cc), a1);
+        a2 = fma_t(__ldg(val2 + j), g2(cc), a2);
+    }
+    y1 = a1;
+    y2 = a2;
+}
+
 // Finish a device-driven loop iteration: set the graph's while condition.
 __device__ __forceinline__ void set_loop_condition(const SolveArgs *a, bool cont)
 {

@@ -205,7 +205,7 @@ void ldu2csr_into(Context *ctx, const cf_ldu_view &v, int32_t *ro, int32_t *col,
                   double *val, int memory);
 
 int stage_cap_for(const Matrix *m);
-void spmv(Matrix *m, bool transpose, const double *x, double *y);
+void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order);
 double norm_factor(Matrix *m, const double *b, const double *x, int norm_type, bool ref_order);
 void solve(Matrix *m, int solver, const cf_controls &c, const double *b, double *x,
            cf_perf *perf);

@@ -227,7 +227,27 @@ __global__ void k_min_abs(int n, const double *__restrict__ v, double *out_bits_
                   (unsigned long long)__double_as_longlong(m));
 }
 
-// Plain y = A x with the reference's row order (SpMv, SolverSingleGPU.h:173-184).
+// y = A x (SpMv, SolverSingleGPU.h:173-184); each row one FMA chain.
+__global__ void __launch_bounds__(kBlock) k_spmv_fast(int n, int cap, const int32_t *__restrict__ ro,
+                                                      const int32_t *__restrict__ col,
+                                                      const double *__restrict__ val,
+                                                      const double *__restrict__ x, double *y)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5;
+    unsigned char *area = smem + warp * stage_bytes_per_warp<double>(cap);
+    double *sv = reinterpret_cast<double *>(area);
+    int32_t *sc = reinterpret_cast<int32_t *>(area + (size_t)(cap + 8) * sizeof(double));
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv, sc);
+        const int row = base + (threadIdx.x & 31);
+        const double v = row_chain<double>(ch, col, val, [&](int c) { return __ldg(x + c); });
+        if (row < n) y[row] = v;
+        __syncwarp();
+    }
+}
+
+// y = A x with the reference's row order (the 8-lane tree of SpMvKernel).
 __global__ void __launch_bounds__(kBlock) k_spmv(int n, int cap, const int32_t *__restrict__ ro,
                                                  const int32_t *__restrict__ col,
                                                  const double *__restrict__ val,
@@ -508,18 +528,19 @@ int stage_cap_for(const Matrix *m)
     return 0;
 }
 
-void spmv(Matrix *m, bool transpose, const double *x, double *y)
+void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order)
 {
     Context *ctx = m->ctx;
     if (transpose) matrix_ensure_transpose(m);
     if (m->n == 0) return;
     const int cap = stage_cap_for(m);
     const size_t smem = cap > 0 ? kWarps * stage_bytes_per_warp<double>(cap) : 0;
+    auto kern = ref_order ? k_spmv : k_spmv_fast;
     if (smem > 48 * 1024)
-        CF_CUDA(cudaFuncSetAttribute(k_spmv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int g = ctx->fast_grid((const void *)k_spmv, smem);
-    k_spmv<<<g, kBlock, smem, ctx->stream>>>(m->n, cap, m->ro.as<int32_t>(), m->col.as<int32_t>(),
-                                             transpose ? m->valT.as<double>() : m->val.as<double>(), x, y);
+        CF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int g = ctx->fast_grid((const void *)kern, smem);
+    kern<<<g, kBlock, smem, ctx->stream>>>(m->n, cap, m->ro.as<int32_t>(), m->col.as<int32_t>(),
+                                           transpose ? m->valT.as<double>() : m->val.as<double>(), x, y);
     CF_CHECK_LAUNCH();
 }
 

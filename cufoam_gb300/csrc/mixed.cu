@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_residual(const SolveArgs *__restr
     CF_FOR_CHUNKS(base, n) {
         const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        const double t = row_product<double>(ch, col, val, [&](int c) { return x[c]; });
+        const double t = row_chain<double>(ch, col, val, [&](int c) { return x[c]; });
         if (row < n) {
             const double ri = b[row] - t;
             r[row] = ri;
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_cg_spmv(const SolveArgs *__restri
     CF_FOR_CHUNKS(base, n) {
         const Chunk<float> ch = stage_chunk<float>(ro, col, val, n, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        const float y = row_product<float>(ch, col, val, g);
+        const float y = row_chain<float>(ch, col, val, g);
         if (row < n) {
             const float pi = g(row);
             pout[row] = pi;
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_bicg_spmv(const SolveArgs *__rest
         const Chunk<float> ch = stage_chunk<float>(ro, col, val, n, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
         float y1, y2;
-        row_product2<float>(ch, col, val, valT, gp, gps, y1, y2);
+        row_chain2<float>(ch, col, val, valT, gp, gps, y1, y2);
         if (row < n) {
             const float pi = gp(row), psi = gps(row);
             pout[row] = pi;
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_mr_spmv(const SolveArgs *__restri
     CF_FOR_CHUNKS(base, n) {
         const Chunk<float> ch = stage_chunk<float>(ro, col, val, n, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        const float v = row_product<float>(ch, col, val, [&](int c) { return r[c]; });
+        const float v = row_chain<float>(ch, col, val, [&](int c) { return r[c]; });
         if (row < n) {
             y[row] = v;
             acc[0] = fma_t(r[row], v, acc[0]);

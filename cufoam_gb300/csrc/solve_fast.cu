@@ -1,0 +1,399 @@
+// solve_fast.cu -- the default (fast) FP64 iteration kernels.
+//
+// GB300 executes FP64 at 2 FMA per cycle per SM (ncu:
+// sm__sass_thread_inst_executed_op_dfma peak), so a fused kernel that forms
+// the SpMV input on the fly (one FP64 op per matrix entry) and sums rows in
+// the reference's 8-lane tree (seven more adds per row) runs out of FP64
+// issue slots before HBM bandwidth.  These kernels keep the reference's
+// operations per vector element but
+//   * sum each row as one FMA chain (one FP64 instruction per entry),
+//   * form the SpMV input vector once per element in a light element-wise
+//     pass ("prep") instead of once per matrix entry,
+// which costs a few bytes per row and halves the FP64 work: CG needs 12
+// FP64 ops per row and iteration instead of 26.  Dot products use the
+// deterministic fast reduction order.  The loop structure, stopping tests
+// and scalars are those of the reference drivers (SolverSingleGPU.h).
+#include "solver_common.cuh"
+
+#include <algorithm>
+
+namespace cf {
+
+// ---------------------------------------------------------------------------
+// CG (SolverSingleGPU.h:366-445) in three passes:
+//   prep:   x += xi_{k-1} p_{k-1} (deferred);  p_k = r + beta p_{k-1}  (p_1 = r)
+//   spmv:   q = A p_k, (p_k, q) -> xi_k
+//   update: r -= xi_k q, (r, r) -> stopping test, beta
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_f_cg_prep(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n;
+    const int k = ld_cg(&st->k) + 1;
+    double *__restrict__ p = a->p[0];
+    const double *__restrict__ r = a->r[0];
+    double *__restrict__ x = a->x;
+    if (k == 1) {
+        CF_FOR_ELEMS(i, n) p[i] = r[i];
+        return;
+    }
+    const double beta = ld_cg(&st->rho0) / ld_cg(&st->rho1);
+    const double xi = ld_cg(&st->xi);
+    CF_FOR_ELEMS(i, n) {
+        const double pi = p[i];
+        x[i] = fma_t(xi, pi, x[i]);
+        p[i] = fma_t(beta, pi, r[i]);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_f_cg_spmv(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n, cap = a->stage_cap;
+    CF_STAGE(double, cap);
+    const double *__restrict__ p = a->p[0];
+    double *__restrict__ q = a->q;
+    const int32_t *ro = a->ro, *col = a->col;
+    const double *val = a->val;
+    double acc[1] = {0.0};
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const int row = base + (threadIdx.x & 31);
+        const double y = row_chain<double>(ch, col, val, [&](int c) { return p[c]; });
+        if (row < n) {
+            q[row] = y;
+            acc[0] = fma_t(p[row], y, acc[0]);
+        }
+        __syncwarp();
+    }
+    double tot[1];
+    if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_A], false, tot) &&
+        threadIdx.x == 0) {
+        st->xi = st->rho0 / tot[0];
+        st->x_pending = 0;
+    }
+}
+
+// r -= xi q, (r, r): two elements per thread per step for memory parallelism
+__global__ void __launch_bounds__(kBlock) k_f_cg_update(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, true);
+    const int n = a->n;
+    const double xi = ld_cg(&st->xi);
+    double *__restrict__ r = a->r[0];
+    const double *__restrict__ q = a->q;
+    double a0 = 0.0, a1 = 0.0;
+    const int stride = gridDim.x * kBlock;
+    int i = blockIdx.x * kBlock + threadIdx.x;
+    for (; i + stride < n; i += 2 * stride) {
+        const double q0 = q[i], q1 = q[i + stride], r0 = r[i], r1 = r[i + stride];
+        const double n0 = fma_t(-xi, q0, r0), n1 = fma_t(-xi, q1, r1);
+        r[i] = n0;
+        r[i + stride] = n1;
+        a0 = fma_t(n0, n0, a0);
+        a1 = fma_t(n1, n1, a1);
+    }
+    if (i < n) {
+        const double n0 = fma_t(-xi, q[i], r[i]);
+        r[i] = n0;
+        a0 = fma_t(n0, n0, a0);
+    }
+    double acc[1] = {a0 + a1};
+    double tot[1];
+    if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_B], false, tot) &&
+        threadIdx.x == 0) {
+        st->rho1 = st->rho0;
+        st->rho0 = tot[0];
+        st->x_pending = 1;
+        finish_step(a, st, sqrt(tot[0]));
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_f_flush_x(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    if (!ld_cg(&st->x_pending)) return;
+    const int n = a->n;
+    const double xi = ld_cg(&st->xi);
+    const double *p = a->p[0];
+    double *x = a->x;
+    CF_FOR_ELEMS(i, n) x[i] = fma_t(xi, p[i], x[i]);
+}
+
+// ---------------------------------------------------------------------------
+// BiCG with A^T (SolverSingleGPU.h:568-675):
+//   prep:   x += xi p (deferred); p = r + theta p; p* = r* + theta p*
+//   spmv:   q = A p, q* = A^T p* (one pass over the shared pattern),
+//           (p*, q) -> xi, breakdown test
+//   update: k_bicg_update (r, r* updates, ||r||, (r, r*), theta)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_f_bicg_prep(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n;
+    const int k = ld_cg(&st->k) + 1;
+    double *__restrict__ p = a->p[0];
+    double *__restrict__ ps = a->ps[0];
+    const double *__restrict__ r = a->r[0];
+    const double *__restrict__ rs = a->rs;
+    double *__restrict__ x = a->x;
+    if (k == 1) {
+        CF_FOR_ELEMS(i, n) {
+            p[i] = r[i];
+            ps[i] = rs[i];
+        }
+        return;
+    }
+    const double theta = ld_cg(&st->theta);
+    const double xi = ld_cg(&st->xi);
+    const bool xpend = ld_cg(&st->x_pending) != 0;
+    CF_FOR_ELEMS(i, n) {
+        const double pi = p[i];
+        if (xpend) x[i] = fma_t(xi, pi, x[i]);
+        p[i] = fma_t(theta, pi, r[i]);
+        ps[i] = fma_t(theta, ps[i], rs[i]);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_f_bicg_spmv(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n, cap = a->stage_cap;
+    CF_STAGE(double, cap);
+    const double *__restrict__ p = a->p[0];
+    const double *__restrict__ ps = a->ps[0];
+    double *__restrict__ q = a->q;
+    double *__restrict__ qs = a->qs;
+    const int32_t *ro = a->ro, *col = a->col;
+    const double *val = a->val, *valT = a->valT;
+    double acc[1] = {0.0};
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const int row = base + (threadIdx.x & 31);
+        double y1, y2;
+        row_chain2<double>(ch, col, val, valT, [&](int c) { return p[c]; },
+                           [&](int c) { return ps[c]; }, y1, y2);
+        if (row < n) {
+            q[row] = y1;
+            qs[row] = y2;
+            acc[0] = fma_t(ps[row], y1, acc[0]);
+        }
+        __syncwarp();
+    }
+    double tot[1];
+    if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_A], false, tot) &&
+        threadIdx.x == 0) {
+        const double xi = st->rho0 / tot[0];
+        st->x_pending = 0;
+        const double bound = st->int_bound;
+        if (xi > -bound && xi < bound) {
+            st->done = 1;
+            st->status = CF_BREAKDOWN;
+        } else {
+            st->xi = xi;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi (SolverSingleGPU.h:924-994):
+//   prep: d = D^-1 r, x += d     spmv: r -= A d, ||r||
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_f_jac_prep(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n;
+    const double *__restrict__ r = a->r[0];
+    const double *__restrict__ dinv = a->dinv;
+    double *__restrict__ d = a->w[1];
+    double *__restrict__ x = a->x;
+    CF_FOR_ELEMS(i, n) {
+        const double di = __dmul_rn(dinv[i], r[i]);
+        d[i] = di;
+        x[i] = fma_t(1.0, di, x[i]);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_f_jac_spmv(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, true);
+    const int n = a->n, cap = a->stage_cap;
+    CF_STAGE(double, cap);
+    const double *__restrict__ d = a->w[1];
+    double *__restrict__ r = a->r[0];
+    const int32_t *ro = a->ro, *col = a->col;
+    const double *val = a->val;
+    double acc[1] = {0.0};
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const int row = base + (threadIdx.x & 31);
+        const double y = row_chain<double>(ch, col, val, [&](int c) { return d[c]; });
+        if (row < n) {
+            const double ri = fma_t(-1.0, y, r[row]);
+            r[row] = ri;
+            acc[0] = fma_t(ri, ri, acc[0]);
+        }
+        __syncwarp();
+    }
+    double tot[1];
+    if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_A], false, tot) &&
+        threadIdx.x == 0)
+        finish_step(a, st, sqrt(tot[0]));
+}
+
+// ---------------------------------------------------------------------------
+// Richardson (SolverSingleGPU.h:762-819): prep x += omega r; spmv r = b - A x
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_f_rich_prep(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n;
+    const double omega = ld_cg(&st->omega);
+    const double *__restrict__ r = a->r[0];
+    double *__restrict__ x = a->x;
+    CF_FOR_ELEMS(i, n) x[i] = fma_t(omega, r[i], x[i]);
+}
+
+__global__ void __launch_bounds__(kBlock) k_f_rich_spmv(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, true);
+    const int n = a->n, cap = a->stage_cap;
+    CF_STAGE(double, cap);
+    const double *__restrict__ x = a->x;
+    const double *__restrict__ b = a->b;
+    double *__restrict__ r = a->r[0];
+    const int32_t *ro = a->ro, *col = a->col;
+    const double *val = a->val;
+    double acc[1] = {0.0};
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const int row = base + (threadIdx.x & 31);
+        const double t = row_chain<double>(ch, col, val, [&](int c) { return x[c]; });
+        if (row < n) {
+            const double ri = b[row] - t;
+            r[row] = ri;
+            acc[0] = fma_t(ri, ri, acc[0]);
+        }
+        __syncwarp();
+    }
+    double tot[1];
+    if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_A], false, tot) &&
+        threadIdx.x == 0)
+        finish_step(a, st, sqrt(tot[0]));
+}
+
+// ---------------------------------------------------------------------------
+// MR family: prep d = M r (kinds 1-3); spmv y = A d (JMR: z = D^-1/2 y),
+// (r, y), (y, y) -> step; update as in solve_fp64.cu (k_mr_update).
+// ---------------------------------------------------------------------------
+template <int KIND>
+__global__ void __launch_bounds__(kBlock) k_f_mr_prep(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n;
+    const double *__restrict__ r = a->r[0];
+    const double *__restrict__ dinv = a->dinv;
+    const double *__restrict__ sD = a->dinv_sqrt;
+    double *__restrict__ d = a->w[1];
+    CF_FOR_ELEMS(i, n) {
+        double v;
+        if (KIND == 1) v = __dmul_rn(dinv[i], r[i]);
+        else if (KIND == 2) v = __dadd_rn(__dmul_rn(dinv[i], r[i]), 0.0);
+        else v = __dmul_rn(sD[i], r[i]);
+        d[i] = v;
+    }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kBlock) k_f_mr_spmv(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n, cap = a->stage_cap;
+    CF_STAGE(double, cap);
+    const double *__restrict__ r = a->r[0];
+    const double *__restrict__ d = (KIND == 0) ? a->r[0] : a->w[1];
+    const double *__restrict__ sD = a->dinv_sqrt;
+    double *__restrict__ y = a->w[0];
+    const int32_t *ro = a->ro, *col = a->col;
+    const double *val = a->val;
+    double acc[2] = {0.0, 0.0};
+    CF_FOR_CHUNKS(base, n) {
+        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const int row = base + (threadIdx.x & 31);
+        double v = row_chain<double>(ch, col, val, [&](int c) { return d[c]; });
+        if (row < n) {
+            if (KIND == 3) v = __dmul_rn(sD[row], v);
+            y[row] = v;
+            acc[0] = fma_t(r[row], v, acc[0]);
+            acc[1] = fma_t(v, v, acc[1]);
+        }
+        __syncwarp();
+    }
+    double tot[2];
+    if (grid_reduce<2, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_A], false, tot) &&
+        threadIdx.x == 0)
+        st->omega = tot[0] / tot[1];
+}
+
+// ---------------------------------------------------------------------------
+Kernels fast_body_kernels(int solver, const void *mr_update[4], const void *bicg_update)
+{
+    Kernels k;
+    switch (solver) {
+    case CF_CG:
+        k.k0 = (const void *)k_f_cg_prep;
+        k.k1 = (const void *)k_f_cg_spmv;
+        k.k2 = (const void *)k_f_cg_update;
+        break;
+    case CF_BICG:
+        k.k0 = (const void *)k_f_bicg_prep;
+        k.k1 = (const void *)k_f_bicg_spmv;
+        k.k2 = bicg_update;
+        break;
+    case CF_JACOBI:
+        k.k0 = (const void *)k_f_jac_prep;
+        k.k1 = (const void *)k_f_jac_spmv;
+        break;
+    case CF_RICHARDSON:
+        k.k0 = (const void *)k_f_rich_prep;
+        k.k1 = (const void *)k_f_rich_spmv;
+        break;
+    case CF_MR:
+        k.k1 = (const void *)k_f_mr_spmv<0>;
+        k.k2 = mr_update[0];
+        break;
+    case CF_MRJACOBI:
+        k.k0 = (const void *)k_f_mr_prep<1>;
+        k.k1 = (const void *)k_f_mr_spmv<1>;
+        k.k2 = mr_update[1];
+        break;
+    case CF_MRS:
+        k.k0 = (const void *)k_f_mr_prep<2>;
+        k.k1 = (const void *)k_f_mr_spmv<2>;
+        k.k2 = mr_update[2];
+        break;
+    case CF_JMR:
+        k.k0 = (const void *)k_f_mr_prep<3>;
+        k.k1 = (const void *)k_f_mr_spmv<3>;
+        k.k2 = mr_update[3];
+        break;
+    default: break;
+    }
+    k.k1_spmv = true;
+    return k;
+}
+
+const void *fast_flush_kernel() { return (const void *)k_f_flush_x; }
+
+} // namespace cf

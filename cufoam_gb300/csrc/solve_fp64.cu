@@ -658,7 +658,10 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     const bool prof = c.profile_kernels != 0;
     bool use_graph = c.use_graph != 0 && ctx->graphs_ok && !prof;
     GraphEntry *ge = nullptr;
-    const Kernels kk = body_kernels(solver);
+    const void *mr_upd[4] = {(const void *)k_mr_update<0>, (const void *)k_mr_update<1>,
+                             (const void *)k_mr_update<2>, (const void *)k_mr_update<3>};
+    const Kernels kk = ref ? body_kernels(solver)
+                           : fast_body_kernels(solver, mr_upd, (const void *)k_bicg_update);
     SolveArgs *d_args = ctx->args.as<SolveArgs>();
     if (use_graph && !mixed) {
         try {
@@ -710,8 +713,8 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     // ---- iterations: device-driven while loop, or host-driven chunks ----
     CF_CUDA(cudaEventRecord(ctx->ev_mid, ctx->stream));
     auto wall0 = std::chrono::steady_clock::now();
-    double kms[2] = {0.0, 0.0};
-    int klaunch[2] = {0, 0};
+    double kms[3] = {0.0, 0.0, 0.0};
+    int klaunch[3] = {0, 0, 0};
     MixedResult mres;
     if (mixed) {
         mres = run_mixed(ctx, m, solver, c, d_args, cap, use_graph);
@@ -719,10 +722,11 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
         CF_CUDA(cudaGraphLaunch(ge->exec, ctx->stream));
     } else {
         const int chunk = 16;
+        const Launch l0 = kk.k0 ? launch_cfg(ctx, kk.k0, false, cap, ref) : Launch{};
         const Launch l1 = launch_cfg(ctx, kk.k1, kk.k1_spmv, cap, ref);
         const Launch l2 = kk.k2 ? launch_cfg(ctx, kk.k2, kk.k2_spmv, cap, ref) : Launch{};
         if (prof) {
-            while (ctx->prof_events.size() < 3 * chunk) {
+            while (ctx->prof_events.size() < 4 * chunk) {
                 cudaEvent_t e;
                 CF_CUDA(cudaEventCreate(&e));
                 ctx->prof_events.push_back(e);
@@ -731,13 +735,14 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
         int k_before = 0;
         for (;;) {
             for (int i = 0; i < chunk; ++i) {
-                if (prof) CF_CUDA(cudaEventRecord(ctx->prof_events[3 * i], ctx->stream));
+                cudaEvent_t *ev = prof ? &ctx->prof_events[4 * i] : nullptr;
+                if (prof) CF_CUDA(cudaEventRecord(ev[0], ctx->stream));
+                if (kk.k0) launch(ctx, ctx->stream, kk.k0, l0, args1);
+                if (prof) CF_CUDA(cudaEventRecord(ev[1], ctx->stream));
                 launch(ctx, ctx->stream, kk.k1, l1, args1);
-                if (prof) CF_CUDA(cudaEventRecord(ctx->prof_events[3 * i + 1], ctx->stream));
-                if (kk.k2) {
-                    launch(ctx, ctx->stream, kk.k2, l2, args1);
-                    if (prof) CF_CUDA(cudaEventRecord(ctx->prof_events[3 * i + 2], ctx->stream));
-                }
+                if (prof) CF_CUDA(cudaEventRecord(ev[2], ctx->stream));
+                if (kk.k2) launch(ctx, ctx->stream, kk.k2, l2, args1);
+                if (prof) CF_CUDA(cudaEventRecord(ev[3], ctx->stream));
             }
             CF_CUDA(cudaMemcpyAsync(ctx->h_state, A.st, sizeof(DevState), cudaMemcpyDeviceToHost,
                                     ctx->stream));
@@ -746,13 +751,18 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
             if (prof) {
                 for (int i = 0; i < chunk; ++i) {
                     if (k_before + i + 1 > k_now) break; // launches after the loop ended
+                    cudaEvent_t *ev = &ctx->prof_events[4 * i];
                     float t = 0.f;
-                    CF_CUDA(cudaEventElapsedTime(&t, ctx->prof_events[3 * i], ctx->prof_events[3 * i + 1]));
+                    if (kk.k0) {
+                        CF_CUDA(cudaEventElapsedTime(&t, ev[0], ev[1]));
+                        kms[2] += t;
+                        klaunch[2] += 1;
+                    }
+                    CF_CUDA(cudaEventElapsedTime(&t, ev[1], ev[2]));
                     kms[0] += t;
                     klaunch[0] += 1;
                     if (kk.k2) {
-                        CF_CUDA(cudaEventElapsedTime(&t, ctx->prof_events[3 * i + 1],
-                                                     ctx->prof_events[3 * i + 2]));
+                        CF_CUDA(cudaEventElapsedTime(&t, ev[2], ev[3]));
                         kms[1] += t;
                         klaunch[1] += 1;
                     }
@@ -768,12 +778,12 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     }
     // ---- deferred updates ------------------------------------------------
     if ((solver == CF_CG || solver == CF_BICG) && !mixed) {
-        launch(ctx, ctx->stream, (const void *)k_flush_x,
-               launch_cfg(ctx, (const void *)k_flush_x, false, cap, false), args1);
+        const void *flush = ref ? (const void *)k_flush_x : fast_flush_kernel();
+        launch(ctx, ctx->stream, flush, launch_cfg(ctx, flush, false, cap, false), args1);
         k_clear_pending<<<1, 32, 0, ctx->stream>>>(A.st);
         CF_CHECK_LAUNCH();
     }
-    if (solver == CF_RICHARDSON && !mixed) {
+    if (solver == CF_RICHARDSON && !mixed && ref) {
         launch(ctx, ctx->stream, (const void *)k_rich_finish,
                launch_cfg(ctx, (const void *)k_rich_finish, false, cap, false), args1);
     }
@@ -818,10 +828,12 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
             CF_CUDA(cudaEventElapsedTime(&setup, ctx->ev_start, ctx->ev_mid));
             perf->kernel_ms[0] = kms[0];
             perf->kernel_ms[1] = kms[1];
-            perf->kernel_ms[2] = setup;
+            perf->kernel_ms[2] = kms[2];
+            perf->kernel_ms[3] = setup;
             perf->kernel_launches[0] = klaunch[0];
             perf->kernel_launches[1] = klaunch[1];
-            perf->kernel_launches[2] = 1;
+            perf->kernel_launches[2] = klaunch[2];
+            perf->kernel_launches[3] = 1;
         }
     }
 }

@@ -76,8 +76,9 @@ static __device__ __noinline__ void finish_step(const SolveArgs *a, DevState *st
 // host-side launch helpers
 // ---------------------------------------------------------------------------
 struct Kernels {
-    const void *k1 = nullptr;    // first body kernel
-    const void *k2 = nullptr;    // second body kernel (may be null)
+    const void *k0 = nullptr;    // element-wise prep kernel (may be null)
+    const void *k1 = nullptr;    // SpMV body kernel
+    const void *k2 = nullptr;    // update body kernel (may be null)
     bool k1_spmv = false, k2_spmv = false;
     size_t value_bytes = sizeof(double);
 };
@@ -107,6 +108,7 @@ static void launch_body(Context *ctx, cudaStream_t s, const Kernels &kk, int cap
                         SolveArgs *d_args)
 {
     void *args[] = {&d_args};
+    if (kk.k0) launch(ctx, s, kk.k0, launch_cfg(ctx, kk.k0, false, cap, ref, kk.value_bytes), args);
     launch(ctx, s, kk.k1, launch_cfg(ctx, kk.k1, kk.k1_spmv, cap, ref, kk.value_bytes), args);
     if (kk.k2) launch(ctx, s, kk.k2, launch_cfg(ctx, kk.k2, kk.k2_spmv, cap, ref, kk.value_bytes), args);
 }
@@ -154,5 +156,8 @@ static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int p
     }
     return &(ctx->graphs[key] = ge);
 }
+
+Kernels fast_body_kernels(int solver, const void *mr_update[4], const void *bicg_update);
+const void *fast_flush_kernel();
 
 } // namespace cf

@@ -1,0 +1,63 @@
+"""Access to the C++ plugin layer (cuFoamGB300.{H,C}) compiled against the
+minifoam stand-in: ``foam_solve`` runs a plugin exactly as OpenFOAM would
+(lduMatrix::solver::New by name, then solve(psi, source, cmpt))."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .. import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _build.build()
+        from .. import _capi
+        _capi.load()  # the plugin library links against it
+        L = C.CDLL(_build.PLUGIN_LIB)
+        L.mf_solve.restype = C.c_int
+        L.mf_solve.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                               C.c_double, C.c_int, C.c_int, C.POINTER(C.c_char_p),
+                               C.POINTER(C.c_char_p), C.c_void_p, C.c_char_p, C.c_int]
+        _lib = L
+    return _lib
+
+
+class FoamError(RuntimeError):
+    pass
+
+
+def foam_solve(solver: str, ldu, source, psi, tolerance: float = 1e-6, rel_tol: float = 0.0,
+               max_iter: int = 1000, symmetric: bool | None = None, **controls):
+    """Run the plugin `solver` on an LDU matrix through the OpenFOAM-style
+    interface; psi (float64 array) is updated in place.  Returns the
+    solverPerformance fields as a dict."""
+    if symmetric is None:
+        symmetric = np.array_equal(ldu.lower, ldu.upper)
+    d = np.ascontiguousarray(ldu.diag, np.float64)
+    lo = np.ascontiguousarray(ldu.lower, np.float64)
+    up = np.ascontiguousarray(ldu.upper, np.float64)
+    la = np.ascontiguousarray(ldu.lower_addr, np.int32)
+    ua = np.ascontiguousarray(ldu.upper_addr, np.int32)
+    b = np.ascontiguousarray(source, np.float64)
+    if psi.dtype != np.float64 or not psi.flags["C_CONTIGUOUS"]:
+        raise TypeError("psi must be a contiguous float64 array")
+    keys = [k.encode() for k in controls]
+    vals = [str(v).encode() for v in controls.values()]
+    ck = (C.c_char_p * max(1, len(keys)))(*keys)
+    cv = (C.c_char_p * max(1, len(vals)))(*vals)
+    out = np.zeros(4)
+    err = C.create_string_buffer(1024)
+    rc = lib().mf_solve(solver.encode(), ldu.n, lo.shape[0], d.ctypes.data,
+                        None if symmetric else lo.ctypes.data, up.ctypes.data, la.ctypes.data,
+                        ua.ctypes.data, b.ctypes.data, psi.ctypes.data, tolerance, rel_tol,
+                        max_iter, len(keys), ck, cv, out.ctypes.data, err, 1024)
+    if rc != 0:
+        raise FoamError(err.value.decode())
+    return {"initialResidual": out[0], "finalResidual": out[1], "nIterations": int(out[2]),
+            "converged": bool(out[3])}

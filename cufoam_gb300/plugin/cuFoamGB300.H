@@ -1,0 +1,77 @@
+/*
+ * cuFoamGB300.H -- the eight cuFoam lduMatrix::solver plugins on top of the
+ * GB300 C ABI (include/cufoam_gb300.h).
+ *
+ * Drop-in for the reference's plugin library: the same class names
+ * (cuFoamCG, cuFoamBiCG, cuFoamJacobi, cuFoamMR, cuFoamMRJacobi, cuFoamMRS,
+ * cuFoamJMR, cuFoamRichardson; e.g. cuFoamCG/cuFoamCG.H:8-31), the same
+ * constructor and solve(psi, source, cmpt) signature, the same symmetric /
+ * asymmetric registration tables, selected by name in fvSolution:
+ *
+ *     p { solver cuFoamCG; tolerance 1e-8; maxIter 5000; }
+ *
+ * Optional controls (all default to the reference's behaviour):
+ *     precision   FP64 | mixed        (mixed: FP32 inner solve, FP64 refinement)
+ *     reduction   fast | reference    (reference: the reference's exact sums)
+ *     normType    reference | openfoam
+ *     useRelTol   false               (true: honour relTol_/minIter_ like OpenFOAM)
+ *
+ * Residuals in the returned solverPerformance are normalised by normFactor
+ * (OpenFOAM's convention); the stopping test is the reference's
+ * ||r||_2 <= tolerance * normFactor.
+ *
+ * Compiles against OpenFOAM (wmake, Make/files + Make/options) or against
+ * the minimal stand-in in minifoam/ used by the tests.
+ */
+#ifndef CUFOAM_GB300_PLUGIN_H
+#define CUFOAM_GB300_PLUGIN_H
+
+#include "lduMatrix.H"
+#include "cufoam_gb300.h"
+
+namespace Foam {
+
+class cuFoamGB300Solver : public lduMatrix::solver {
+protected:
+    const int32_t kind_;
+
+    cf_controls gb300Controls() const;
+
+public:
+    cuFoamGB300Solver(int32_t kind, const word &fieldName, const lduMatrix &matrix,
+                      const FieldField<Field, scalar> &interfaceBouCoeffs,
+                      const FieldField<Field, scalar> &interfaceIntCoeffs,
+                      const lduInterfaceFieldPtrsList &interfaces,
+                      const dictionary &solverControls);
+
+    virtual ~cuFoamGB300Solver() {}
+
+    virtual solverPerformance solve(scalarField &psi, const scalarField &source,
+                                    const direction cmpt = 0) const;
+};
+
+#define CUFOAM_GB300_DECLARE_SOLVER(Name)                                          \
+    class Name : public cuFoamGB300Solver {                                        \
+    public:                                                                        \
+        TypeName(#Name);                                                           \
+        Name(const word &fieldName, const lduMatrix &matrix,                       \
+             const FieldField<Field, scalar> &interfaceBouCoeffs,                  \
+             const FieldField<Field, scalar> &interfaceIntCoeffs,                  \
+             const lduInterfaceFieldPtrsList &interfaces,                          \
+             const dictionary &solverControls);                                    \
+    };
+
+CUFOAM_GB300_DECLARE_SOLVER(cuFoamCG)
+CUFOAM_GB300_DECLARE_SOLVER(cuFoamBiCG)
+CUFOAM_GB300_DECLARE_SOLVER(cuFoamJacobi)
+CUFOAM_GB300_DECLARE_SOLVER(cuFoamMR)
+CUFOAM_GB300_DECLARE_SOLVER(cuFoamMRJacobi)
+CUFOAM_GB300_DECLARE_SOLVER(cuFoamMRS)
+CUFOAM_GB300_DECLARE_SOLVER(cuFoamJMR)
+CUFOAM_GB300_DECLARE_SOLVER(cuFoamRichardson)
+
+#undef CUFOAM_GB300_DECLARE_SOLVER
+
+} // namespace Foam
+
+#endif

@@ -138,10 +138,11 @@ typedef struct cf_perf {
     int32_t history_length;      /* entries written to controls->history */
     /* with profile_kernels: summed device time and launch count of
        [0] the SpMV body kernel, [1] the update body kernel,
-       [2] set-up (normFactor, power method, initial residual) */
-    double kernel_ms[3];
-    int32_t kernel_launches[3];
-    int32_t reserved[7];
+       [2] the element-wise prep body kernel, [3] set-up (normFactor,
+       power method, initial residual) */
+    double kernel_ms[4];
+    int32_t kernel_launches[4];
+    int32_t reserved[6];
 } cf_perf;
 
 typedef struct cf_device_info {
@@ -189,9 +190,12 @@ cf_status cf_ldu2csr(cf_context *ctx, const cf_ldu_view *ldu, int32_t *row_offse
                      int32_t *cols, double *vals, int32_t memory);
 
 /* ---- operations -------------------------------------------------------- */
-/* y = A x (transpose = 0) or A^T x, with the reference's row summation
- * (SpMv, SolverSingleGPU.h:173-184). */
-cf_status cf_spmv(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t memory);
+/* y = A x (transpose = 0) or A^T x (SpMv, SolverSingleGPU.h:173-184).
+ * row_order CF_REDUCE_REFERENCE sums each row in the reference's 8-lane
+ * order (SpMvKernel, gis/SparseSystem/kernels.h:206-237); CF_REDUCE_FAST
+ * sums it as one FMA chain. */
+cf_status cf_spmv(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t memory,
+                  int32_t row_order);
 /* normFactor(source, psi) (gis/gis.cu:106-123 for CF_NORM_REFERENCE_L2). */
 cf_status cf_norm_factor(cf_matrix *m, const double *source, const double *psi,
                          int32_t memory, int32_t norm_type, int32_t reduction, double *out);

@@ -71,7 +71,7 @@ def test_null_arguments_are_rejected_without_a_device():
     lib = _capi.load()
     assert lib.cf_solve(None, 0, None, None, None, None) == _capi.CF_BAD_INPUT
     assert lib.cf_matrix_create_ldu(None, None, None) == _capi.CF_BAD_INPUT
-    assert lib.cf_spmv(None, 0, None, None, 0) == _capi.CF_BAD_INPUT
+    assert lib.cf_spmv(None, 0, None, None, 0, 0) == _capi.CF_BAD_INPUT
 
 
 class _FakeMatrix:

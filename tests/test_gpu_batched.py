@@ -29,12 +29,15 @@ def test_batched_matches_independent_solves(ctx, config):
         for j in range(3):
             res = results[s * 3 + j]
             want = O.plugin_solve(O.CG, L, rhs[s][j], np.zeros(L.n), tol, maxit)
+            # a different summation order than the oracle: same iteration
+            # count within one, both at the tolerance, same normFactor and
+            # initial residual to rounding, true residual at the tolerance
             assert abs(res["n_iterations"] - want.n_iterations) <= 1, (s, j)
-            assert abs(res["final_residual"] - want.final_residual) <= 1e-12
-            assert res["status"] == 0
+            assert res["status"] == 0 and res["final_residual"] <= tol
             assert abs(res["norm_factor"] - want.norm_factor) <= 1e-13 * want.norm_factor
+            assert abs(res["initial_residual"] - want.initial_residual) <= 1e-13
             true_rel = O.true_residual_norm(A, rhs[s][j], xs[s][j]) / res["norm_factor"]
-            assert true_rel <= 2 * tol
+            assert true_rel <= 1.5 * tol
 
 
 def test_batched_graph_and_direct_launch_agree(ctx):

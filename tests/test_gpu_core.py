@@ -113,6 +113,10 @@ def test_spmv_bit_exact(ctx, case):
     assert M.spmv(x).tobytes() == O.ref_spmv(A, x).tobytes()
     T = O.ldu2csr(L.transposed())
     assert M.spmv(x, transpose=True).tobytes() == O.ref_spmv(T, x).tobytes()
+    # FMA-chain order: same values to rounding
+    y = M.spmv(x, row_order="fast")
+    ref = O.ref_spmv(A, x)
+    assert np.allclose(y, ref, rtol=1e-14, atol=1e-14 * np.abs(ref).max())
 
 
 def test_norm_factor(ctx, ref_grid):
