@@ -115,6 +115,7 @@ def load(build_if_missing: bool = True):
         "cf_solve": (C.c_int32, [P, C.c_int32, C.POINTER(cf_controls), P, P,
                                  C.POINTER(cf_perf)]),
         "cf_adjoint_gradients": (C.c_int32, [P, P, P, P, P, P, C.c_int32]),
+        "cf_norm_factor_noalloc": (C.c_int32, [C.c_int32, P, P, P, P, P, C.c_int32, P, P]),
     }
     for name, (res, args) in sig.items():
         if not hasattr(L, name):

@@ -16,7 +16,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libcufoam_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
-SOURCES = ["capi.cu", "matrix.cu", "solve_fp64.cu", "solve_fast.cu", "mixed.cu", "adjoint.cu", "batched.cu"]
+SOURCES = ["capi.cu", "matrix.cu", "solve_fp64.cu", "solve_fast.cu", "mixed.cu", "adjoint.cu", "batched.cu", "noalloc.cu"]
 HEADERS = ["internal.h", "device.cuh", "solver_common.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

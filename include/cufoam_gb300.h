@@ -217,6 +217,32 @@ cf_status cf_adjoint_gradients(cf_matrix *m, const double *lambda, const double 
                                double *d_diag, double *d_lower, double *d_upper,
                                int32_t memory);
 
+/* ---- allocation-free normFactor ------------------------------------------ */
+/* No counterpart in the reference.  normFactor (the reference's L2 form,
+ * gis/gis.cu:106-123) of a CSR matrix the caller already holds on the
+ * device, for callers that must not allocate device memory: an application
+ * whose own memory pool owns the GPU and forbids driver allocations after
+ * start-up, or a latency-critical loop where a cudaMalloc/cudaFree (which
+ * can synchronise the whole device) is not acceptable.  It allocates nothing.
+ *
+ * All pointers are device pointers; the result is written to *norm_factor
+ * (device memory) by work enqueued on `cuda_stream`; the call does not wait
+ * for it.  The matrix arrays are read only inside [0, nnz).
+ * Scratch: one fixed array of about 33 KB inside the library, which every
+ * GPU that loads the library keeps until the process exits.  All calls
+ * share it and it keeps the last call's contents (the call restarts its
+ * counters itself): calls whose work overlaps on the GPU race -- order them,
+ * e.g. on one stream.  The first call on a device looks up the array's
+ * device address on that device; make that first call before any stream
+ * capture.
+ * reduction: CF_REDUCE_FAST, or CF_REDUCE_REFERENCE (the reference's grid of
+ * maxThreadsPerSM/256 * SMs blocks) -- rejected with CF_UNSUPPORTED when
+ * that grid needs more than the 2048 block partials the scratch holds.
+ * CF_BAD_INPUT for n_rows <= 0 or a null pointer. */
+cf_status cf_norm_factor_noalloc(int32_t n_rows, const int32_t *row_offsets, const int32_t *cols,
+                                 const double *vals, const double *source, const double *psi,
+                                 int32_t reduction, double *norm_factor, void *cuda_stream);
+
 /* ---- batched solves ---------------------------------------------------- */
 /* Many independent LDU systems, each with n_rhs right-hand sides sharing its
  * matrix (OpenFOAM solves Ux, Uy, Uz with one matrix, calling solve() per
