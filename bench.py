@@ -334,6 +334,17 @@ def run_ours(args):
             dist.destroy_process_group()
         return 0
 
+    extras = {}
+    if world == 1 and not args.no_extras:
+        try:
+            extras["mixed_vs_fp64"] = mixed_vs_fp64(ctx, device)
+        except Exception as e:  # reported, never fatal to the headline line
+            extras["mixed_vs_fp64"] = {"error": repr(e)}
+        try:
+            extras["batched_vs_sequential"] = batched_vs_sequential(ctx, device)
+        except Exception as e:
+            extras["batched_vs_sequential"] = {"error": repr(e)}
+
     base_gbs, cores, base_dt, base_it = cpu_baseline(L, b, 40)
     line = {
         "metric": "solve_hbm_gbs", "value": round(value, 2), "unit": "GB/s",
@@ -363,10 +374,114 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clock_info,
     }
+    line.update(extras)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def mixed_vs_fp64(ctx, device, n: int = 256, tol: float = 1e-10, max_iter: int = 40000):
+    """BiCG on the n^3 upwind convection-diffusion system (cell Peclet up to
+    10): FP64 solve vs the mixed-precision solve (FP32 inner BiCG, FP64
+    refinement) to the same FP64 relative residual."""
+    import torch
+
+    import cufoam_gb300 as cf
+    from cufoam_gb300 import workloads as W
+    t0 = time.perf_counter()
+    L, stats = W.grid_convdiff(n, n, n, 7, 10.0)
+    b = W.uniform(8, L.n)
+    gen_s = time.perf_counter() - t0
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    dev = f"cuda:{device}"
+    src = torch.from_numpy(b).to(dev)
+    out = {"workload": f"convdiff7_upwind_{n}^3_pe{stats['pe_max']:.0f}_BiCG", "rows": L.n,
+           "tolerance": tol, "generate_s": round(gen_s, 1)}
+    res = {}
+    for prec in ("FP64", "mixed"):
+        ctrl = {"tolerance": tol, "maxIter": max_iter, "precision": prec}
+        psi = torch.zeros(L.n, dtype=torch.float64, device=dev)
+        cf.cuFoamBiCG("U", M, dict(ctrl, maxIter=5)).solve(psi, src)  # warm-up (graphs, FP32 copy)
+        psi.zero_()
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        perf = cf.cuFoamBiCG("U", M, ctrl).solve(psi, src)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+        r = src - M.spmv(psi, row_order="fast")
+        true_rel = float(torch.linalg.norm(r)) / perf.norm_factor
+        res[prec] = (psi, perf, wall, true_rel)
+        out[prec] = {"ms": round(perf.solve_ms, 2), "wall_ms": round(1e3 * wall, 2),
+                     "iterations": perf.n_iterations, "status": perf.status_name,
+                     "final_rel_residual": perf.final_residual,
+                     "true_rel_residual": true_rel}
+        if prec == "mixed":
+            out[prec]["refinements"] = perf.n_outer
+    x64, x32 = res["FP64"][0], res["mixed"][0]
+    out["mixed"]["rel_error_vs_fp64"] = float(torch.linalg.norm(x32 - x64) / torch.linalg.norm(x64))
+    out["speedup"] = round(res["FP64"][1].solve_ms / res["mixed"][1].solve_ms, 3)
+    M.close()
+    return out
+
+
+def batched_vs_sequential(ctx, device, n_systems: int = 512, tol: float = 1e-8,
+                          max_iter: int = 5000):
+    """512 lognormal 7-point systems (box sides uniform in 16..64, rows
+    randomly permuted) x 3 right-hand sides: one persistent batched launch
+    vs one cuFoamCG solve per (system, right-hand side)."""
+    import torch
+
+    import cufoam_gb300 as cf
+    from cufoam_gb300 import workloads as W
+    from cufoam_gb300.batch import BatchSolver, c4_systems
+    t0 = time.perf_counter()
+    systems, sizes = c4_systems(n_systems, seed=4)
+    rhs = [np.stack([W.uniform(10_000 + 3 * s + j, L.n) for j in range(3)])
+           for s, L in enumerate(systems)]
+    gen_s = time.perf_counter() - t0
+    B = BatchSolver(systems, n_rhs=3, context=ctx)
+    dev = f"cuda:{device}"
+    packed = torch.from_numpy(B.pack(rhs)).to(dev)
+    cands = [(1, 256, 0), (2, 256, 0), (4, 256, 0), (8, 256, 0), (4, 512, 0)]
+    cfg, entry = B.tune(packed, tolerance=tol, max_iter=max_iter, candidates=cands, use_cache=False)
+    x, res, ms = B.solve(packed, tolerance=tol, max_iter=max_iter)
+    torch.cuda.synchronize()
+    n_solves = 3 * n_systems
+    ok = sum(1 for r in res if r["status"] == 0)
+    # sequential: one solve per (system, rhs) through the plugin path, device vectors
+    mats = [cf.LduMatrix.from_ldu(L, ctx) for L in systems]
+    srcs = [[torch.from_numpy(np.ascontiguousarray(rhs[s][j])).to(dev) for j in range(3)]
+            for s in range(n_systems)]
+    psis = [torch.zeros(L.n, dtype=torch.float64, device=dev) for L in systems]
+    solver_ctrl = {"tolerance": tol, "maxIter": max_iter}
+    cf.cuFoamCG("U", mats[0], solver_ctrl).solve(psis[0], srcs[0][0])
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream(device)
+    e0.record(stream)
+    seq_iters = 0
+    for s in range(n_systems):
+        sol = cf.cuFoamCG("U", mats[s], solver_ctrl)
+        for j in range(3):
+            psis[s].zero_()
+            seq_iters += sol.solve(psis[s], srcs[s][j]).n_iterations
+    e1.record(stream)
+    torch.cuda.synchronize()
+    seq_ms = e0.elapsed_time(e1)
+    for m in mats:
+        m.close()
+    B.close()
+    return {"workload": f"{n_systems} lognormal 7-point boxes (16..64)^3 permuted x 3 rhs, CG FP64",
+            "rows": int(sizes.prod(axis=1).sum()), "tolerance": tol, "generate_s": round(gen_s, 1),
+            "autotuned": {"cluster": cfg[0], "threads": cfg[1], "order": cfg[2]},
+            "batched_ms": round(ms, 2), "batched_solves_per_s": round(n_solves / (ms * 1e-3), 1),
+            "batched_converged": ok, "sequential_ms": round(seq_ms, 2),
+            "sequential_solves_per_s": round(n_solves / (seq_ms * 1e-3), 1),
+            "speedup": round(seq_ms / ms, 3),
+            "iterations_batched": int(sum(r["n_iterations"] for r in res)),
+            "iterations_sequential": int(seq_iters)}
 
 
 def run_profile(args):
@@ -399,6 +514,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the mixed-vs-FP64 and batched-vs-sequential comparisons")
     ap.add_argument("--profile", action="store_true",
                     help="short host-driven run for an ncu capture (prints no JSON)")
     args = ap.parse_args()

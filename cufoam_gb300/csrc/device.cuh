@@ -24,6 +24,13 @@ constexpr unsigned kFull = 0xffffffffu;
 
 template <class T> __device__ __forceinline__ T ld_cg(const T *p) { return __ldcg(p); }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation may start while its predecessor drains; pdl_wait() blocks
+// until the predecessor grid has completed and its memory is visible (a
+// no-op for ordinary launches).  pdl_trigger() lets the successor launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Block tree over NV per-thread values in the reference's order: strides
 // 128 and 64 through shared memory, then 32..1 inside warp 0 (the shuffle
 // tree adds lane i+s into lane i exactly like the warp-synchronous steps).
@@ -71,6 +78,7 @@ __device__ __forceinline__ bool grid_reduce(T (&acc)[NV], T *partials, int strid
 {
     __shared__ T sm[NV * kBlock];
     __shared__ bool s_last;
+    pdl_trigger();
     block_tree<NV, T>(acc, sm);
     if (threadIdx.x == 0) {
 #pragma unroll

@@ -44,6 +44,7 @@ struct DevState {
     double rho0, rho1;   // CG / BiCG inner products
     double xi;           // CG / BiCG step length
     double theta;        // BiCG direction update factor
+    double beta;         // CG direction update factor rho0 / rho1 of the next step
     double omega;        // MR / MRJacobi / JMR / MRS step, Richardson relaxation
     double norm;         // latest ||r||_2 as recorded by the reference
     double norm0;        // initial ||r||_2
@@ -144,6 +145,7 @@ struct GraphEntry {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long cond = 0;
+    bool pdl = false;
 };
 
 struct Context {
@@ -155,6 +157,7 @@ struct Context {
     size_t l2_bytes = 0;
     std::string last_error;
     bool graphs_ok = true;
+    bool pdl_ok = true;        // programmatic launches accepted in loop graphs
 
     // workspace (grow-only, reused by every solve)
     DeviceBuffer vec[24];
@@ -185,6 +188,7 @@ struct Matrix {
     bool have_valT = false, have_32 = false, have_T32 = false;
     double diag_abs_min = 0.0;
     bool have_dmin = false;
+    bool from_csr = false;     // built from a CSR matrix (no LDU arrays)
 };
 
 // ---------------------------------------------------------------------------
@@ -205,6 +209,12 @@ void ldu2csr_into(Context *ctx, const cf_ldu_view &v, int32_t *ro, int32_t *col,
                   double *val, int memory);
 
 int stage_cap_for(const Matrix *m);
+Matrix *matrix_from_csr(Context *ctx, int n, int64_t nnz, const int32_t *ro, const int32_t *col,
+                        const double *val);
+void matrix_set_transpose_csr(Matrix *m, const int32_t *roT, const int32_t *colT, const double *valT);
+void matrix_set_inverse_diagonal(Matrix *m, const double *dinv);
+void csr_transpose(Context *ctx, int n_rows, int n_cols, int64_t nnz, const int32_t *ro,
+                   const int32_t *col, const double *val, int32_t *roT, int32_t *colT, double *valT);
 void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order);
 double norm_factor(Matrix *m, const double *b, const double *x, int norm_type, bool ref_order);
 void solve(Matrix *m, int solver, const cf_controls &c, const double *b, double *x,

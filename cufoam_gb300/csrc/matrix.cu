@@ -268,6 +268,84 @@ __global__ void __launch_bounds__(kBlock) k_spmv(int n, int cap, const int32_t *
 }
 
 // ---------------------------------------------------------------------------
+// matrices given as CSR (the libGIS-compatible entry points)
+// ---------------------------------------------------------------------------
+// FindDiag (gis/SparseSystem/kernels.h:447-464): the entry with col == row,
+// scanning the row while col <= row; rows without one read as 0.
+__global__ void k_csr_diag(int n, const int32_t *__restrict__ ro, const int32_t *__restrict__ col,
+                           const double *__restrict__ val, double *diag)
+{
+    CF_FOR_ELEMS(i, n) {
+        double d = 0.0;
+        for (int j = ro[i]; j < ro[i + 1] && col[j] <= i; ++j)
+            if (col[j] == i) d = val[j];
+        diag[i] = d;
+    }
+}
+
+__global__ void k_csr_check(int n, int n_cols, const int32_t *__restrict__ ro,
+                            const int32_t *__restrict__ col, int64_t nnz, int *err)
+{
+    CF_FOR_ELEMS(i, n) {
+        const int b = ro[i], e = ro[i + 1];
+        if (b < 0 || e < b || (int64_t)e > nnz) atomicOr(err, 1);
+        else
+            for (int j = b; j < e; ++j)
+                if (col[j] < 0 || col[j] >= n_cols) atomicOr(err, 2);
+    }
+}
+
+__global__ void k_count_cols(int n, const int32_t *__restrict__ ro, const int32_t *__restrict__ col,
+                             int32_t *cnt)
+{
+    CF_FOR_ELEMS(i, n)
+        for (int j = ro[i]; j < ro[i + 1]; ++j) atomicAdd(cnt + col[j], 1);
+}
+
+__global__ void k_transpose_place(int n, const int32_t *__restrict__ ro, const int32_t *__restrict__ col,
+                                  const double *__restrict__ val, const int32_t *__restrict__ roT,
+                                  int32_t *cursor, int32_t *colT, double *valT)
+{
+    CF_FOR_ELEMS(i, n)
+        for (int j = ro[i]; j < ro[i + 1]; ++j) {
+            const int c = col[j];
+            const int pos = roT[c] + atomicAdd(cursor + c, 1);
+            colT[pos] = i;
+            valT[pos] = val[j];
+        }
+}
+
+// sort each row of the transpose by (original) row index: the result equals
+// a stable sort of A's entries by column, as the reference's Transpose
+// (Thrust stable_sort_by_key, SolverSingleGPU.h:33-71) produces
+__global__ void k_sort_rows(int n, const int32_t *__restrict__ ro, int32_t *col, double *val)
+{
+    CF_FOR_ELEMS(i, n) {
+        const int b = ro[i], e = ro[i + 1];
+        for (int j = b + 1; j < e; ++j) {
+            const int c = col[j];
+            const double v = val[j];
+            int t = j - 1;
+            while (t >= b && col[t] > c) {
+                col[t + 1] = col[t];
+                val[t + 1] = val[t];
+                --t;
+            }
+            col[t + 1] = c;
+            val[t + 1] = v;
+        }
+    }
+}
+
+__global__ void k_same_pattern(int64_t m, const int32_t *__restrict__ a, const int32_t *__restrict__ b,
+                               int *diff)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (a[i] != b[i]) atomicOr(diff, 1);
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 static int grid_for(Context *ctx, int64_t work, int per_block = kBlock)
@@ -455,9 +533,15 @@ void matrix_update_values(Matrix *m, const double *diag, const double *lower, co
 // A^T values on A's pattern: the same fill with lower and upper swapped.
 // Equals the reference's Transpose (Thrust stable sort by column,
 // SolverSingleGPU.h:33-71) because row c of A^T lists A[i][c] by ascending i.
+static void matrix_transpose_from_csr(Matrix *m);
+
 void matrix_ensure_transpose(Matrix *m)
 {
     if (m->have_valT) return;
+    if (m->from_csr) {
+        matrix_transpose_from_csr(m);
+        return;
+    }
     Context *ctx = m->ctx;
     m->valT.ensure(sizeof(double) * (m->nnz + 4));
     CF_CUDA(cudaMemsetAsync(m->valT.as<double>() + m->nnz, 0, sizeof(double) * 4, ctx->stream));
@@ -518,6 +602,141 @@ void ldu2csr_into(Context *ctx, const cf_ldu_view &v, int32_t *ro, int32_t *col,
     download(ctx, col, tmp.col.ptr, sizeof(int32_t) * (size_t)tmp.nnz, memory);
     download(ctx, val, tmp.val.ptr, sizeof(double) * (size_t)tmp.nnz, memory);
     CF_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+// General device transpose of an n_rows x n_cols CSR matrix into caller
+// buffers (roT[n_cols+1], colT[nnz], valT[nnz]).
+void csr_transpose(Context *ctx, int n_rows, int n_cols, int64_t nnz, const int32_t *ro,
+                   const int32_t *col, const double *val, int32_t *roT, int32_t *colT, double *valT)
+{
+    DeviceBuffer cnt, tmp;
+    cnt.ensure(sizeof(int32_t) * ((size_t)n_cols + 1));
+    CF_CUDA(cudaMemsetAsync(cnt.ptr, 0, sizeof(int32_t) * ((size_t)n_cols + 1), ctx->stream));
+    const int g = grid_for(ctx, (int64_t)n_rows + 1);
+    if (n_rows > 0) {
+        k_count_cols<<<g, kBlock, 0, ctx->stream>>>(n_rows, ro, col, cnt.as<int32_t>() + 1);
+        CF_CHECK_LAUNCH();
+    }
+    // counts were written one slot to the right: roT = inclusive scan
+    exclusive_scan(ctx, n_cols + 1, cnt.as<int32_t>(), roT, tmp);
+    // exclusive scan of [0, c0, c1, ...] gives [0, 0, c0, ...]: shift by one
+    // instead: recompute from counts placed at [c] directly
+    CF_CUDA(cudaMemsetAsync(cnt.ptr, 0, sizeof(int32_t) * ((size_t)n_cols + 1), ctx->stream));
+    if (n_rows > 0) {
+        k_count_cols<<<g, kBlock, 0, ctx->stream>>>(n_rows, ro, col, cnt.as<int32_t>());
+        CF_CHECK_LAUNCH();
+    }
+    exclusive_scan(ctx, n_cols + 1, cnt.as<int32_t>(), roT, tmp);
+    CF_CUDA(cudaMemsetAsync(cnt.ptr, 0, sizeof(int32_t) * ((size_t)n_cols + 1), ctx->stream));
+    if (n_rows > 0) {
+        k_transpose_place<<<g, kBlock, 0, ctx->stream>>>(n_rows, ro, col, val, roT, cnt.as<int32_t>(),
+                                                         colT, valT);
+        CF_CHECK_LAUNCH();
+    }
+    if (n_cols > 0) {
+        k_sort_rows<<<grid_for(ctx, n_cols), kBlock, 0, ctx->stream>>>(n_cols, roT, colT, valT);
+        CF_CHECK_LAUNCH();
+    }
+}
+
+static bool same_pattern(Context *ctx, int64_t m, const int32_t *a, const int32_t *b)
+{
+    if (m == 0) return true;
+    DeviceBuffer flag;
+    flag.ensure(sizeof(int));
+    CF_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
+    k_same_pattern<<<grid_for(ctx, m), kBlock, 0, ctx->stream>>>(m, a, b, flag.as<int>());
+    CF_CHECK_LAUNCH();
+    return read_flag(ctx, flag.as<int>()) == 0;
+}
+
+// A device matrix from a square CSR matrix in device memory (copied into
+// padded buffers; the diagonal found as the reference's FindDiag does).
+Matrix *matrix_from_csr(Context *ctx, int n, int64_t nnz, const int32_t *ro, const int32_t *col,
+                        const double *val)
+{
+    require(n > 0 && nnz >= 0 && nnz < INT32_MAX, CF_BAD_INPUT, "bad CSR size");
+    Matrix *m = new Matrix();
+    try {
+        m->ctx = ctx;
+        m->n = n;
+        m->nf = -1;
+        m->nnz = nnz;
+        m->from_csr = true;
+        const size_t pad = 4;
+        m->ro.ensure(sizeof(int32_t) * (n + 1 + pad));
+        m->col.ensure(sizeof(int32_t) * (nnz + pad));
+        m->val.ensure(sizeof(double) * (nnz + pad));
+        CF_CUDA(cudaMemcpyAsync(m->ro.ptr, ro, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToDevice, ctx->stream));
+        CF_CUDA(cudaMemcpyAsync(m->col.ptr, col, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, ctx->stream));
+        CF_CUDA(cudaMemcpyAsync(m->val.ptr, val, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, ctx->stream));
+        CF_CUDA(cudaMemsetAsync(m->col.as<int32_t>() + nnz, 0, sizeof(int32_t) * pad, ctx->stream));
+        CF_CUDA(cudaMemsetAsync(m->val.as<double>() + nnz, 0, sizeof(double) * pad, ctx->stream));
+        DeviceBuffer flag;
+        flag.ensure(sizeof(int) * 2);
+        CF_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int) * 2, ctx->stream));
+        const int gc = grid_for(ctx, (int64_t)n + 1);
+        k_csr_check<<<gc, kBlock, 0, ctx->stream>>>(n, n, m->ro.as<int32_t>(), m->col.as<int32_t>(), nnz,
+                                                    flag.as<int>());
+        CF_CHECK_LAUNCH();
+        int32_t last = 0;
+        CF_CUDA(cudaMemcpyAsync(&last, m->ro.as<int32_t>() + n, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        const int err = read_flag(ctx, flag.as<int>());
+        require(err == 0 && (int64_t)last == nnz, CF_BAD_INPUT, "invalid CSR matrix");
+        m->diag.ensure(sizeof(double) * (n + pad));
+        k_csr_diag<<<gc, kBlock, 0, ctx->stream>>>(n, m->ro.as<int32_t>(), m->col.as<int32_t>(),
+                                                   m->val.as<double>(), m->diag.as<double>());
+        CF_CHECK_LAUNCH();
+        m->dinv.ensure(sizeof(double) * (n + pad));
+        m->dinv_sqrt.ensure(sizeof(double) * (n + pad));
+        k_diag_derived<<<gc, kBlock, 0, ctx->stream>>>(n, m->diag.as<double>(), m->dinv.as<double>(),
+                                                       m->dinv_sqrt.as<double>());
+        CF_CHECK_LAUNCH();
+        CF_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
+        k_max_chunk<<<grid_for(ctx, (n + 31) / 32), kBlock, 0, ctx->stream>>>(n, m->ro.as<int32_t>(),
+                                                                               flag.as<int>());
+        CF_CHECK_LAUNCH();
+        m->max_chunk = read_flag(ctx, flag.as<int>());
+    } catch (...) {
+        delete m;
+        throw;
+    }
+    return m;
+}
+
+// A^T values on A's pattern from a CSR A^T (given, or computed): the
+// patterns must coincide (true for every LDU matrix).
+void matrix_set_transpose_csr(Matrix *m, const int32_t *roT, const int32_t *colT, const double *valT)
+{
+    Context *ctx = m->ctx;
+    require(same_pattern(ctx, (int64_t)m->n + 1, m->ro.as<int32_t>(), roT) &&
+                same_pattern(ctx, m->nnz, m->col.as<int32_t>(), colT),
+            CF_UNSUPPORTED, "A^T must have the sparsity pattern of A (structurally symmetric matrix)");
+    m->valT.ensure(sizeof(double) * (m->nnz + 4));
+    CF_CUDA(cudaMemcpyAsync(m->valT.ptr, valT, sizeof(double) * m->nnz, cudaMemcpyDeviceToDevice, ctx->stream));
+    CF_CUDA(cudaMemsetAsync(m->valT.as<double>() + m->nnz, 0, sizeof(double) * 4, ctx->stream));
+    m->have_valT = true;
+    m->have_T32 = false;
+}
+
+static void matrix_transpose_from_csr(Matrix *m)
+{
+    Context *ctx = m->ctx;
+    DeviceBuffer roT, colT, valT;
+    roT.ensure(sizeof(int32_t) * ((size_t)m->n + 1));
+    colT.ensure(sizeof(int32_t) * ((size_t)m->nnz + 1));
+    valT.ensure(sizeof(double) * ((size_t)m->nnz + 1));
+    csr_transpose(ctx, m->n, m->n, m->nnz, m->ro.as<int32_t>(), m->col.as<int32_t>(), m->val.as<double>(),
+                  roT.as<int32_t>(), colT.as<int32_t>(), valT.as<double>());
+    matrix_set_transpose_csr(m, roT.as<int32_t>(), colT.as<int32_t>(), valT.as<double>());
+}
+
+// 1/a_ii taken from a diagonal preconditioner matrix (MRS's invM).
+void matrix_set_inverse_diagonal(Matrix *m, const double *dinv)
+{
+    Context *ctx = m->ctx;
+    CF_CUDA(cudaMemcpyAsync(m->dinv.ptr, dinv, sizeof(double) * m->n, cudaMemcpyDeviceToDevice, ctx->stream));
 }
 
 int stage_cap_for(const Matrix *m)

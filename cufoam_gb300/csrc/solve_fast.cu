@@ -25,6 +25,16 @@ namespace cf {
 //   spmv:   q = A p_k, (p_k, q) -> xi_k
 //   update: r -= xi_k q, (r, r) -> stopping test, beta
 // ---------------------------------------------------------------------------
+// Element-wise passes process four elements per thread per step, loading
+// all inputs before any store, so each thread keeps several independent
+// loads in flight.
+#define CF_X4_LOOP(i, n)                                                   \
+    const int stride_ = gridDim.x * kBlock;                                \
+    int i = blockIdx.x * kBlock + threadIdx.x;                             \
+    for (; i + 3 * stride_ < (n); i += 4 * stride_)
+#define CF_X4_IDX(i, u) ((i) + (u) * stride_)
+#define CF_X4_TAIL(i, n) for (; i < (n); i += stride_)
+
 __global__ void __launch_bounds__(kBlock) k_f_cg_prep(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
@@ -38,9 +48,23 @@ __global__ void __launch_bounds__(kBlock) k_f_cg_prep(const SolveArgs *__restric
         CF_FOR_ELEMS(i, n) p[i] = r[i];
         return;
     }
-    const double beta = ld_cg(&st->rho0) / ld_cg(&st->rho1);
+    const double beta = ld_cg(&st->beta);
     const double xi = ld_cg(&st->xi);
-    CF_FOR_ELEMS(i, n) {
+    CF_X4_LOOP(i, n) {
+        double pv[4], xv[4], rv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            pv[u] = p[CF_X4_IDX(i, u)];
+            xv[u] = x[CF_X4_IDX(i, u)];
+            rv[u] = r[CF_X4_IDX(i, u)];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            x[CF_X4_IDX(i, u)] = fma_t(xi, pv[u], xv[u]);
+            p[CF_X4_IDX(i, u)] = fma_t(beta, pv[u], rv[u]);
+        }
+    }
+    CF_X4_TAIL(i, n) {
         const double pi = p[i];
         x[i] = fma_t(xi, pi, x[i]);
         p[i] = fma_t(beta, pi, r[i]);
@@ -76,7 +100,7 @@ __global__ void __launch_bounds__(kBlock) k_f_cg_spmv(const SolveArgs *__restric
     }
 }
 
-// r -= xi q, (r, r): two elements per thread per step for memory parallelism
+// r -= xi q, (r, r)
 __global__ void __launch_bounds__(kBlock) k_f_cg_update(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
@@ -85,28 +109,33 @@ __global__ void __launch_bounds__(kBlock) k_f_cg_update(const SolveArgs *__restr
     const double xi = ld_cg(&st->xi);
     double *__restrict__ r = a->r[0];
     const double *__restrict__ q = a->q;
-    double a0 = 0.0, a1 = 0.0;
-    const int stride = gridDim.x * kBlock;
-    int i = blockIdx.x * kBlock + threadIdx.x;
-    for (; i + stride < n; i += 2 * stride) {
-        const double q0 = q[i], q1 = q[i + stride], r0 = r[i], r1 = r[i + stride];
-        const double n0 = fma_t(-xi, q0, r0), n1 = fma_t(-xi, q1, r1);
-        r[i] = n0;
-        r[i + stride] = n1;
-        a0 = fma_t(n0, n0, a0);
-        a1 = fma_t(n1, n1, a1);
+    double part[4] = {0.0, 0.0, 0.0, 0.0};
+    CF_X4_LOOP(i, n) {
+        double qv[4], rv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            qv[u] = q[CF_X4_IDX(i, u)];
+            rv[u] = r[CF_X4_IDX(i, u)];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double ri = fma_t(-xi, qv[u], rv[u]);
+            r[CF_X4_IDX(i, u)] = ri;
+            part[u] = fma_t(ri, ri, part[u]);
+        }
     }
-    if (i < n) {
-        const double n0 = fma_t(-xi, q[i], r[i]);
-        r[i] = n0;
-        a0 = fma_t(n0, n0, a0);
+    CF_X4_TAIL(i, n) {
+        const double ri = fma_t(-xi, q[i], r[i]);
+        r[i] = ri;
+        part[0] = fma_t(ri, ri, part[0]);
     }
-    double acc[1] = {a0 + a1};
+    double acc[1] = {(part[0] + part[1]) + (part[2] + part[3])};
     double tot[1];
     if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_B], false, tot) &&
         threadIdx.x == 0) {
         st->rho1 = st->rho0;
         st->rho0 = tot[0];
+        st->beta = st->rho0 / st->rho1;
         st->x_pending = 1;
         finish_step(a, st, sqrt(tot[0]));
     }
@@ -151,7 +180,24 @@ __global__ void __launch_bounds__(kBlock) k_f_bicg_prep(const SolveArgs *__restr
     const double theta = ld_cg(&st->theta);
     const double xi = ld_cg(&st->xi);
     const bool xpend = ld_cg(&st->x_pending) != 0;
-    CF_FOR_ELEMS(i, n) {
+    CF_X4_LOOP(i, n) {
+        double pv[4], rv[4], psv[4], rsv[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            pv[u] = p[CF_X4_IDX(i, u)];
+            rv[u] = r[CF_X4_IDX(i, u)];
+            psv[u] = ps[CF_X4_IDX(i, u)];
+            rsv[u] = rs[CF_X4_IDX(i, u)];
+            xv[u] = xpend ? x[CF_X4_IDX(i, u)] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (xpend) x[CF_X4_IDX(i, u)] = fma_t(xi, pv[u], xv[u]);
+            p[CF_X4_IDX(i, u)] = fma_t(theta, pv[u], rv[u]);
+            ps[CF_X4_IDX(i, u)] = fma_t(theta, psv[u], rsv[u]);
+        }
+    }
+    CF_X4_TAIL(i, n) {
         const double pi = p[i];
         if (xpend) x[i] = fma_t(xi, pi, x[i]);
         p[i] = fma_t(theta, pi, r[i]);
@@ -213,7 +259,22 @@ __global__ void __launch_bounds__(kBlock) k_f_jac_prep(const SolveArgs *__restri
     const double *__restrict__ dinv = a->dinv;
     double *__restrict__ d = a->w[1];
     double *__restrict__ x = a->x;
-    CF_FOR_ELEMS(i, n) {
+    CF_X4_LOOP(i, n) {
+        double dv[4], rv[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            dv[u] = dinv[CF_X4_IDX(i, u)];
+            rv[u] = r[CF_X4_IDX(i, u)];
+            xv[u] = x[CF_X4_IDX(i, u)];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double di = __dmul_rn(dv[u], rv[u]);
+            d[CF_X4_IDX(i, u)] = di;
+            x[CF_X4_IDX(i, u)] = fma_t(1.0, di, xv[u]);
+        }
+    }
+    CF_X4_TAIL(i, n) {
         const double di = __dmul_rn(dinv[i], r[i]);
         d[i] = di;
         x[i] = fma_t(1.0, di, x[i]);
@@ -259,7 +320,17 @@ __global__ void __launch_bounds__(kBlock) k_f_rich_prep(const SolveArgs *__restr
     const double omega = ld_cg(&st->omega);
     const double *__restrict__ r = a->r[0];
     double *__restrict__ x = a->x;
-    CF_FOR_ELEMS(i, n) x[i] = fma_t(omega, r[i], x[i]);
+    CF_X4_LOOP(i, n) {
+        double rv[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            rv[u] = r[CF_X4_IDX(i, u)];
+            xv[u] = x[CF_X4_IDX(i, u)];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[CF_X4_IDX(i, u)] = fma_t(omega, rv[u], xv[u]);
+    }
+    CF_X4_TAIL(i, n) x[i] = fma_t(omega, r[i], x[i]);
 }
 
 __global__ void __launch_bounds__(kBlock) k_f_rich_spmv(const SolveArgs *__restrict__ a)
@@ -346,8 +417,123 @@ __global__ void __launch_bounds__(kBlock) k_f_mr_spmv(const SolveArgs *__restric
         st->omega = tot[0] / tot[1];
 }
 
+// BiCG update: r -= xi q, r* -= xi q*, ||r||, (r, r*); the step logic of
+// SolverSingleGPU.h:632-671 (stop when ||r|| < tol, theta = rho0 / rho1).
+__global__ void __launch_bounds__(kBlock) k_f_bicg_update(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, true);
+    const int n = a->n;
+    const double xi = ld_cg(&st->xi);
+    double *__restrict__ r = a->r[0];
+    double *__restrict__ rs = a->rs;
+    const double *__restrict__ q = a->q;
+    const double *__restrict__ qs = a->qs;
+    double p0[4] = {0.0, 0.0, 0.0, 0.0}, p1[4] = {0.0, 0.0, 0.0, 0.0};
+    CF_X4_LOOP(i, n) {
+        double qv[4], rv[4], qsv[4], rsv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            qv[u] = q[CF_X4_IDX(i, u)];
+            rv[u] = r[CF_X4_IDX(i, u)];
+            qsv[u] = qs[CF_X4_IDX(i, u)];
+            rsv[u] = rs[CF_X4_IDX(i, u)];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double ri = fma_t(-xi, qv[u], rv[u]);
+            const double rsi = fma_t(-xi, qsv[u], rsv[u]);
+            r[CF_X4_IDX(i, u)] = ri;
+            rs[CF_X4_IDX(i, u)] = rsi;
+            p0[u] = fma_t(ri, ri, p0[u]);
+            p1[u] = fma_t(ri, rsi, p1[u]);
+        }
+    }
+    CF_X4_TAIL(i, n) {
+        const double ri = fma_t(-xi, q[i], r[i]);
+        const double rsi = fma_t(-xi, qs[i], rs[i]);
+        r[i] = ri;
+        rs[i] = rsi;
+        p0[0] = fma_t(ri, ri, p0[0]);
+        p1[0] = fma_t(ri, rsi, p1[0]);
+    }
+    double acc[2] = {(p0[0] + p0[1]) + (p0[2] + p0[3]), (p1[0] + p1[1]) + (p1[2] + p1[3])};
+    double tot[2];
+    if (grid_reduce<2, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_B], false, tot) &&
+        threadIdx.x == 0) {
+        const double norm = sqrt(tot[0]);
+        const int k = st->k + 1;
+        st->k = k;
+        st->norm = norm;
+        st->x_pending = 1;
+        if (a->hist && k < st->hist_cap) a->hist[k] = norm;
+        bool cont = true;
+        int status = CF_NOT_CONVERGED;
+        if (norm < st->tol && k >= st->min_steps) { cont = false; status = CF_OK; }
+        else if (k >= st->max_steps) { cont = false; }
+        else if (!isfinite(norm)) { cont = false; status = CF_NONFINITE; }
+        st->body_count += 1;
+        if (st->body_count > k + 2 || (a->abort_flag && *a->abort_flag)) { cont = false; status = CF_TIMEOUT; }
+        if (cont) {
+            st->rho1 = st->rho0;
+            st->rho0 = tot[1];
+            st->theta = st->rho0 / st->rho1;
+        } else {
+            st->done = 1;
+            st->status = status;
+        }
+        set_loop_condition(a, cont);
+    }
+}
+
+// MR family update: x += alpha d, r -= alpha y, ||r|| (d = r for MR, the
+// prep vector otherwise).
+template <int KIND>
+__global__ void __launch_bounds__(kBlock) k_f_mr_update(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, true);
+    const int n = a->n;
+    const double alpha = ld_cg(&st->omega);
+    double *__restrict__ r = a->r[0];
+    double *__restrict__ x = a->x;
+    const double *__restrict__ y = a->w[0];
+    const double *__restrict__ d = (KIND == 0) ? a->r[0] : a->w[1];
+    double part[4] = {0.0, 0.0, 0.0, 0.0};
+    CF_X4_LOOP(i, n) {
+        double rv[4], xv[4], yv[4], dv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            rv[u] = r[CF_X4_IDX(i, u)];
+            xv[u] = x[CF_X4_IDX(i, u)];
+            yv[u] = y[CF_X4_IDX(i, u)];
+            dv[u] = (KIND == 0) ? rv[u] : d[CF_X4_IDX(i, u)];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            x[CF_X4_IDX(i, u)] = fma_t(alpha, dv[u], xv[u]);
+            const double ri = fma_t(-alpha, yv[u], rv[u]);
+            r[CF_X4_IDX(i, u)] = ri;
+            part[u] = fma_t(ri, ri, part[u]);
+        }
+    }
+    CF_X4_TAIL(i, n) {
+        const double ri0 = r[i];
+        const double di = (KIND == 0) ? ri0 : d[i];
+        x[i] = fma_t(alpha, di, x[i]);
+        const double ri = fma_t(-alpha, y[i], ri0);
+        r[i] = ri;
+        part[0] = fma_t(ri, ri, part[0]);
+    }
+    double acc[1] = {(part[0] + part[1]) + (part[2] + part[3])};
+    double tot[1];
+    if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_B], false, tot) &&
+        threadIdx.x == 0)
+        finish_step(a, st, sqrt(tot[0]));
+}
+
 // ---------------------------------------------------------------------------
-Kernels fast_body_kernels(int solver, const void *mr_update[4], const void *bicg_update)
+Kernels fast_body_kernels(int solver)
 {
     Kernels k;
     switch (solver) {
@@ -359,7 +545,7 @@ Kernels fast_body_kernels(int solver, const void *mr_update[4], const void *bicg
     case CF_BICG:
         k.k0 = (const void *)k_f_bicg_prep;
         k.k1 = (const void *)k_f_bicg_spmv;
-        k.k2 = bicg_update;
+        k.k2 = (const void *)k_f_bicg_update;
         break;
     case CF_JACOBI:
         k.k0 = (const void *)k_f_jac_prep;
@@ -371,22 +557,22 @@ Kernels fast_body_kernels(int solver, const void *mr_update[4], const void *bicg
         break;
     case CF_MR:
         k.k1 = (const void *)k_f_mr_spmv<0>;
-        k.k2 = mr_update[0];
+        k.k2 = (const void *)k_f_mr_update<0>;
         break;
     case CF_MRJACOBI:
         k.k0 = (const void *)k_f_mr_prep<1>;
         k.k1 = (const void *)k_f_mr_spmv<1>;
-        k.k2 = mr_update[1];
+        k.k2 = (const void *)k_f_mr_update<1>;
         break;
     case CF_MRS:
         k.k0 = (const void *)k_f_mr_prep<2>;
         k.k1 = (const void *)k_f_mr_spmv<2>;
-        k.k2 = mr_update[2];
+        k.k2 = (const void *)k_f_mr_update<2>;
         break;
     case CF_JMR:
         k.k0 = (const void *)k_f_mr_prep<3>;
         k.k1 = (const void *)k_f_mr_spmv<3>;
-        k.k2 = mr_update[3];
+        k.k2 = (const void *)k_f_mr_update<3>;
         break;
     default: break;
     }

@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(const SolveArgs *__restrict_
     CF_STAGE(double, cap);
     const int k = ld_cg(&st->k) + 1;
     const bool first = (k == 1);
-    const double beta = first ? 0.0 : ld_cg(&st->rho0) / ld_cg(&st->rho1);
+    const double beta = first ? 0.0 : ld_cg(&st->beta); // rho0 / rho1, formed once
     const double xi_prev = ld_cg(&st->xi);
     const bool xpend = ld_cg(&st->x_pending) != 0;
     const double *pin = a->p[(k + 1) & 1];
@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(const SolveArgs *__restric
                                a->ref_order, tot) && threadIdx.x == 0) {
         st->rho1 = st->rho0;
         st->rho0 = tot[0];
+        st->beta = st->rho0 / st->rho1;
         st->x_pending = 1;
         finish_step(a, st, sqrt(tot[0]));
     }
@@ -658,10 +659,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     const bool prof = c.profile_kernels != 0;
     bool use_graph = c.use_graph != 0 && ctx->graphs_ok && !prof;
     GraphEntry *ge = nullptr;
-    const void *mr_upd[4] = {(const void *)k_mr_update<0>, (const void *)k_mr_update<1>,
-                             (const void *)k_mr_update<2>, (const void *)k_mr_update<3>};
-    const Kernels kk = ref ? body_kernels(solver)
-                           : fast_body_kernels(solver, mr_upd, (const void *)k_bicg_update);
+    const Kernels kk = ref ? body_kernels(solver) : fast_body_kernels(solver);
     SolveArgs *d_args = ctx->args.as<SolveArgs>();
     if (use_graph && !mixed) {
         try {
@@ -737,11 +735,11 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
             for (int i = 0; i < chunk; ++i) {
                 cudaEvent_t *ev = prof ? &ctx->prof_events[4 * i] : nullptr;
                 if (prof) CF_CUDA(cudaEventRecord(ev[0], ctx->stream));
-                if (kk.k0) launch(ctx, ctx->stream, kk.k0, l0, args1);
+                if (kk.k0) launch(ctx, ctx->stream, kk.k0, l0, args1, !prof);
                 if (prof) CF_CUDA(cudaEventRecord(ev[1], ctx->stream));
-                launch(ctx, ctx->stream, kk.k1, l1, args1);
+                launch(ctx, ctx->stream, kk.k1, l1, args1, !prof);
                 if (prof) CF_CUDA(cudaEventRecord(ev[2], ctx->stream));
-                if (kk.k2) launch(ctx, ctx->stream, kk.k2, l2, args1);
+                if (kk.k2) launch(ctx, ctx->stream, kk.k2, l2, args1, !prof);
                 if (prof) CF_CUDA(cudaEventRecord(ev[3], ctx->stream));
             }
             CF_CUDA(cudaMemcpyAsync(ctx->h_state, A.st, sizeof(DevState), cudaMemcpyDeviceToHost,

@@ -63,8 +63,11 @@ static __device__ __noinline__ void finish_step(const SolveArgs *a, DevState *st
     set_loop_condition(a, cont);
 }
 
-// A body kernel that finds the loop already finished ends the graph loop.
+// Prologue of every loop-body kernel: wait for the predecessor kernel
+// (programmatic launches start early), then end the graph loop if the solve
+// has already finished.
 #define CF_EXIT_IF_DONE(a, st, is_last_kernel)                                  \
+    pdl_wait();                                                                 \
     if (ld_cg(&(st)->done)) {                                                   \
         if ((is_last_kernel) && blockIdx.x == 0 && threadIdx.x == 0)            \
             set_loop_condition(a, false);                                       \
@@ -99,27 +102,41 @@ static Launch launch_cfg(Context *ctx, const void *kern, bool is_spmv, int cap, 
     return l;
 }
 
-static void launch(Context *ctx, cudaStream_t s, const void *kern, const Launch &l, void **args)
+// pdl: launch with programmatic stream serialisation (the kernel must begin
+// with pdl_wait(), as every loop-body kernel does through CF_EXIT_IF_DONE).
+static void launch(Context *ctx, cudaStream_t s, const void *kern, const Launch &l, void **args,
+                   bool pdl = false)
 {
-    CF_CUDA(cudaLaunchKernel(kern, dim3(l.grid), dim3(kBlock), args, l.smem, s));
+    (void)ctx;
+    if (!pdl) {
+        CF_CUDA(cudaLaunchKernel(kern, dim3(l.grid), dim3(kBlock), args, l.smem, s));
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(l.grid);
+    cfg.blockDim = dim3(kBlock);
+    cfg.dynamicSmemBytes = l.smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    CF_CUDA(cudaLaunchKernelExC(&cfg, kern, args));
 }
 
 static void launch_body(Context *ctx, cudaStream_t s, const Kernels &kk, int cap, bool ref,
-                        SolveArgs *d_args)
+                        SolveArgs *d_args, bool pdl = false)
 {
     void *args[] = {&d_args};
-    if (kk.k0) launch(ctx, s, kk.k0, launch_cfg(ctx, kk.k0, false, cap, ref, kk.value_bytes), args);
-    launch(ctx, s, kk.k1, launch_cfg(ctx, kk.k1, kk.k1_spmv, cap, ref, kk.value_bytes), args);
-    if (kk.k2) launch(ctx, s, kk.k2, launch_cfg(ctx, kk.k2, kk.k2_spmv, cap, ref, kk.value_bytes), args);
+    if (kk.k0) launch(ctx, s, kk.k0, launch_cfg(ctx, kk.k0, false, cap, ref, kk.value_bytes), args, pdl);
+    launch(ctx, s, kk.k1, launch_cfg(ctx, kk.k1, kk.k1_spmv, cap, ref, kk.value_bytes), args, pdl);
+    if (kk.k2) launch(ctx, s, kk.k2, launch_cfg(ctx, kk.k2, kk.k2_spmv, cap, ref, kk.value_bytes), args, pdl);
 }
 
-static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int precision, int cap,
-                              bool ref, SolveArgs *d_args)
+static bool build_loop_graph(Context *ctx, const Kernels &kk, int cap, bool ref, SolveArgs *d_args,
+                             bool pdl, GraphEntry &ge)
 {
-    GraphKey key{solver, precision, ref ? 1 : 0, cap, 0};
-    auto it = ctx->graphs.find(key);
-    if (it != ctx->graphs.end()) return &it->second;
-    GraphEntry ge;
     cudaStream_t cs = nullptr;
     try {
         CF_CUDA(cudaGraphCreate(&ge.graph, 0));
@@ -137,13 +154,15 @@ static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int p
         CF_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         CF_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal));
-        launch_body(ctx, cs, kk, cap, ref, d_args);
+        launch_body(ctx, cs, kk, cap, ref, d_args, pdl);
         cudaGraph_t out = nullptr;
         CF_CUDA(cudaStreamEndCapture(cs, &out));
         CF_CUDA(cudaStreamDestroy(cs));
         cs = nullptr;
         CF_CUDA(cudaGraphInstantiate(&ge.exec, ge.graph, 0));
-    } catch (...) {
+        ge.pdl = pdl;
+        return true;
+    } catch (const Error &) {
         if (cs) {
             cudaGraph_t junk = nullptr;
             cudaStreamEndCapture(cs, &junk);
@@ -151,13 +170,31 @@ static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int p
         }
         if (ge.exec) cudaGraphExecDestroy(ge.exec);
         if (ge.graph) cudaGraphDestroy(ge.graph);
+        ge = GraphEntry();
         cudaGetLastError();
-        throw;
+        return false;
+    }
+}
+
+// The device-driven loop of one solver configuration, built once per
+// context: with programmatic launches between the body kernels where the
+// driver accepts them in a conditional body, else without.
+static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int precision, int cap,
+                              bool ref, SolveArgs *d_args)
+{
+    GraphKey key{solver, precision, ref ? 1 : 0, cap, 0};
+    auto it = ctx->graphs.find(key);
+    if (it != ctx->graphs.end()) return &it->second;
+    GraphEntry ge;
+    if (!(ctx->pdl_ok && build_loop_graph(ctx, kk, cap, ref, d_args, true, ge))) {
+        ctx->pdl_ok = false;
+        if (!build_loop_graph(ctx, kk, cap, ref, d_args, false, ge))
+            throw Error{CF_CUDA_ERROR, "cannot build the solver loop graph"};
     }
     return &(ctx->graphs[key] = ge);
 }
 
-Kernels fast_body_kernels(int solver, const void *mr_update[4], const void *bicg_update);
+Kernels fast_body_kernels(int solver);
 const void *fast_flush_kernel();
 
 } // namespace cf
