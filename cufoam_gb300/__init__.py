@@ -185,6 +185,20 @@ class LduMatrix:
         self._lib.cf_matrix_shape(self._h, C.byref(n), C.byref(f), C.byref(z))
         return n.value, f.value, z.value
 
+    _FORMATS = {"auto": 0, "csr": 1, "sell": 2}
+
+    def set_format(self, fmt: str) -> None:
+        """Storage the fast kernels read: "auto" (SELL-32 when the padding
+        stays within 20% of nnz, else CSR), "csr" or "sell"."""
+        self.ctx.check(self._lib.cf_matrix_set_format(self._h, self._FORMATS[fmt]),
+                       "cf_matrix_set_format")
+
+    def format(self):
+        """(format the fast kernels use, stored entries incl. padding)."""
+        f, z = C.c_int32(), C.c_int64()
+        self.ctx.check(self._lib.cf_matrix_format(self._h, C.byref(f), C.byref(z)), "cf_matrix_format")
+        return {1: "csr", 2: "sell"}[f.value], z.value
+
     def update_values(self, diag, lower, upper) -> None:
         pd, m1, k1 = _ptr(diag, np.float64, "diag")
         pl, m2, k2 = _ptr(lower, np.float64, "lower")

@@ -18,6 +18,7 @@ CF_MEM_HOST, CF_MEM_DEVICE = 0, 1
 CF_PREC_FP64, CF_PREC_MIXED = 0, 1
 CF_REDUCE_FAST, CF_REDUCE_REFERENCE = 0, 1
 CF_NORM_REFERENCE_L2, CF_NORM_OPENFOAM_L1 = 0, 1
+CF_FORMAT_AUTO, CF_FORMAT_CSR, CF_FORMAT_SELL = 0, 1, 2
 
 
 class cf_ldu_view(C.Structure):
@@ -39,7 +40,8 @@ class cf_controls(C.Structure):
                 ("history", C.c_void_p), ("history_capacity", C.c_int32),
                 ("use_graph", C.c_int32), ("time_limit_s", C.c_double),
                 ("profile_kernels", C.c_int32), ("transpose", C.c_int32),
-                ("reserved", C.c_int32 * 6)]
+                ("absolute_tolerance", C.c_int32), ("history_time", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class cf_perf(C.Structure):
@@ -108,6 +110,8 @@ def load(build_if_missing: bool = True):
         "cf_matrix_shape": (C.c_int32, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                         C.POINTER(C.c_int64)]),
         "cf_matrix_export_csr": (C.c_int32, [P, C.c_int32, P, P, P, C.c_int32]),
+        "cf_matrix_set_format": (C.c_int32, [P, C.c_int32]),
+        "cf_matrix_format": (C.c_int32, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
         "cf_ldu2csr": (C.c_int32, [P, C.POINTER(cf_ldu_view), P, P, P, C.c_int32]),
         "cf_spmv": (C.c_int32, [P, C.c_int32, P, P, C.c_int32, C.c_int32]),
         "cf_norm_factor": (C.c_int32, [P, P, P, C.c_int32, C.c_int32, C.c_int32,

@@ -61,6 +61,44 @@ def build_plugin(force: bool = False) -> str:
     return PLUGIN_LIB
 
 
+COMPAT_DIR = os.path.join(HERE, "compat")
+GIS_LIB = os.path.join(BUILD_DIR, "libGIS.so")
+GIS_HARNESS = os.path.join(BUILD_DIR, "libgis_harness.so")
+
+
+def cuda_home() -> str:
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+
+
+def build_gis(force: bool = False) -> str:
+    """libGIS.so: the reference solver library's gis.h interface on this
+    library (compat/gis_compat.cu), plus the ctypes harness that drives it
+    as the plugins do."""
+    src = os.path.join(COMPAT_DIR, "gis_compat.cu")
+    hdr = os.path.join(COMPAT_DIR, "SingleGPUCompat.h")
+    deps = [src, hdr, os.path.join(CSRC, "internal.h"), os.path.join(INCLUDE, "cufoam_gb300.h"), LIB_PATH]
+    if force or not os.path.exists(GIS_LIB) or os.path.getmtime(GIS_LIB) < _newest(deps):
+        tmp = GIS_LIB + f".tmp{os.getpid()}"
+        cmd = [nvcc()] + _flags() + ["-I" + COMPAT_DIR, "-shared", src, "-o", tmp,
+                                     "-L" + BUILD_DIR, "-lcufoam_gb300", "-Xlinker", "-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"libGIS build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, GIS_LIB)
+    hsrc = os.path.join(COMPAT_DIR, "gis_harness.cpp")
+    if force or not os.path.exists(GIS_HARNESS) or os.path.getmtime(GIS_HARNESS) < _newest([hsrc, hdr, GIS_LIB]):
+        tmp = GIS_HARNESS + f".tmp{os.getpid()}"
+        cu = cuda_home()
+        cmd = ["g++", "-O2", "-std=c++14", "-shared", "-fPIC", "-Wall", "-I" + COMPAT_DIR,
+               "-I" + os.path.join(cu, "include"), hsrc, "-L" + BUILD_DIR, "-lGIS",
+               "-L" + os.path.join(cu, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"gis harness build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, GIS_HARNESS)
+    return GIS_LIB
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD_DIR, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "cufoam_gb300.h")]
@@ -96,6 +134,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB_PATH)
     build_plugin(force)
+    build_gis(force)
     return LIB_PATH
 
 

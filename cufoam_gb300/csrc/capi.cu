@@ -319,6 +319,32 @@ cf_status cf_matrix_update_values(cf_matrix *m, const double *diag, const double
     });
 }
 
+cf_status cf_matrix_set_format(cf_matrix *m, int32_t format)
+{
+    if (!m) return CF_BAD_INPUT;
+    return guarded(m->owner, [&] {
+        cf::require(format == CF_FORMAT_AUTO || format == CF_FORMAT_CSR || format == CF_FORMAT_SELL,
+                    CF_BAD_INPUT, "bad format");
+        cf::Matrix *mi = m->impl;
+        if (mi->format_request != format) {
+            mi->format_request = format;
+            mi->sell = -1;
+            mi->have_sval = mi->have_svalT = mi->have_sval32 = mi->have_svalT32 = false;
+        }
+    });
+}
+
+cf_status cf_matrix_format(cf_matrix *m, int32_t *format, int64_t *stored_entries)
+{
+    if (!m) return CF_BAD_INPUT;
+    return guarded(m->owner, [&] {
+        const bool sell = cf::matrix_ensure_sell(m->impl, false, false);
+        CF_CUDA(cudaStreamSynchronize(m->owner->impl->stream));
+        if (format) *format = sell ? CF_FORMAT_SELL : CF_FORMAT_CSR;
+        if (stored_entries) *stored_entries = sell ? m->impl->sell_nnz : m->impl->nnz;
+    });
+}
+
 void cf_matrix_destroy(cf_matrix *m)
 {
     if (!m) return;

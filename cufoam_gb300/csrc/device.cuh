@@ -296,4 +296,125 @@ __device__ __forceinline__ void set_loop_condition(const SolveArgs *a, bool cont
     if (a->use_cond) cudaGraphSetConditional(a->cond, cont ? 1u : 0u);
 }
 
+// ---------------------------------------------------------------------------
+// SELL-32: the matrix cut into slices of 32 consecutive rows; each slice is
+// padded to its longest row and stored entry-major (entry t of the slice's
+// 32 rows is 32 consecutive elements at off[s] + 32 t).  Lane l of a warp
+// owns row 32 s + l and reads its entries with fully coalesced 128-byte
+// (index) and 256-byte (value) loads, with no staging.  Padding entries hold
+// value 0 and a valid column and add +-0 to the FMA chain, so rows sum in the
+// same entry order, to the same value, as row_chain.
+// ---------------------------------------------------------------------------
+
+// L2 policy for arrays read once per pass: evict first, so that the Krylov
+// vectors (re-read by the next kernels) stay resident in L2 while the matrix
+// streams through.
+__device__ __forceinline__ uint64_t l2_evict_first_policy()
+{
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ double ld_stream(const double *p, uint64_t pol)
+{
+    double v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float ld_stream(const float *p, uint64_t pol)
+{
+    float v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ int32_t ld_stream(const int32_t *p, uint64_t pol)
+{
+    int32_t v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+// f(row, sum_t val[t] g(col[t])) for every row, one warp per slice; the
+// entries are taken B at a time (all B loads and gathers issued before the
+// first FMA).  The slice length is warp-uniform, so the guards never diverge.
+template <class V, int B, class G, class F>
+__device__ __forceinline__ void sell_rows(int n, int n_slices, const int32_t *__restrict__ off,
+                                          const int32_t *__restrict__ col, const V *__restrict__ val,
+                                          G g, F f)
+{
+    const uint64_t pol = l2_evict_first_policy();
+    const int lane = threadIdx.x & 31;
+    const int nw = gridDim.x * kWarps;
+    for (int s = blockIdx.x * kWarps + (threadIdx.x >> 5); s < n_slices; s += nw) {
+        const int b = __ldg(off + s);
+        const int len = (__ldg(off + s + 1) - b) >> 5;
+        const int32_t *cp = col + b + lane;
+        const V *vp = val + b + lane;
+        V acc = V(0);
+        for (int t0 = 0; t0 < len; t0 += B) {
+            int c[B];
+            V v[B], x[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (t0 + u < len) {
+                    c[u] = ld_stream(cp + 32 * (t0 + u), pol);
+                    v[u] = ld_stream(vp + 32 * (t0 + u), pol);
+                }
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (t0 + u < len) x[u] = g(c[u]);
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (t0 + u < len) acc = fma_t(v[u], x[u], acc);
+        }
+        const int row = s * 32 + lane;
+        if (row < n) f(row, acc);
+    }
+}
+
+// Two products over one SELL pattern (A and A^T values): f(row, y1, y2).
+template <class V, int B, class G1, class G2, class F>
+__device__ __forceinline__ void sell_rows2(int n, int n_slices, const int32_t *__restrict__ off,
+                                           const int32_t *__restrict__ col, const V *__restrict__ val1,
+                                           const V *__restrict__ val2, G1 g1, G2 g2, F f)
+{
+    const uint64_t pol = l2_evict_first_policy();
+    const int lane = threadIdx.x & 31;
+    const int nw = gridDim.x * kWarps;
+    for (int s = blockIdx.x * kWarps + (threadIdx.x >> 5); s < n_slices; s += nw) {
+        const int b = __ldg(off + s);
+        const int len = (__ldg(off + s + 1) - b) >> 5;
+        const int32_t *cp = col + b + lane;
+        const V *vp1 = val1 + b + lane;
+        const V *vp2 = val2 + b + lane;
+        V a1 = V(0), a2 = V(0);
+        for (int t0 = 0; t0 < len; t0 += B) {
+            int c[B];
+            V v1[B], v2[B], x1[B], x2[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (t0 + u < len) {
+                    c[u] = ld_stream(cp + 32 * (t0 + u), pol);
+                    v1[u] = ld_stream(vp1 + 32 * (t0 + u), pol);
+                    v2[u] = ld_stream(vp2 + 32 * (t0 + u), pol);
+                }
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (t0 + u < len) {
+                    x1[u] = g1(c[u]);
+                    x2[u] = g2(c[u]);
+                }
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (t0 + u < len) {
+                    a1 = fma_t(v1[u], x1[u], a1);
+                    a2 = fma_t(v2[u], x2[u], a2);
+                }
+        }
+        const int row = s * 32 + lane;
+        if (row < n) f(row, a1, a2);
+    }
+}
+
 } // namespace cf

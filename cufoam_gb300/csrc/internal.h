@@ -71,6 +71,8 @@ struct DevState {
     uint32_t counters[16];
 };
 
+constexpr int32_t kFlagAbsTol = 1;   // DevState::flags: tolerance is absolute
+
 enum CounterSlot {
     SLOT_A = 0, SLOT_B, SLOT_C, SLOT_D, SLOT_NF1, SLOT_NF2, SLOT_INIT, SLOT_POW, SLOT_MISC
 };
@@ -91,6 +93,14 @@ struct SolveArgs {
     const double *valT;
     const float *val32;
     const float *valT32;
+    // SELL-32 copy of the matrix for the fast kernels (n_slices = 0: none)
+    int32_t n_slices;
+    const int32_t *s_off;      // [n_slices + 1] element offset of each slice
+    const int32_t *s_col;
+    const double *s_val;
+    const double *s_valT;
+    const float *s_val32;
+    const float *s_valT32;
     const double *diag;        // a_ii
     const double *dinv;        // 1 / a_ii
     const double *dinv_sqrt;   // sqrt(1 / a_ii)
@@ -114,6 +124,7 @@ struct SolveArgs {
     DevState *st;
     DevState *st_in;           // inner (FP32) solve of the mixed-precision loop
     double *hist;
+    unsigned long long *hist_t; // device clock (ns) at the end of each step
     unsigned long long cond;   // cudaGraphConditionalHandle of the running loop
     int32_t use_cond;
     int32_t power_steps;       // Richardson: power-method steps
@@ -133,11 +144,11 @@ struct DeviceBuffer {
 };
 
 struct GraphKey {
-    int solver, precision, reduction, stage_cap, phase;
+    int solver, precision, reduction, stage_cap, phase, format;
     bool operator<(const GraphKey &o) const
     {
-        return std::tie(solver, precision, reduction, stage_cap, phase) <
-               std::tie(o.solver, o.precision, o.reduction, o.stage_cap, o.phase);
+        return std::tie(solver, precision, reduction, stage_cap, phase, format) <
+               std::tie(o.solver, o.precision, o.reduction, o.stage_cap, o.phase, o.format);
     }
 };
 
@@ -161,7 +172,7 @@ struct Context {
 
     // workspace (grow-only, reused by every solve)
     DeviceBuffer vec[24];
-    DeviceBuffer partials, partials32, hist, state, state_in, args;
+    DeviceBuffer partials, partials32, hist, hist_t, state, state_in, args;
     SolveArgs *h_args = nullptr;   // pinned
     DevState *h_state = nullptr;   // pinned
     DevState *h_state_in = nullptr; // pinned
@@ -189,6 +200,14 @@ struct Matrix {
     double diag_abs_min = 0.0;
     bool have_dmin = false;
     bool from_csr = false;     // built from a CSR matrix (no LDU arrays)
+    // SELL-32 copy for the fast kernels; the layout depends on the pattern
+    // only, the value copies are refreshed after every value change
+    int format_request = CF_FORMAT_AUTO;
+    int sell = -1;             // -1 not decided, 0 CSR kernels, 1 SELL-32
+    int32_t n_slices = 0;
+    int64_t sell_nnz = 0;      // stored entries including padding
+    DeviceBuffer s_off, s_col, s_val, s_valT, s_val32, s_valT32;
+    bool have_sval = false, have_svalT = false, have_sval32 = false, have_svalT32 = false;
 };
 
 // ---------------------------------------------------------------------------
@@ -209,6 +228,7 @@ void ldu2csr_into(Context *ctx, const cf_ldu_view &v, int32_t *ro, int32_t *col,
                   double *val, int memory);
 
 int stage_cap_for(const Matrix *m);
+bool matrix_ensure_sell(Matrix *m, bool transpose, bool fp32);
 Matrix *matrix_from_csr(Context *ctx, int n, int64_t nnz, const int32_t *ro, const int32_t *col,
                         const double *val);
 void matrix_set_transpose_csr(Matrix *m, const int32_t *roT, const int32_t *colT, const double *valT);

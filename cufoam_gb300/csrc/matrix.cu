@@ -268,6 +268,55 @@ __global__ void __launch_bounds__(kBlock) k_spmv(int n, int cap, const int32_t *
 }
 
 // ---------------------------------------------------------------------------
+// SELL-32 copy (layout described in device.cuh)
+// ---------------------------------------------------------------------------
+// slot s: 32 x the longest row of slice s (slot n_slices = 0); the stored
+// total accumulates in 64 bits
+__global__ void k_sell_len(int n, int n_slices, const int32_t *__restrict__ ro, int32_t *slen,
+                           unsigned long long *total)
+{
+    CF_FOR_ELEMS(s, n_slices + 1) {
+        int mx = 0;
+        if (s < n_slices) {
+            const int r1 = min(n, 32 * s + 32);
+            for (int r = 32 * s; r < r1; ++r) mx = max(mx, __ldg(ro + r + 1) - __ldg(ro + r));
+            atomicAdd(total, 32ull * (unsigned long long)mx);
+        }
+        slen[s] = 32 * mx;
+    }
+}
+
+// one thread per slot of the last slice's 32 rows (rows >= n hold value 0,
+// column 0); pattern (scol != nullptr) and / or values
+template <class S, class V>
+__global__ void k_sell_fill(int n, int n_slices, const int32_t *__restrict__ ro,
+                            const int32_t *__restrict__ col, const S *__restrict__ val,
+                            const int32_t *__restrict__ soff, int32_t *scol, V *sval)
+{
+    CF_FOR_ELEMS(i, 32 * n_slices) {
+        const int s = i >> 5, lane = i & 31;
+        const int b = soff[s], len = (soff[s + 1] - b) >> 5;
+        const int rs = i < n ? ro[i] : 0, re = i < n ? ro[i + 1] : 0;
+        for (int t = 0; t < len; ++t) {
+            const int j = rs + t;
+            const int o = b + 32 * t + lane;
+            if (scol) scol[o] = j < re ? col[j] : (i < n ? i : 0);
+            if (sval) sval[o] = j < re ? (V)val[j] : V(0);
+        }
+    }
+}
+
+// y = A x over the SELL-32 copy (the fast order of k_spmv_fast)
+__global__ void __launch_bounds__(kBlock) k_spmv_sell(int n, int n_slices, const int32_t *__restrict__ off,
+                                                      const int32_t *__restrict__ col,
+                                                      const double *__restrict__ val,
+                                                      const double *__restrict__ x, double *y)
+{
+    sell_rows<double, 8>(n, n_slices, off, col, val, [&](int c) { return __ldg(x + c); },
+                         [&](int row, double v) { y[row] = v; });
+}
+
+// ---------------------------------------------------------------------------
 // matrices given as CSR (the libGIS-compatible entry points)
 // ---------------------------------------------------------------------------
 // FindDiag (gis/SparseSystem/kernels.h:447-464): the entry with col == row,
@@ -528,6 +577,7 @@ void matrix_update_values(Matrix *m, const double *diag, const double *lower, co
         CF_CHECK_LAUNCH();
     }
     m->have_valT = m->have_32 = m->have_T32 = m->have_dmin = false;
+    m->have_sval = m->have_svalT = m->have_sval32 = m->have_svalT32 = false;
 }
 
 // A^T values on A's pattern: the same fill with lower and upper swapped.
@@ -611,16 +661,9 @@ void csr_transpose(Context *ctx, int n_rows, int n_cols, int64_t nnz, const int3
 {
     DeviceBuffer cnt, tmp;
     cnt.ensure(sizeof(int32_t) * ((size_t)n_cols + 1));
-    CF_CUDA(cudaMemsetAsync(cnt.ptr, 0, sizeof(int32_t) * ((size_t)n_cols + 1), ctx->stream));
     const int g = grid_for(ctx, (int64_t)n_rows + 1);
-    if (n_rows > 0) {
-        k_count_cols<<<g, kBlock, 0, ctx->stream>>>(n_rows, ro, col, cnt.as<int32_t>() + 1);
-        CF_CHECK_LAUNCH();
-    }
-    // counts were written one slot to the right: roT = inclusive scan
-    exclusive_scan(ctx, n_cols + 1, cnt.as<int32_t>(), roT, tmp);
-    // exclusive scan of [0, c0, c1, ...] gives [0, 0, c0, ...]: shift by one
-    // instead: recompute from counts placed at [c] directly
+    // column counts in cnt[0..n_cols-1], cnt[n_cols] = 0: the exclusive scan
+    // is the row offsets of A^T
     CF_CUDA(cudaMemsetAsync(cnt.ptr, 0, sizeof(int32_t) * ((size_t)n_cols + 1), ctx->stream));
     if (n_rows > 0) {
         k_count_cols<<<g, kBlock, 0, ctx->stream>>>(n_rows, ro, col, cnt.as<int32_t>());
@@ -718,6 +761,7 @@ void matrix_set_transpose_csr(Matrix *m, const int32_t *roT, const int32_t *colT
     CF_CUDA(cudaMemsetAsync(m->valT.as<double>() + m->nnz, 0, sizeof(double) * 4, ctx->stream));
     m->have_valT = true;
     m->have_T32 = false;
+    m->have_svalT = m->have_svalT32 = false;
 }
 
 static void matrix_transpose_from_csr(Matrix *m)
@@ -730,6 +774,85 @@ static void matrix_transpose_from_csr(Matrix *m)
     csr_transpose(ctx, m->n, m->n, m->nnz, m->ro.as<int32_t>(), m->col.as<int32_t>(), m->val.as<double>(),
                   roT.as<int32_t>(), colT.as<int32_t>(), valT.as<double>());
     matrix_set_transpose_csr(m, roT.as<int32_t>(), colT.as<int32_t>(), valT.as<double>());
+}
+
+// Decide the fast kernels' format (once per pattern) and bring the SELL-32
+// value copies up to date: FP64 A, plus A^T (transpose) and FP32 (fp32)
+// copies when asked.  Returns whether the fast kernels use SELL-32.
+bool matrix_ensure_sell(Matrix *m, bool transpose, bool fp32)
+{
+    Context *ctx = m->ctx;
+    if (m->sell < 0) {
+        m->sell = 0;
+        if (m->format_request != CF_FORMAT_CSR && m->n > 0) {
+            const int ns = (m->n + 31) / 32;
+            m->s_off.ensure(sizeof(int32_t) * ((size_t)ns + 1));
+            DeviceBuffer slen, tmp, tot;
+            slen.ensure(sizeof(int32_t) * ((size_t)ns + 1));
+            tot.ensure(sizeof(unsigned long long));
+            CF_CUDA(cudaMemsetAsync(tot.ptr, 0, sizeof(unsigned long long), ctx->stream));
+            k_sell_len<<<grid_for(ctx, (int64_t)ns + 1), kBlock, 0, ctx->stream>>>(
+                m->n, ns, m->ro.as<int32_t>(), slen.as<int32_t>(), tot.as<unsigned long long>());
+            CF_CHECK_LAUNCH();
+            unsigned long long total = 0;
+            CF_CUDA(cudaMemcpyAsync(&total, tot.ptr, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
+            CF_CUDA(cudaStreamSynchronize(ctx->stream));
+            const bool fits = total < (unsigned long long)INT32_MAX - 64;
+            const bool good = fits && (double)total <= 1.2 * (double)m->nnz + 32.0 * 8 &&
+                              m->nnz <= 32 * (int64_t)m->n;
+            require(m->format_request != CF_FORMAT_SELL || fits, CF_UNSUPPORTED,
+                    "SELL-32 copy exceeds 2^31 entries");
+            if (m->format_request == CF_FORMAT_SELL || good) {
+                exclusive_scan(ctx, ns + 1, slen.as<int32_t>(), m->s_off.as<int32_t>(), tmp);
+                m->n_slices = ns;
+                m->sell_nnz = (int64_t)total;
+                m->s_col.ensure(sizeof(int32_t) * ((size_t)total + 32));
+                k_sell_fill<double, double><<<grid_for(ctx, 32 * (int64_t)ns), kBlock, 0, ctx->stream>>>(
+                    m->n, ns, m->ro.as<int32_t>(), m->col.as<int32_t>(), nullptr, m->s_off.as<int32_t>(),
+                    m->s_col.as<int32_t>(), (double *)nullptr);
+                CF_CHECK_LAUNCH();
+                m->sell = 1;
+            }
+        }
+        m->have_sval = m->have_svalT = m->have_sval32 = m->have_svalT32 = false;
+    }
+    if (m->sell != 1) return false;
+    if (transpose) matrix_ensure_transpose(m);
+    auto fill = [&](const double *src, DeviceBuffer &dst, bool f32) {
+        const int ns = m->n_slices;
+        const dim3 g(grid_for(ctx, 32 * (int64_t)ns));
+        if (f32) {
+            dst.ensure(sizeof(float) * ((size_t)m->sell_nnz + 32));
+            k_sell_fill<double, float><<<g, kBlock, 0, ctx->stream>>>(m->n, ns, m->ro.as<int32_t>(),
+                                                                      m->col.as<int32_t>(), src,
+                                                                      m->s_off.as<int32_t>(), nullptr,
+                                                                      dst.as<float>());
+        } else {
+            dst.ensure(sizeof(double) * ((size_t)m->sell_nnz + 32));
+            k_sell_fill<double, double><<<g, kBlock, 0, ctx->stream>>>(m->n, ns, m->ro.as<int32_t>(),
+                                                                       m->col.as<int32_t>(), src,
+                                                                       m->s_off.as<int32_t>(), nullptr,
+                                                                       dst.as<double>());
+        }
+        CF_CHECK_LAUNCH();
+    };
+    if (!m->have_sval) {
+        fill(m->val.as<double>(), m->s_val, false);
+        m->have_sval = true;
+    }
+    if (transpose && !m->have_svalT) {
+        fill(m->valT.as<double>(), m->s_valT, false);
+        m->have_svalT = true;
+    }
+    if (fp32 && !m->have_sval32) {
+        fill(m->val.as<double>(), m->s_val32, true);
+        m->have_sval32 = true;
+    }
+    if (fp32 && transpose && !m->have_svalT32) {
+        fill(m->valT.as<double>(), m->s_valT32, true);
+        m->have_svalT32 = true;
+    }
+    return true;
 }
 
 // 1/a_ii taken from a diagonal preconditioner matrix (MRS's invM).
@@ -752,6 +875,15 @@ void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order)
     Context *ctx = m->ctx;
     if (transpose) matrix_ensure_transpose(m);
     if (m->n == 0) return;
+    if (!ref_order && matrix_ensure_sell(m, transpose, false)) {
+        const int g = ctx->fast_grid((const void *)k_spmv_sell, 0);
+        k_spmv_sell<<<g, kBlock, 0, ctx->stream>>>(m->n, m->n_slices, m->s_off.as<int32_t>(),
+                                                   m->s_col.as<int32_t>(),
+                                                   transpose ? m->s_valT.as<double>() : m->s_val.as<double>(),
+                                                   x, y);
+        CF_CHECK_LAUNCH();
+        return;
+    }
     const int cap = stage_cap_for(m);
     const size_t smem = cap > 0 ? kWarps * stage_bytes_per_warp<double>(cap) : 0;
     auto kern = ref_order ? k_spmv : k_spmv_fast;

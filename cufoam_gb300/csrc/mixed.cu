@@ -31,25 +31,17 @@ __global__ void __launch_bounds__(kBlock) k_mx_correct(const SolveArgs *__restri
 }
 
 // r = b - A x, ||r|| (FP64); records the outer step.
+template <int FMT>
 __global__ void __launch_bounds__(kBlock) k_mx_residual(const SolveArgs *__restrict__ a)
 {
-    const int n = a->n, cap = a->stage_cap;
-    CF_STAGE(double, cap);
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val, *x = a->x, *b = a->b;
+    const double *x = a->x, *b = a->b;
     double *r = a->r[0];
     double acc[1] = {0.0};
-    CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
-        const int row = base + (threadIdx.x & 31);
-        const double t = row_chain<double>(ch, col, val, [&](int c) { return x[c]; });
-        if (row < n) {
-            const double ri = b[row] - t;
-            r[row] = ri;
-            acc[0] = fma_t(ri, ri, acc[0]);
-        }
-        __syncwarp();
-    }
+    for_rows<FMT, double>(a, a->val, a->s_val, [&](int c) { return x[c]; }, [&](int row, double t) {
+        const double ri = b[row] - t;
+        r[row] = ri;
+        acc[0] = fma_t(ri, ri, acc[0]);
+    });
     double tot[1];
     if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &a->st->counters[SLOT_MISC],
                                false, tot) && threadIdx.x == 0) {
@@ -58,7 +50,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_residual(const SolveArgs *__restr
         const int k = st->k + 1; // outer steps
         st->k = k;
         st->norm = norm;
-        if (a->hist && k < st->hist_cap) a->hist[k] = norm;
+        record_hist(a, st, k, norm);
         if (!isfinite(norm)) {
             st->done = 1;
             st->status = CF_NONFINITE;
@@ -109,12 +101,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_setup(const SolveArgs *__restrict
 }
 
 // CG: K1 p = r + beta p_old (on the fly), q = A32 p, (p, q); deferred d update
+template <int FMT>
 __global__ void __launch_bounds__(kBlock) k_mx_cg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     CF_EXIT_IF_DONE(a, st, false);
-    const int n = a->n, cap = a->stage_cap;
-    CF_STAGE(float, cap);
     const int k = ld_cg(&st->k) + 1;
     const bool first = (k == 1);
     const float beta = first ? 0.f : (float)ld_cg(&st->rho0) / (float)ld_cg(&st->rho1);
@@ -124,23 +115,15 @@ __global__ void __launch_bounds__(kBlock) k_mx_cg_spmv(const SolveArgs *__restri
     float *pout = a->fp[k & 1];
     const float *r = a->fr;
     float *d = a->fx, *q = a->fq;
-    const int32_t *ro = a->ro, *col = a->col;
-    const float *val = a->val32;
     auto g = [&](int c) { return first ? r[c] : fma_t(beta, pin[c], r[c]); };
     float acc[1] = {0.f};
-    CF_FOR_CHUNKS(base, n) {
-        const Chunk<float> ch = stage_chunk<float>(ro, col, val, n, base, cap, sv_, sc_);
-        const int row = base + (threadIdx.x & 31);
-        const float y = row_chain<float>(ch, col, val, g);
-        if (row < n) {
-            const float pi = g(row);
-            pout[row] = pi;
-            q[row] = y;
-            if (xpend) d[row] = fma_t(xi_prev, pin[row], d[row]);
-            acc[0] = fma_t(pi, y, acc[0]);
-        }
-        __syncwarp();
-    }
+    for_rows<FMT, float>(a, a->val32, a->s_val32, g, [&](int row, float y) {
+        const float pi = g(row);
+        pout[row] = pi;
+        q[row] = y;
+        if (xpend) d[row] = fma_t(xi_prev, pin[row], d[row]);
+        acc[0] = fma_t(pi, y, acc[0]);
+    });
     float tot[1];
     if (grid_reduce<1, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
                               tot) && threadIdx.x == 0) {
@@ -186,12 +169,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_flush(const SolveArgs *__restrict
 }
 
 // BiCG: q = A32 p and q* = A32^T p* over the shared pattern
+template <int FMT>
 __global__ void __launch_bounds__(kBlock) k_mx_bicg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     CF_EXIT_IF_DONE(a, st, false);
-    const int n = a->n, cap = a->stage_cap;
-    CF_STAGE(float, cap);
     const int k = ld_cg(&st->k) + 1;
     const bool first = (k == 1);
     const float theta = (float)ld_cg(&st->theta);
@@ -201,27 +183,19 @@ __global__ void __launch_bounds__(kBlock) k_mx_bicg_spmv(const SolveArgs *__rest
     float *pout = a->fp[k & 1], *psout = a->fps[k & 1];
     const float *r = a->fr, *rs = a->frs;
     float *d = a->fx, *q = a->fq, *qs = a->fqs;
-    const int32_t *ro = a->ro, *col = a->col;
-    const float *val = a->val32, *valT = a->valT32;
     auto gp = [&](int c) { return first ? r[c] : fma_t(theta, pin[c], r[c]); };
     auto gps = [&](int c) { return first ? rs[c] : fma_t(theta, psin[c], rs[c]); };
     float acc[1] = {0.f};
-    CF_FOR_CHUNKS(base, n) {
-        const Chunk<float> ch = stage_chunk<float>(ro, col, val, n, base, cap, sv_, sc_);
-        const int row = base + (threadIdx.x & 31);
-        float y1, y2;
-        row_chain2<float>(ch, col, val, valT, gp, gps, y1, y2);
-        if (row < n) {
-            const float pi = gp(row), psi = gps(row);
-            pout[row] = pi;
-            psout[row] = psi;
-            q[row] = y1;
-            qs[row] = y2;
-            if (xpend) d[row] = fma_t(xi_prev, pin[row], d[row]);
-            acc[0] = fma_t(psi, y1, acc[0]);
-        }
-        __syncwarp();
-    }
+    for_rows2<FMT, float>(a, a->val32, a->valT32, a->s_val32, a->s_valT32, gp, gps,
+                          [&](int row, float y1, float y2) {
+                              const float pi = gp(row), psi = gps(row);
+                              pout[row] = pi;
+                              psout[row] = psi;
+                              q[row] = y1;
+                              qs[row] = y2;
+                              if (xpend) d[row] = fma_t(xi_prev, pin[row], d[row]);
+                              acc[0] = fma_t(psi, y1, acc[0]);
+                          });
     float tot[1];
     if (grid_reduce<1, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
                               tot) && threadIdx.x == 0) {
@@ -282,28 +256,19 @@ __global__ void __launch_bounds__(kBlock) k_mx_bicg_update(const SolveArgs *__re
 }
 
 // MR: K1 y = A32 r, (r, y), (y, y); K2 d += w r, r -= w y
+template <int FMT>
 __global__ void __launch_bounds__(kBlock) k_mx_mr_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     CF_EXIT_IF_DONE(a, st, false);
-    const int n = a->n, cap = a->stage_cap;
-    CF_STAGE(float, cap);
     const float *r = a->fr;
     float *y = a->fq;
-    const int32_t *ro = a->ro, *col = a->col;
-    const float *val = a->val32;
     float acc[2] = {0.f, 0.f};
-    CF_FOR_CHUNKS(base, n) {
-        const Chunk<float> ch = stage_chunk<float>(ro, col, val, n, base, cap, sv_, sc_);
-        const int row = base + (threadIdx.x & 31);
-        const float v = row_chain<float>(ch, col, val, [&](int c) { return r[c]; });
-        if (row < n) {
-            y[row] = v;
-            acc[0] = fma_t(r[row], v, acc[0]);
-            acc[1] = fma_t(v, v, acc[1]);
-        }
-        __syncwarp();
-    }
+    for_rows<FMT, float>(a, a->val32, a->s_val32, [&](int c) { return r[c]; }, [&](int row, float v) {
+        y[row] = v;
+        acc[0] = fma_t(r[row], v, acc[0]);
+        acc[1] = fma_t(v, v, acc[1]);
+    });
     float tot[2];
     if (grid_reduce<2, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
                               tot) && threadIdx.x == 0)
@@ -334,17 +299,24 @@ __global__ void __launch_bounds__(kBlock) k_mx_mr_update(const SolveArgs *__rest
 // ---------------------------------------------------------------------------
 // host driver of the refinement loop
 // ---------------------------------------------------------------------------
-static Kernels inner_kernels(int solver)
+template <int FMT>
+static Kernels inner_kernels_t(int solver)
 {
     Kernels k;
     k.value_bytes = sizeof(float);
     switch (solver) {
-    case CF_CG: k.k1 = (const void *)k_mx_cg_spmv; k.k1_spmv = true; k.k2 = (const void *)k_mx_cg_update; break;
-    case CF_BICG: k.k1 = (const void *)k_mx_bicg_spmv; k.k1_spmv = true; k.k2 = (const void *)k_mx_bicg_update; break;
-    case CF_MR: k.k1 = (const void *)k_mx_mr_spmv; k.k1_spmv = true; k.k2 = (const void *)k_mx_mr_update; break;
+    case CF_CG: k.k1 = (const void *)k_mx_cg_spmv<FMT>; k.k2 = (const void *)k_mx_cg_update; break;
+    case CF_BICG: k.k1 = (const void *)k_mx_bicg_spmv<FMT>; k.k2 = (const void *)k_mx_bicg_update; break;
+    case CF_MR: k.k1 = (const void *)k_mx_mr_spmv<FMT>; k.k2 = (const void *)k_mx_mr_update; break;
     default: break;
     }
+    k.k1_spmv = FMT == kCsr;   // the SELL passes stage nothing
     return k;
+}
+
+static Kernels inner_kernels(int solver, bool sell)
+{
+    return sell ? inner_kernels_t<kSell>(solver) : inner_kernels_t<kCsr>(solver);
 }
 
 bool mixed_supported(int solver) { return solver == CF_CG || solver == CF_BICG || solver == CF_MR; }
@@ -364,6 +336,11 @@ void mixed_prepare(Context *ctx, Matrix *m, int solver, SolveArgs &A)
     A.val32 = m->val32.as<float>();
     A.valT32 = m->have_T32 ? m->valT32.as<float>() : nullptr;
     if (tr) std::swap(A.val32, A.valT32);
+    if (A.n_slices > 0) { // SELL-32 copies (FP32 values filled by the caller's matrix_ensure_sell)
+        A.s_val32 = m->s_val32.as<float>();
+        A.s_valT32 = m->have_svalT32 ? m->s_valT32.as<float>() : nullptr;
+        if (tr) std::swap(A.s_val32, A.s_valT32);
+    }
     A.fx = ctx->vec[14].as<float>();
     A.fr = ctx->vec[15].as<float>();
     A.fp[0] = ctx->vec[16].as<float>();
@@ -385,12 +362,14 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
     MixedResult res;
     SolveArgs &A = *ctx->h_args;
     void *args1[] = {&d_args};
-    const Kernels kk = inner_kernels(solver);
+    const bool sell = A.n_slices > 0;
+    const Kernels kk = inner_kernels(solver, sell);
+    const void *k_residual = sell ? (const void *)k_mx_residual<kSell> : (const void *)k_mx_residual<kCsr>;
     bool use_graph = use_graph_in;
     GraphEntry *ge = nullptr;
     if (use_graph) {
         try {
-            ge = loop_graph(ctx, kk, solver, CF_PREC_MIXED, cap, false, d_args);
+            ge = loop_graph(ctx, kk, solver, CF_PREC_MIXED, cap, false, d_args, sell ? 1 : 0);
         } catch (const Error &) {
             ctx->graphs_ok = false;
             use_graph = false;
@@ -438,8 +417,7 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
                    launch_cfg(ctx, (const void *)k_mx_flush, false, cap, false), args1);
         launch(ctx, ctx->stream, (const void *)k_mx_correct,
                launch_cfg(ctx, (const void *)k_mx_correct, false, cap, false), args1);
-        launch(ctx, ctx->stream, (const void *)k_mx_residual,
-               launch_cfg(ctx, (const void *)k_mx_residual, true, cap, false), args1);
+        launch(ctx, ctx->stream, k_residual, launch_cfg(ctx, k_residual, !sell, cap, false), args1);
         CF_CUDA(cudaMemcpyAsync(&SI, A.st_in, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
         CF_CUDA(cudaMemcpyAsync(ctx->h_state, A.st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
         CF_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -71,27 +71,18 @@ __global__ void __launch_bounds__(kBlock) k_f_cg_prep(const SolveArgs *__restric
     }
 }
 
+template <int FMT>
 __global__ void __launch_bounds__(kBlock) k_f_cg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, false);
-    const int n = a->n, cap = a->stage_cap;
-    CF_STAGE(double, cap);
     const double *__restrict__ p = a->p[0];
     double *__restrict__ q = a->q;
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val;
     double acc[1] = {0.0};
-    CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
-        const int row = base + (threadIdx.x & 31);
-        const double y = row_chain<double>(ch, col, val, [&](int c) { return p[c]; });
-        if (row < n) {
-            q[row] = y;
-            acc[0] = fma_t(p[row], y, acc[0]);
-        }
-        __syncwarp();
-    }
+    for_rows<FMT, double>(a, a->val, a->s_val, [&](int c) { return p[c]; }, [&](int row, double y) {
+        q[row] = y;
+        acc[0] = fma_t(p[row], y, acc[0]);
+    });
     double tot[1];
     if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_A], false, tot) &&
         threadIdx.x == 0) {
@@ -205,32 +196,22 @@ __global__ void __launch_bounds__(kBlock) k_f_bicg_prep(const SolveArgs *__restr
     }
 }
 
+template <int FMT>
 __global__ void __launch_bounds__(kBlock) k_f_bicg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, false);
-    const int n = a->n, cap = a->stage_cap;
-    CF_STAGE(double, cap);
     const double *__restrict__ p = a->p[0];
     const double *__restrict__ ps = a->ps[0];
     double *__restrict__ q = a->q;
     double *__restrict__ qs = a->qs;
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val, *valT = a->valT;
     double acc[1] = {0.0};
-    CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
-        const int row = base + (threadIdx.x & 31);
-        double y1, y2;
-        row_chain2<double>(ch, col, val, valT, [&](int c) { return p[c]; },
-                           [&](int c) { return ps[c]; }, y1, y2);
-        if (row < n) {
-            q[row] = y1;
-            qs[row] = y2;
-            acc[0] = fma_t(ps[row], y1, acc[0]);
-        }
-        __syncwarp();
-    }
+    for_rows2<FMT, double>(a, a->val, a->valT, a->s_val, a->s_valT, [&](int c) { return p[c]; },
+                   [&](int c) { return ps[c]; }, [&](int row, double y1, double y2) {
+                       q[row] = y1;
+                       qs[row] = y2;
+                       acc[0] = fma_t(ps[row], y1, acc[0]);
+                   });
     double tot[1];
     if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_A], false, tot) &&
         threadIdx.x == 0) {
@@ -281,28 +262,19 @@ __global__ void __launch_bounds__(kBlock) k_f_jac_prep(const SolveArgs *__restri
     }
 }
 
+template <int FMT>
 __global__ void __launch_bounds__(kBlock) k_f_jac_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, true);
-    const int n = a->n, cap = a->stage_cap;
-    CF_STAGE(double, cap);
     const double *__restrict__ d = a->w[1];
     double *__restrict__ r = a->r[0];
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val;
     double acc[1] = {0.0};
-    CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
-        const int row = base + (threadIdx.x & 31);
-        const double y = row_chain<double>(ch, col, val, [&](int c) { return d[c]; });
-        if (row < n) {
-            const double ri = fma_t(-1.0, y, r[row]);
-            r[row] = ri;
-            acc[0] = fma_t(ri, ri, acc[0]);
-        }
-        __syncwarp();
-    }
+    for_rows<FMT, double>(a, a->val, a->s_val, [&](int c) { return d[c]; }, [&](int row, double y) {
+        const double ri = fma_t(-1.0, y, r[row]);
+        r[row] = ri;
+        acc[0] = fma_t(ri, ri, acc[0]);
+    });
     double tot[1];
     if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_A], false, tot) &&
         threadIdx.x == 0)
@@ -333,29 +305,20 @@ __global__ void __launch_bounds__(kBlock) k_f_rich_prep(const SolveArgs *__restr
     CF_X4_TAIL(i, n) x[i] = fma_t(omega, r[i], x[i]);
 }
 
+template <int FMT>
 __global__ void __launch_bounds__(kBlock) k_f_rich_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, true);
-    const int n = a->n, cap = a->stage_cap;
-    CF_STAGE(double, cap);
     const double *__restrict__ x = a->x;
     const double *__restrict__ b = a->b;
     double *__restrict__ r = a->r[0];
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val;
     double acc[1] = {0.0};
-    CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
-        const int row = base + (threadIdx.x & 31);
-        const double t = row_chain<double>(ch, col, val, [&](int c) { return x[c]; });
-        if (row < n) {
-            const double ri = b[row] - t;
-            r[row] = ri;
-            acc[0] = fma_t(ri, ri, acc[0]);
-        }
-        __syncwarp();
-    }
+    for_rows<FMT, double>(a, a->val, a->s_val, [&](int c) { return x[c]; }, [&](int row, double t) {
+        const double ri = b[row] - t;
+        r[row] = ri;
+        acc[0] = fma_t(ri, ri, acc[0]);
+    });
     double tot[1];
     if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_A], false, tot) &&
         threadIdx.x == 0)
@@ -385,32 +348,22 @@ __global__ void __launch_bounds__(kBlock) k_f_mr_prep(const SolveArgs *__restric
     }
 }
 
-template <int KIND>
+template <int KIND, int FMT>
 __global__ void __launch_bounds__(kBlock) k_f_mr_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, false);
-    const int n = a->n, cap = a->stage_cap;
-    CF_STAGE(double, cap);
     const double *__restrict__ r = a->r[0];
     const double *__restrict__ d = (KIND == 0) ? a->r[0] : a->w[1];
     const double *__restrict__ sD = a->dinv_sqrt;
     double *__restrict__ y = a->w[0];
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val;
     double acc[2] = {0.0, 0.0};
-    CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
-        const int row = base + (threadIdx.x & 31);
-        double v = row_chain<double>(ch, col, val, [&](int c) { return d[c]; });
-        if (row < n) {
-            if (KIND == 3) v = __dmul_rn(sD[row], v);
-            y[row] = v;
-            acc[0] = fma_t(r[row], v, acc[0]);
-            acc[1] = fma_t(v, v, acc[1]);
-        }
-        __syncwarp();
-    }
+    for_rows<FMT, double>(a, a->val, a->s_val, [&](int c) { return d[c]; }, [&](int row, double v) {
+        if (KIND == 3) v = __dmul_rn(sD[row], v);
+        y[row] = v;
+        acc[0] = fma_t(r[row], v, acc[0]);
+        acc[1] = fma_t(v, v, acc[1]);
+    });
     double tot[2];
     if (grid_reduce<2, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_A], false, tot) &&
         threadIdx.x == 0)
@@ -466,7 +419,7 @@ __global__ void __launch_bounds__(kBlock) k_f_bicg_update(const SolveArgs *__res
         st->k = k;
         st->norm = norm;
         st->x_pending = 1;
-        if (a->hist && k < st->hist_cap) a->hist[k] = norm;
+        record_hist(a, st, k, norm);
         bool cont = true;
         int status = CF_NOT_CONVERGED;
         if (norm < st->tol && k >= st->min_steps) { cont = false; status = CF_OK; }
@@ -533,51 +486,58 @@ __global__ void __launch_bounds__(kBlock) k_f_mr_update(const SolveArgs *__restr
 }
 
 // ---------------------------------------------------------------------------
-Kernels fast_body_kernels(int solver)
+template <int FMT>
+static Kernels fast_kernels(int solver)
 {
     Kernels k;
     switch (solver) {
     case CF_CG:
         k.k0 = (const void *)k_f_cg_prep;
-        k.k1 = (const void *)k_f_cg_spmv;
+        k.k1 = (const void *)k_f_cg_spmv<FMT>;
         k.k2 = (const void *)k_f_cg_update;
         break;
     case CF_BICG:
         k.k0 = (const void *)k_f_bicg_prep;
-        k.k1 = (const void *)k_f_bicg_spmv;
+        k.k1 = (const void *)k_f_bicg_spmv<FMT>;
         k.k2 = (const void *)k_f_bicg_update;
         break;
     case CF_JACOBI:
         k.k0 = (const void *)k_f_jac_prep;
-        k.k1 = (const void *)k_f_jac_spmv;
+        k.k1 = (const void *)k_f_jac_spmv<FMT>;
         break;
     case CF_RICHARDSON:
         k.k0 = (const void *)k_f_rich_prep;
-        k.k1 = (const void *)k_f_rich_spmv;
+        k.k1 = (const void *)k_f_rich_spmv<FMT>;
         break;
     case CF_MR:
-        k.k1 = (const void *)k_f_mr_spmv<0>;
+        k.k1 = (const void *)k_f_mr_spmv<0, FMT>;
         k.k2 = (const void *)k_f_mr_update<0>;
         break;
     case CF_MRJACOBI:
         k.k0 = (const void *)k_f_mr_prep<1>;
-        k.k1 = (const void *)k_f_mr_spmv<1>;
+        k.k1 = (const void *)k_f_mr_spmv<1, FMT>;
         k.k2 = (const void *)k_f_mr_update<1>;
         break;
     case CF_MRS:
         k.k0 = (const void *)k_f_mr_prep<2>;
-        k.k1 = (const void *)k_f_mr_spmv<2>;
+        k.k1 = (const void *)k_f_mr_spmv<2, FMT>;
         k.k2 = (const void *)k_f_mr_update<2>;
         break;
     case CF_JMR:
         k.k0 = (const void *)k_f_mr_prep<3>;
-        k.k1 = (const void *)k_f_mr_spmv<3>;
+        k.k1 = (const void *)k_f_mr_spmv<3, FMT>;
         k.k2 = (const void *)k_f_mr_update<3>;
         break;
     default: break;
     }
-    k.k1_spmv = true;
+    // the SELL-32 passes stage nothing (no dynamic shared memory)
+    k.k1_spmv = FMT == kCsr;
     return k;
+}
+
+Kernels fast_body_kernels(int solver, bool sell)
+{
+    return sell ? fast_kernels<kSell>(solver) : fast_kernels<kCsr>(solver);
 }
 
 const void *fast_flush_kernel() { return (const void *)k_f_flush_x; }

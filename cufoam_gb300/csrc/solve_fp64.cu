@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kBlock) k_nf_dist(const SolveArgs *__restrict_
         DevState *st = a->st;
         const double nf = l1 ? tot[0] + 1e-20 : sqrt(tot[0]) + sqrt(tot[1]) + 1e-20;
         st->nf = nf;
-        st->tol = st->tolerance * nf;
+        st->tol = (st->flags & kFlagAbsTol) ? st->tolerance : st->tolerance * nf;
     }
 }
 
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_update(const SolveArgs *__restr
         st->k = k;
         st->norm = norm;
         st->x_pending = 1;
-        if (a->hist && k < st->hist_cap) a->hist[k] = norm;
+        record_hist(a, st, k, norm);
         bool cont = true;
         int status = CF_NOT_CONVERGED;
         if (norm < st->tol && k >= st->min_steps) { cont = false; status = CF_OK; }
@@ -589,6 +589,9 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     const bool tr = c.transpose != 0;
     if (solver == CF_BICG || tr) matrix_ensure_transpose(m);
     if (solver == CF_RICHARDSON) matrix_ensure_dmin(m);
+    // the fast loops read the SELL-32 copy when the pattern suits it (FP32
+    // values too for the mixed inner solve)
+    const bool sell = !ref && matrix_ensure_sell(m, solver == CF_BICG || tr, mixed);
 
     // ---- vectors -------------------------------------------------------
     double *x, *b;
@@ -609,6 +612,8 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     const bool want_hist = c.history && c.history_capacity > 0;
     const int hist_cap = want_hist ? c.history_capacity : 0;
     if (want_hist) ctx->hist.ensure(sizeof(double) * (size_t)hist_cap);
+    const bool hist_time = want_hist && c.history_time != 0;
+    if (hist_time) ctx->hist_t.ensure(sizeof(unsigned long long) * (size_t)hist_cap);
 
     SolveArgs &A = *ctx->h_args;
     A = SolveArgs{};
@@ -618,7 +623,17 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     A.col = m->col.as<int32_t>();
     A.val = m->val.as<double>();
     A.valT = m->have_valT ? m->valT.as<double>() : nullptr;
-    if (tr) std::swap(A.val, A.valT); // A^T on the same pattern; its transpose is A
+    if (sell) {
+        A.n_slices = m->n_slices;
+        A.s_off = m->s_off.as<int32_t>();
+        A.s_col = m->s_col.as<int32_t>();
+        A.s_val = m->s_val.as<double>();
+        A.s_valT = m->have_svalT ? m->s_valT.as<double>() : nullptr;
+    }
+    if (tr) {
+        std::swap(A.val, A.valT); // A^T on the same pattern; its transpose is A
+        std::swap(A.s_val, A.s_valT);
+    }
     A.diag = m->diag.as<double>();
     A.dinv = m->dinv.as<double>();
     A.dinv_sqrt = m->dinv_sqrt.as<double>();
@@ -640,6 +655,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     A.ref_order = ref ? 1 : 0;
     A.st = ctx->state.as<DevState>();
     A.hist = want_hist ? ctx->hist.as<double>() : nullptr;
+    A.hist_t = hist_time ? ctx->hist_t.as<unsigned long long>() : nullptr;
     A.power_steps = c.power_max_steps;
     A.abort_flag = (c.time_limit_s > 0) ? ctx->d_abort : nullptr;
 
@@ -655,15 +671,16 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     S.hist_cap = hist_cap;
     S.diag_abs_min = m->diag_abs_min;
     S.omega = c.richardson_omega;
+    S.flags = c.absolute_tolerance ? kFlagAbsTol : 0;
 
     const bool prof = c.profile_kernels != 0;
     bool use_graph = c.use_graph != 0 && ctx->graphs_ok && !prof;
     GraphEntry *ge = nullptr;
-    const Kernels kk = ref ? body_kernels(solver) : fast_body_kernels(solver);
+    const Kernels kk = ref ? body_kernels(solver) : fast_body_kernels(solver, sell);
     SolveArgs *d_args = ctx->args.as<SolveArgs>();
     if (use_graph && !mixed) {
         try {
-            ge = loop_graph(ctx, kk, solver, CF_PREC_FP64, cap, ref, d_args);
+            ge = loop_graph(ctx, kk, solver, CF_PREC_FP64, cap, ref, d_args, sell ? 1 : 0);
         } catch (const Error &) {
             ctx->graphs_ok = false; // fall back to host-driven launches
             use_graph = false;
@@ -802,7 +819,14 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     int hist_len = 0;
     if (want_hist) {
         hist_len = std::min(R.k + 1, hist_cap);
-        download(ctx, c.history, A.hist, sizeof(double) * (size_t)hist_len, CF_MEM_HOST);
+        if (hist_time) {
+            std::vector<unsigned long long> t((size_t)hist_len);
+            download(ctx, t.data(), A.hist_t, sizeof(unsigned long long) * (size_t)hist_len, CF_MEM_HOST);
+            CF_CUDA(cudaStreamSynchronize(ctx->stream));
+            for (int i = 0; i < hist_len; ++i) c.history[i] = 1e-9 * (double)(t[(size_t)i] - t[0]);
+        } else {
+            download(ctx, c.history, A.hist, sizeof(double) * (size_t)hist_len, CF_MEM_HOST);
+        }
     }
     CF_CUDA(cudaStreamSynchronize(ctx->stream));
     float ms = 0.f;

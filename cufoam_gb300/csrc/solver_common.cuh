@@ -16,8 +16,76 @@ namespace cf {
     int32_t *sc_ = reinterpret_cast<int32_t *>(area_ + (size_t)((cap) + 8) * sizeof(V))
 
 // ---------------------------------------------------------------------------
+// SpMV row passes.  The fast kernels read the matrix either as CSR with
+// warp-chunk staging (kCsr) or from its SELL-32 copy (kSell); both sum each
+// row as one FMA chain in entry order.  for_rows calls f(row, sum_j a_ij g(j))
+// for every row; val is the CSR value array, sval its SELL-32 copy.
+// ---------------------------------------------------------------------------
+enum { kCsr = 0, kSell = 1 };
+
+// SELL passes take two entries per thread per batch: 48 registers, five
+// 256-thread blocks per SM (measured on the 7-point 128^3 system: within a
+// few percent of the best batch / occupancy pairing, with no spills).
+constexpr int kSellBatch = 2;
+
+template <int FMT, class V, class G, class F>
+__device__ __forceinline__ void for_rows(const SolveArgs *a, const V *val, const V *sval, G g, F f)
+{
+    if constexpr (FMT == kSell) {
+        sell_rows<V, kSellBatch>(a->n, a->n_slices, a->s_off, a->s_col, sval, g, f);
+    } else {
+        const int n = a->n, cap = a->stage_cap;
+        CF_STAGE(V, cap);
+        CF_FOR_CHUNKS(base, n) {
+            const Chunk<V> ch = stage_chunk<V>(a->ro, a->col, val, n, base, cap, sv_, sc_);
+            const int row = base + (threadIdx.x & 31);
+            const V y = row_chain<V>(ch, a->col, val, g);
+            if (row < n) f(row, y);
+            __syncwarp();
+        }
+    }
+}
+
+// The same for two value arrays on one pattern: f(row, y1, y2).
+template <int FMT, class V, class G1, class G2, class F>
+__device__ __forceinline__ void for_rows2(const SolveArgs *a, const V *val1, const V *val2, const V *sval1,
+                                          const V *sval2, G1 g1, G2 g2, F f)
+{
+    if constexpr (FMT == kSell) {
+        sell_rows2<V, 1>(a->n, a->n_slices, a->s_off, a->s_col, sval1, sval2, g1, g2, f);
+    } else {
+        const int n = a->n, cap = a->stage_cap;
+        CF_STAGE(V, cap);
+        CF_FOR_CHUNKS(base, n) {
+            const Chunk<V> ch = stage_chunk<V>(a->ro, a->col, val1, n, base, cap, sv_, sc_);
+            const int row = base + (threadIdx.x & 31);
+            V y1, y2;
+            row_chain2<V>(ch, a->col, val1, val2, g1, g2, y1, y2);
+            if (row < n) f(row, y1, y2);
+            __syncwarp();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // loop bookkeeping (thread 0 of the last block)
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// history entry k: ||r|| and / or the device clock
+static __device__ __forceinline__ void record_hist(const SolveArgs *a, const DevState *st, int k, double norm)
+{
+    if (k < st->hist_cap) {
+        if (a->hist) a->hist[k] = norm;
+        if (a->hist_t) a->hist_t[k] = global_ns();
+    }
+}
+
 static __device__ __noinline__ void finish_init(const SolveArgs *a, DevState *st, double rr, bool bicg)
 {
     const double norm0 = sqrt(rr);
@@ -25,7 +93,7 @@ static __device__ __noinline__ void finish_init(const SolveArgs *a, DevState *st
     st->rho1 = 0.0;
     st->norm0 = norm0;
     st->norm = norm0;
-    if (a->hist && st->hist_cap > 0) a->hist[0] = norm0;
+    record_hist(a, st, 0, norm0);
     double tol = st->tol;
     if (st->rel_tol > 0.0) tol = fmax(tol, st->rel_tol * norm0);
     st->tol = tol;
@@ -47,7 +115,7 @@ static __device__ __noinline__ void finish_step(const SolveArgs *a, DevState *st
     const int k = st->k + 1;
     st->k = k;
     st->norm = norm;
-    if (a->hist && k < st->hist_cap) a->hist[k] = norm;
+    record_hist(a, st, k, norm);
     const bool finite = isfinite(norm);
     bool cont = finite && k < st->max_steps && (norm > st->tol || k < st->min_steps);
     int status = !finite ? CF_NONFINITE : (norm > st->tol ? CF_NOT_CONVERGED : CF_OK);
@@ -180,9 +248,9 @@ static bool build_loop_graph(Context *ctx, const Kernels &kk, int cap, bool ref,
 // context: with programmatic launches between the body kernels where the
 // driver accepts them in a conditional body, else without.
 static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int precision, int cap,
-                              bool ref, SolveArgs *d_args)
+                              bool ref, SolveArgs *d_args, int format = 0)
 {
-    GraphKey key{solver, precision, ref ? 1 : 0, cap, 0};
+    GraphKey key{solver, precision, ref ? 1 : 0, cap, 0, format};
     auto it = ctx->graphs.find(key);
     if (it != ctx->graphs.end()) return &it->second;
     GraphEntry ge;
@@ -194,7 +262,7 @@ static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int p
     return &(ctx->graphs[key] = ge);
 }
 
-Kernels fast_body_kernels(int solver);
+Kernels fast_body_kernels(int solver, bool sell);
 const void *fast_flush_kernel();
 
 } // namespace cf

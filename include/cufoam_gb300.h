@@ -119,7 +119,12 @@ typedef struct cf_controls {
     int32_t profile_kernels; /* 1: host-driven loop with CUDA events around every
                                 body kernel; fills cf_perf.kernel_ms */
     int32_t transpose;       /* 1: solve A^T psi = source (the adjoint system) */
-    int32_t reserved[6];
+    int32_t absolute_tolerance; /* 1: tolerance is an absolute ||r||_2 threshold
+                                   (libGIS's `error` argument), no normFactor scaling */
+    int32_t history_time;    /* 1: history holds seconds since the initial residual
+                                at the end of each step (device clock), the
+                                reference's DetailType::Time, instead of ||r||_2 */
+    int32_t reserved[4];
 } cf_controls;
 
 /* solverPerformance plus diagnostics. */
@@ -179,6 +184,19 @@ cf_status cf_matrix_create_ldu(cf_context *ctx, const cf_ldu_view *ldu, cf_matri
 cf_status cf_matrix_update_values(cf_matrix *m, const double *diag, const double *lower,
                                   const double *upper, int32_t memory);
 void cf_matrix_destroy(cf_matrix *m);
+/* Storage the fast (CF_REDUCE_FAST) kernels read the matrix from.  AUTO
+ * (the default) picks SELL-32 -- slices of 32 rows padded to their longest
+ * row, entry-major, read with coalesced loads and no staging -- when the
+ * padding adds at most 20% to nnz and rows average at most 32 entries, and
+ * the CSR arrays with warp-chunk staging otherwise.  Both formats sum each
+ * row in entry order, so results do not depend on the choice.  The
+ * reference-order kernels always read the CSR arrays.  No reference
+ * counterpart (the reference has CSR only). */
+enum { CF_FORMAT_AUTO = 0, CF_FORMAT_CSR = 1, CF_FORMAT_SELL = 2 };
+cf_status cf_matrix_set_format(cf_matrix *m, int32_t format);
+/* The format the fast kernels use now (CF_FORMAT_CSR or CF_FORMAT_SELL;
+ * decides AUTO first) and the stored entries including padding. */
+cf_status cf_matrix_format(cf_matrix *m, int32_t *format, int64_t *stored_entries);
 cf_status cf_matrix_shape(const cf_matrix *m, int32_t *n_rows, int32_t *n_faces, int64_t *nnz);
 /* CSR arrays of A (transpose = 0) or A^T (transpose = 1; the reference's
  * Transpose, gis/gis.h:10-11).  row_offsets[n+1], cols[nnz], vals[nnz]. */

@@ -119,6 +119,46 @@ def test_spmv_bit_exact(ctx, case):
     assert np.allclose(y, ref, rtol=1e-14, atol=1e-14 * np.abs(ref).max())
 
 
+@pytest.mark.parametrize("case", ["c1", "lognormal", "convdiff", "star", "permuted", "ragged"])
+def test_spmv_formats_agree(ctx, case):
+    """The fast kernels read CSR (warp-chunk staging) or the SELL-32 copy;
+    both sum each row as one FMA chain in entry order, so they agree
+    exactly (zeros up to sign), for A and A^T, and after a value update."""
+    L = {"c1": lambda: O.grid_const(64, 64, 1),
+         "lognormal": lambda: O.grid_lognormal(20, 17, 9, 3),
+         "convdiff": lambda: O.grid_convdiff(16, 15, 14, 4)[0],
+         "star": lambda: _star_ldu(3000),
+         "permuted": lambda: O.permute_ldu(O.grid_lognormal(11, 10, 9, 6), O.permutation(6, 990)),
+         "ragged": lambda: O.grid_lognormal(7, 5, 3, 9),   # 105 rows: last slice partly empty
+         }[case]()
+    M = _matrix(ctx, L)
+    fmt, stored = M.format()
+    nnz = M.shape()[2]
+    if case == "star":
+        assert fmt == "csr" and stored == nnz      # padding to the long row: too much
+    else:
+        assert fmt == "sell" and nnz <= stored <= 1.2 * nnz + 256
+    x = O.uniform(7, L.n)
+    A = O.ldu2csr(L)
+    ref = O.ref_spmv(A, x)
+    ys = {}
+    for f in ("csr", "sell"):
+        M.set_format(f)
+        assert M.format()[0] == f
+        ys[f] = (M.spmv(x, row_order="fast"), M.spmv(x, transpose=True, row_order="fast"))
+    assert np.array_equal(ys["csr"][0], ys["sell"][0])
+    assert np.array_equal(ys["csr"][1], ys["sell"][1])
+    assert np.allclose(ys["sell"][0], ref, rtol=1e-14, atol=1e-14 * np.abs(ref).max())
+    # new coefficients reach the SELL copy
+    L2 = O.LDU(L.n, L.diag * 1.5, L.lower * 0.5, L.upper * 0.25, L.lower_addr, L.upper_addr)
+    M.update_values(L2.diag, L2.lower, L2.upper)
+    ref2 = O.ref_spmv(O.ldu2csr(L2), x)
+    y2 = M.spmv(x, row_order="fast")
+    assert np.allclose(y2, ref2, rtol=1e-14, atol=1e-14 * np.abs(ref2).max())
+    M.set_format("csr")
+    assert np.array_equal(M.spmv(x, row_order="fast"), y2)
+
+
 def test_norm_factor(ctx, ref_grid):
     L = O.grid_lognormal(17, 13, 11, 8)
     A = O.ldu2csr(L)
@@ -175,9 +215,10 @@ def test_solver_reference_order_is_bit_exact(ctx, ref_grid, name, case):
     assert perf.final_residual == want.final_residual
 
 
+@pytest.mark.parametrize("fmt", ["sell", "csr"])
 @pytest.mark.parametrize("case", list(CASES))
 @pytest.mark.parametrize("name", list(O.SOLVER_NAMES))
-def test_solver_fast_order_parity(ctx, name, case):
+def test_solver_fast_order_parity(ctx, name, case, fmt):
     """Fast reduction order: a different (deterministic) summation order, so
     Krylov residuals drift apart at rounding level late in the solve; the
     iteration count agrees within one, the early history within 1e-12
@@ -187,6 +228,7 @@ def test_solver_fast_order_parity(ctx, name, case):
     L, b, tol, maxit = _problem(case, kind)
     want = O.plugin_solve(kind, L, b, np.zeros(L.n), tol, maxit)
     M = _matrix(ctx, L)
+    M.set_format(fmt)
     psi = np.zeros(L.n)
     perf = cf._TABLE["cuFoam" + name]("p", M, {"tolerance": tol, "maxIter": maxit}).solve(
         psi, b, history=maxit + 1)
