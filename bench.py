@@ -42,27 +42,34 @@ WORKLOAD = "poisson7_128^3_fp64_cuFoamCG_tol1e-8"
 # ---------------------------------------------------------------------------
 # algorithmic bytes of the fused CG schedule (FP64 values, int32 indices)
 # ---------------------------------------------------------------------------
-def spmv_bytes(n: int, nnz: int) -> int:
-    """CSR SpMV compulsory traffic: values+columns, row offsets, x once, y."""
-    return 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
+# The iteration kernels stream the matrix in the format the library picked
+# for it (SELL-32 for this stencil: 12 B per stored entry incl. padding, one
+# int32 offset per 32-row slice); the set-up kernels read the CSR arrays.
+# Every figure below counts each vector a kernel touches once.
+def csr_matrix_bytes(n: int, nnz: int) -> int:
+    return 12 * nnz + 4 * (n + 1)
 
 
-def cg_spmv_bytes(n: int, nnz: int) -> int:
-    """k_f_cg_spmv: matrix, p read (gathered, counted once), q written."""
-    return spmv_bytes(n, nnz)
+def sell_matrix_bytes(n: int, stored: int) -> int:
+    return 12 * stored + 4 * ((n + 31) // 32 + 1)
 
 
-def cg_iteration_bytes(n: int, nnz: int) -> int:
+def spmv_bytes(mat: int, n: int) -> int:
+    """SpMV compulsory traffic: the matrix, x once, y written."""
+    return mat + 8 * n + 8 * n
+
+
+def cg_iteration_bytes(mat: int, n: int) -> int:
     """One CG step of the default schedule: prep (r, p, x read; p, x
-    written), spmv (q = A p), update (q, r read; r written)."""
-    return 40 * n + cg_spmv_bytes(n, nnz) + 24 * n
+    written), spmv (q = A p; p gathered, counted once), update (q, r read;
+    r written)."""
+    return 40 * n + spmv_bytes(mat, n) + 24 * n
 
 
-def solve_bytes(n: int, nnz: int, iters: int) -> int:
-    matrix = 12 * nnz + 4 * (n + 1)
-    setup = 8 * n + (matrix + 16 * n) + (matrix + 24 * n)     # nf_sum, nf_dist, res_init
-    per_iter = cg_iteration_bytes(n, nnz)
-    first = per_iter - 24 * n                                   # step 1: p = r, no x update
+def solve_bytes(mat_iter: int, mat_csr: int, n: int, iters: int) -> int:
+    setup = 8 * n + (mat_csr + 16 * n) + (mat_csr + 24 * n)     # nf_sum, nf_dist, res_init
+    per_iter = cg_iteration_bytes(mat_iter, n)
+    first = per_iter - 24 * n                                     # step 1: p = r, no x update
     flush = 24 * n
     if iters == 0:
         return setup
@@ -170,7 +177,8 @@ def cpu_baseline(L, b, iters: int):
     dt = time.perf_counter() - t0
     nf_time_share = 0  # normFactor is not part of the sample
     del nf_time_share
-    bytes_ = (12 * A.nnz + 4 * (A.n + 1) + 24 * A.n) + r.n_iterations * cg_iteration_bytes(A.n, A.nnz)
+    mat = csr_matrix_bytes(A.n, A.nnz)
+    bytes_ = (mat + 24 * A.n) + r.n_iterations * cg_iteration_bytes(mat, A.n)
     return bytes_ / dt / 1e9, O.get_threads(), dt, r.n_iterations
 
 
@@ -190,7 +198,8 @@ def run_reference(args):
         t0 = time.perf_counter()
         O.solve(O.CG, A, b, x0, 0.0, sample)
         times.append(time.perf_counter() - t0)
-    bytes_step = (12 * A.nnz + 4 * (A.n + 1) + 24 * A.n) + sample * cg_iteration_bytes(A.n, A.nnz)
+    mat = csr_matrix_bytes(A.n, A.nnz)
+    bytes_step = (mat + 24 * A.n) + sample * cg_iteration_bytes(mat, A.n)
     total = sum(times)
     value = bytes_step * args.steps / total / 1e9
     cores = O.get_threads()
@@ -233,6 +242,9 @@ def run_ours(args):
     ctx.set_stream(stream)
     M = cf.LduMatrix.from_ldu(L, ctx)
     n, nf, nnz = M.shape()
+    fmt, stored = M.format()
+    mat_csr = csr_matrix_bytes(n, nnz)
+    mat_it = sell_matrix_bytes(n, stored) if fmt == "sell" else mat_csr
     src = torch.from_numpy(b).to(f"cuda:{device}")
     psi = torch.zeros(n, dtype=torch.float64, device=f"cuda:{device}")
     solver = cf.cuFoamCG("p", M, {"tolerance": TOL, "maxIter": MAX_ITER})
@@ -267,7 +279,8 @@ def run_ours(args):
         t = torch.tensor([ms], device=f"cuda:{device}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    bytes_total = sum(solve_bytes(n, nnz, k) for k in its) * world
+    bytes_total = sum(solve_bytes(mat_it, mat_csr, n, k) for k in its) * world
+    csr_equiv = sum(solve_bytes(mat_csr, mat_csr, n, k) for k in its) * world
     value = bytes_total / (ms * 1e-3) / 1e9
     launches = sum(5 + 3 * k for k in its)  # nf_sum, nf_dist, res_init, 3/iter, flush, clear
 
@@ -298,7 +311,7 @@ def run_ours(args):
         t = torch.tensor([e_dt], device=f"cuda:{device}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e_dt = float(t.item())
-    e2e_value = sum(solve_bytes(n, nnz, k) for k in e_its) * world / e_dt / 1e9
+    e2e_value = sum(solve_bytes(mat_it, mat_csr, n, k) for k in e_its) * world / e_dt / 1e9
 
     # ---- dominant kernel: per-launch time with CUDA events (profiled solve)
     psi.zero_()
@@ -309,25 +322,27 @@ def run_ours(args):
     k2_ms = pp.kernel_ms[1] / max(pp.kernel_launches[1], 1)
     k0_ms = pp.kernel_ms[2] / max(pp.kernel_launches[2], 1)
     peak, peak_kind = measured_hbm_peak()
-    k1_gbs = cg_spmv_bytes(n, nnz) / (k1_ms * 1e-3) / 1e9
+    k1_bytes = spmv_bytes(mat_it, n)
+    k1_gbs = k1_bytes / (k1_ms * 1e-3) / 1e9
     k2_gbs = 24 * n / (k2_ms * 1e-3) / 1e9
     k0_gbs = 40 * n / (k0_ms * 1e-3) / 1e9
 
     # ---- plain SpMV (y = A x) with CUDA events ---------------------------
     x = torch.from_numpy(W.uniform(5, n)).to(f"cuda:{device}")
+    y = torch.empty_like(x)
     for _ in range(3):
-        M.spmv(x, row_order="fast")
+        M.spmv(x, row_order="fast", out=y)
     torch.cuda.synchronize()
     reps = 50
     s0 = torch.cuda.Event(enable_timing=True)
     s1 = torch.cuda.Event(enable_timing=True)
     s0.record(stream)
     for _ in range(reps):
-        M.spmv(x, row_order="fast")
+        M.spmv(x, row_order="fast", out=y)   # enqueued back to back on the stream
     s1.record(stream)
     torch.cuda.synchronize()
     spmv_ms = s0.elapsed_time(s1) / reps
-    spmv_gbs = spmv_bytes(n, nnz) / (spmv_ms * 1e-3) / 1e9
+    spmv_gbs = spmv_bytes(mat_it, n) / (spmv_ms * 1e-3) / 1e9
 
     if rank != 0:
         if dist:
@@ -336,10 +351,14 @@ def run_ours(args):
 
     extras = {}
     if world == 1 and not args.no_extras:
-        try:
-            extras["mixed_vs_fp64"] = mixed_vs_fp64(ctx, device)
-        except Exception as e:  # reported, never fatal to the headline line
-            extras["mixed_vs_fp64"] = {"error": repr(e)}
+        # C3: MR reaches 1e-10 in both precisions; BiCG (FP64 and FP32 alike)
+        # does not converge on this system, reported with its status
+        for key, solver, mx in (("mixed_vs_fp64", "cuFoamMR", 100000),
+                                ("mixed_vs_fp64_bicg", "cuFoamBiCG", 10000)):
+            try:
+                extras[key] = mixed_vs_fp64(ctx, device, solver, max_iter=mx)
+            except Exception as e:  # reported, never fatal to the headline line
+                extras[key] = {"error": repr(e)}
         try:
             extras["batched_vs_sequential"] = batched_vs_sequential(ctx, device)
         except Exception as e:
@@ -353,17 +372,20 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "rows": n, "nnz": nnz, "faces": nf,
                    "iterations": iters, "tolerance": TOL, "reduction": "fast",
-                   "l2": "inputs larger than L2 (216.9 MB per SpMV pass vs 129 MB L2)",
+                   "spmv_format": fmt, "stored_entries": stored,
+                   "l2": f"inputs larger than L2 ({spmv_bytes(mat_it, n) / 1e6:.1f} MB per SpMV "
+                         f"pass vs 129 MB L2)",
                    "parallelism": f"replicas x{world}"},
+        "csr_equivalent_gbs": round(csr_equiv / (ms * 1e-3) / 1e9, 2),
         "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": round(1e3 * e_dt / len(e_its), 3)},
         "roofline": {"bound": "hbm", "kernel": "k_f_cg_spmv", "achieved": round(k1_gbs, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(k1_gbs / peak, 4),
                      "peak_source": peak_kind,
-                     "bytes_per_launch": cg_spmv_bytes(n, nnz),
+                     "bytes_per_launch": k1_bytes,
                      "us_per_launch": round(k1_ms * 1e3, 2),
-                     "traffic": profiled_traffic("k_f_cg_spmv_poisson128.md")},
+                     "traffic": profiled_traffic("k_f_cg_spmv_sell_poisson128.md")},
         "kernels": {"k_f_cg_update_gbs": round(k2_gbs, 1), "k_f_cg_update_us": round(k2_ms * 1e3, 2),
                     "k_f_cg_prep_gbs": round(k0_gbs, 1), "k_f_cg_prep_us": round(k0_ms * 1e3, 2),
                     "spmv_gbs": round(spmv_gbs, 1), "spmv_us": round(spmv_ms * 1e3, 2),
@@ -381,46 +403,48 @@ def run_ours(args):
     return 0
 
 
-def mixed_vs_fp64(ctx, device, n: int = 256, tol: float = 1e-10, max_iter: int = 40000):
-    """BiCG on the n^3 upwind convection-diffusion system (cell Peclet up to
-    10): FP64 solve vs the mixed-precision solve (FP32 inner BiCG, FP64
-    refinement) to the same FP64 relative residual."""
+def mixed_vs_fp64(ctx, device, solver: str = "cuFoamMR", n: int = 256, pe: float = 10.0,
+                  tol: float = 1e-10, max_iter: int = 100000):
+    """One solver on the n^3 upwind convection-diffusion system (cell Peclet
+    up to pe): the plain FP64 solve vs the mixed-precision solve (FP32 inner
+    solver, FP64 residual / normFactor / refinement) to the same FP64
+    relative residual; the mixed answer's error against the FP64 one."""
     import torch
 
     import cufoam_gb300 as cf
     from cufoam_gb300 import workloads as W
     t0 = time.perf_counter()
-    L, stats = W.grid_convdiff(n, n, n, 7, 10.0)
+    L, stats = W.grid_convdiff(n, n, n, 7, pe)
     b = W.uniform(8, L.n)
     gen_s = time.perf_counter() - t0
     M = cf.LduMatrix.from_ldu(L, ctx)
     dev = f"cuda:{device}"
     src = torch.from_numpy(b).to(dev)
-    out = {"workload": f"convdiff7_upwind_{n}^3_pe{stats['pe_max']:.0f}_BiCG", "rows": L.n,
-           "tolerance": tol, "generate_s": round(gen_s, 1)}
+    out = {"workload": f"convdiff7_upwind_{n}^3_pe{stats['pe_max']:g}_{solver}", "rows": L.n,
+           "nnz": M.shape()[2], "tolerance": tol, "max_iter": max_iter, "generate_s": round(gen_s, 1)}
     res = {}
     for prec in ("FP64", "mixed"):
-        ctrl = {"tolerance": tol, "maxIter": max_iter, "precision": prec}
+        ctrl = {"tolerance": tol, "maxIter": max_iter, "precision": prec, "maxRefinements": 200}
         psi = torch.zeros(L.n, dtype=torch.float64, device=dev)
-        cf.cuFoamBiCG("U", M, dict(ctrl, maxIter=5)).solve(psi, src)  # warm-up (graphs, FP32 copy)
+        cf._TABLE[solver]("U", M, dict(ctrl, maxIter=5)).solve(psi, src)  # warm-up: graphs, FP32 copy
         psi.zero_()
         torch.cuda.synchronize()
         w0 = time.perf_counter()
-        perf = cf.cuFoamBiCG("U", M, ctrl).solve(psi, src)
+        perf = cf._TABLE[solver]("U", M, ctrl).solve(psi, src)
         torch.cuda.synchronize()
         wall = time.perf_counter() - w0
         r = src - M.spmv(psi, row_order="fast")
         true_rel = float(torch.linalg.norm(r)) / perf.norm_factor
-        res[prec] = (psi, perf, wall, true_rel)
+        res[prec] = (psi, perf)
         out[prec] = {"ms": round(perf.solve_ms, 2), "wall_ms": round(1e3 * wall, 2),
                      "iterations": perf.n_iterations, "status": perf.status_name,
-                     "final_rel_residual": perf.final_residual,
-                     "true_rel_residual": true_rel}
+                     "final_rel_residual": perf.final_residual, "true_rel_residual": true_rel}
         if prec == "mixed":
             out[prec]["refinements"] = perf.n_outer
-    x64, x32 = res["FP64"][0], res["mixed"][0]
+    (x64, p64), (x32, p32) = res["FP64"], res["mixed"]
     out["mixed"]["rel_error_vs_fp64"] = float(torch.linalg.norm(x32 - x64) / torch.linalg.norm(x64))
-    out["speedup"] = round(res["FP64"][1].solve_ms / res["mixed"][1].solve_ms, 3)
+    both = p64.status_name == "ok" and p32.status_name == "ok"
+    out["speedup"] = round(p64.solve_ms / p32.solve_ms, 3) if both else None
     M.close()
     return out
 
@@ -449,6 +473,13 @@ def batched_vs_sequential(ctx, device, n_systems: int = 512, tol: float = 1e-8,
     torch.cuda.synchronize()
     n_solves = 3 * n_systems
     ok = sum(1 for r in res if r["status"] == 0)
+    # the same batch in mixed precision (FP32 CG sweeps, FP64 refinement)
+    cfg32, _ = B.tune(packed, tolerance=tol, max_iter=max_iter, candidates=cands, use_cache=False,
+                      precision="mixed")
+    x32, res32, ms32 = B.solve(packed, tolerance=tol, max_iter=max_iter, precision="mixed")
+    torch.cuda.synchronize()
+    ok32 = sum(1 for r in res32 if r["status"] == 0)
+    err32 = float(torch.linalg.norm(x32 - x) / torch.linalg.norm(x))
     # sequential: one solve per (system, rhs) through the plugin path, device vectors
     mats = [cf.LduMatrix.from_ldu(L, ctx) for L in systems]
     srcs = [[torch.from_numpy(np.ascontiguousarray(rhs[s][j])).to(dev) for j in range(3)]
@@ -481,7 +512,14 @@ def batched_vs_sequential(ctx, device, n_systems: int = 512, tol: float = 1e-8,
             "sequential_solves_per_s": round(n_solves / (seq_ms * 1e-3), 1),
             "speedup": round(seq_ms / ms, 3),
             "iterations_batched": int(sum(r["n_iterations"] for r in res)),
-            "iterations_sequential": int(seq_iters)}
+            "iterations_sequential": int(seq_iters),
+            "mixed": {"autotuned": {"cluster": cfg32[0], "threads": cfg32[1], "order": cfg32[2]},
+                      "batched_ms": round(ms32, 2),
+                      "batched_solves_per_s": round(n_solves / (ms32 * 1e-3), 1),
+                      "converged": ok32, "speedup_vs_sequential_fp64": round(seq_ms / ms32, 3),
+                      "speedup_vs_batched_fp64": round(ms / ms32, 3),
+                      "rel_error_vs_batched_fp64": err32,
+                      "iterations": int(sum(r["n_iterations"] for r in res32))}}
 
 
 def run_profile(args):

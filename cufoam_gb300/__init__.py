@@ -84,8 +84,14 @@ class Context:
 
     def set_stream(self, stream) -> None:
         """Order the library's work on `stream` (a torch.cuda.Stream, a raw
-        cudaStream_t as int, or None for a private stream)."""
-        raw = getattr(stream, "cuda_stream", stream)
+        cudaStream_t as int, or None for a private stream).  Torch's default
+        stream (handle 0) is the legacy default stream (cudaStreamLegacy)."""
+        if stream is None:
+            raw = None
+        else:
+            raw = getattr(stream, "cuda_stream", stream)
+            if raw == 0:
+                raw = 1   # cudaStreamLegacy
         self.check(self._lib.cf_context_set_stream(self._h, C.c_void_p(raw) if raw else None),
                    "set_stream")
 
@@ -219,10 +225,19 @@ class LduMatrix:
                        "cf_matrix_export_csr")
         return ro, cols, vals
 
-    def spmv(self, x, transpose: bool = False, row_order: str = "reference"):
+    def spmv(self, x, transpose: bool = False, row_order: str = "reference", out=None):
         """y = A x (or A^T x); row_order "reference" sums rows in the
-        reference's 8-lane order, "fast" as one FMA chain."""
+        reference's 8-lane order, "fast" as one FMA chain.  With a CUDA
+        tensor `out` (and x on the device) the product is only enqueued on
+        the context's stream (no synchronisation)."""
         px, mx, kx = _ptr(x, np.float64, "x")
+        if out is not None:
+            po, mo, _ = _ptr(out, np.float64, "out")
+            if mx != _capi.CF_MEM_DEVICE or mo != _capi.CF_MEM_DEVICE:
+                raise ValueError("out= needs x and out on the device")
+            self.ctx.check(self._lib.cf_spmv_async(self._h, int(transpose), px, po, _REDUCE[row_order]),
+                           "cf_spmv_async")
+            return out
         if mx == _capi.CF_MEM_DEVICE:
             import torch
             y = torch.empty_like(kx)
@@ -245,6 +260,97 @@ class LduMatrix:
             self._h, pb, px, mb, _NORM[norm_type], _REDUCE[reduction], C.byref(out)),
             "cf_norm_factor")
         return out.value
+
+
+class CsrMatrix(LduMatrix):
+    """A square matrix given in CSR form (host arrays or CUDA tensors),
+    e.g. read from the reference's file formats (`read_csr`).  Solves,
+    SpMV and normFactor work as for an LduMatrix; coefficient updates and
+    adjoint gradients need the LDU form.  `symmetric()` is the numerical
+    symmetry of the given arrays (it selects the symmetric solver table)."""
+
+    def __init__(self, n, row_offsets, cols, vals, context: Context | None = None):
+        self.ctx = context or default_context()
+        self._lib = self.ctx._lib
+        pr, m1, kr = _ptr(row_offsets, np.int32, "row_offsets")
+        pc, m2, kc = _ptr(cols, np.int32, "cols")
+        pv, m3, kv = _ptr(vals, np.float64, "vals")
+        if len({m1, m2, m3}) != 1:
+            raise ValueError("CSR arrays must all be host arrays or all CUDA tensors")
+        nnz = int(kv.shape[0])
+        h = C.c_void_p()
+        self.ctx.check(self._lib.cf_matrix_create_csr(self.ctx.handle, int(n), nnz, pr, pc, pv, m1,
+                                                      C.byref(h)), "cf_matrix_create_csr")
+        self._h = h
+        self.n = int(n)
+        self.n_faces = -1
+        self._symmetric = _csr_symmetric(n, row_offsets, cols, vals)
+
+    def update_values(self, diag, lower, upper) -> None:
+        raise NotImplementedError("a CSR matrix has no LDU coefficients")
+
+
+def _csr_symmetric(n, ro, cols, vals) -> bool:
+    to_np = lambda a: a.detach().cpu().numpy() if hasattr(a, "detach") else np.asarray(a)
+    ro, cols, vals = to_np(ro), to_np(cols), to_np(vals)
+    rows = np.repeat(np.arange(n), np.diff(ro))
+    a = sorted(zip(rows.tolist(), cols.tolist(), vals.tolist()))
+    b = sorted(zip(cols.tolist(), rows.tolist(), vals.tolist()))
+    return a == b
+
+
+# ---------------------------------------------------------------------------
+# the reference's file formats (gis/SparseSystem/SparseCPU.h)
+# ---------------------------------------------------------------------------
+def _file_lib():
+    return _capi.load()
+
+
+def _file_check(rc, what):
+    if rc != _capi.CF_OK:
+        msg = _file_lib().cf_file_last_error().decode()
+        raise CufoamError(rc, f"{what}: {msg}")
+
+
+def read_csr(path: str):
+    """(rows, cols, row_offsets, col_indices, values) of a Rutherford-Boeing
+    file (name ending in .rb) or of the reference's binary CSR file."""
+    L = _file_lib()
+    r, c, z = C.c_int32(), C.c_int32(), C.c_int64()
+    _file_check(L.cf_csr_file_info(path.encode(), C.byref(r), C.byref(c), C.byref(z)), "cf_csr_file_info")
+    ro = np.empty(r.value + 1, np.int32)
+    ci = np.empty(max(z.value, 1), np.int32)
+    va = np.empty(max(z.value, 1), np.float64)
+    _file_check(L.cf_csr_file_read(path.encode(), ro.ctypes.data, ci.ctypes.data, va.ctypes.data),
+                "cf_csr_file_read")
+    return r.value, c.value, ro, ci[:z.value], va[:z.value]
+
+
+def save_csr(path: str, rows: int, cols: int, row_offsets, col_indices, values) -> None:
+    """The reference's binary CSR file (CPU::SparseCSR::save)."""
+    ro = np.ascontiguousarray(row_offsets, np.int32)
+    ci = np.ascontiguousarray(col_indices, np.int32)
+    va = np.ascontiguousarray(values, np.float64)
+    _file_check(_file_lib().cf_csr_file_save(path.encode(), int(rows), int(cols), int(va.shape[0]),
+                                             ro.ctypes.data, ci.ctypes.data, va.ctypes.data),
+                "cf_csr_file_save")
+
+
+def read_vector(path: str) -> np.ndarray:
+    """A Matrix Market array file (.mtx) or the reference's binary vector."""
+    L = _file_lib()
+    n = C.c_int32()
+    _file_check(L.cf_vector_file_info(path.encode(), C.byref(n)), "cf_vector_file_info")
+    v = np.empty(max(n.value, 1))
+    _file_check(L.cf_vector_file_read(path.encode(), v.ctypes.data), "cf_vector_file_read")
+    return v[:n.value]
+
+
+def save_vector(path: str, values) -> None:
+    """The reference's binary vector file (CPU::Vector::save)."""
+    v = np.ascontiguousarray(values, np.float64)
+    _file_check(_file_lib().cf_vector_file_save(path.encode(), int(v.shape[0]), v.ctypes.data),
+                "cf_vector_file_save")
 
 
 def _same(a, b) -> bool:
@@ -325,6 +431,7 @@ class LduSolver:
         c.power_max_steps = int(d.get("powerMaxSteps", 30))
         c.mixed_max_outer = int(d.get("maxRefinements", 50))
         c.mixed_inner_rtol = float(d.get("innerRelTol", 1e-4))
+        c.mixed_inner_max = int(d.get("innerMaxIter", 0))
         c.use_graph = int(d.get("useGraph", 1))
         c.time_limit_s = float(d.get("timeLimit", 0.0))
         c.profile_kernels = int(d.get("profileKernels", 0))

@@ -41,7 +41,7 @@ class cf_controls(C.Structure):
                 ("use_graph", C.c_int32), ("time_limit_s", C.c_double),
                 ("profile_kernels", C.c_int32), ("transpose", C.c_int32),
                 ("absolute_tolerance", C.c_int32), ("history_time", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("mixed_inner_max", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class cf_perf(C.Structure):
@@ -111,9 +111,19 @@ def load(build_if_missing: bool = True):
                                         C.POINTER(C.c_int64)]),
         "cf_matrix_export_csr": (C.c_int32, [P, C.c_int32, P, P, P, C.c_int32]),
         "cf_matrix_set_format": (C.c_int32, [P, C.c_int32]),
+        "cf_matrix_create_csr": (C.c_int32, [P, C.c_int32, C.c_int64, P, P, P, C.c_int32, P]),
+        "cf_csr_file_info": (C.c_int32, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_int64)]),
+        "cf_csr_file_read": (C.c_int32, [C.c_char_p, P, P, P]),
+        "cf_csr_file_save": (C.c_int32, [C.c_char_p, C.c_int32, C.c_int32, C.c_int64, P, P, P]),
+        "cf_vector_file_info": (C.c_int32, [C.c_char_p, C.POINTER(C.c_int32)]),
+        "cf_vector_file_read": (C.c_int32, [C.c_char_p, P]),
+        "cf_vector_file_save": (C.c_int32, [C.c_char_p, C.c_int32, P]),
+        "cf_file_last_error": (C.c_char_p, []),
         "cf_matrix_format": (C.c_int32, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
         "cf_ldu2csr": (C.c_int32, [P, C.POINTER(cf_ldu_view), P, P, P, C.c_int32]),
         "cf_spmv": (C.c_int32, [P, C.c_int32, P, P, C.c_int32, C.c_int32]),
+        "cf_spmv_async": (C.c_int32, [P, C.c_int32, P, P, C.c_int32]),
         "cf_norm_factor": (C.c_int32, [P, P, P, C.c_int32, C.c_int32, C.c_int32,
                                        C.POINTER(C.c_double)]),
         "cf_solve": (C.c_int32, [P, C.c_int32, C.POINTER(cf_controls), P, P,

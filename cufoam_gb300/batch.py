@@ -112,8 +112,11 @@ class BatchSolver:
 
     # ---- solve ------------------------------------------------------------
     def solve(self, sources, psi=None, tolerance: float = 1e-6, max_iter: int = 1000,
-              config=None, use_graph: bool = True):
-        """Returns (psi in the batch layout, per-(system, rhs) results, device ms)."""
+              config=None, use_graph: bool = True, precision: str = "FP64",
+              inner_rtol: float = 1e-4):
+        """Returns (psi in the batch layout, per-(system, rhs) results, device ms).
+        precision "mixed": FP32 CG sweeps (inner relative tolerance
+        `inner_rtol`) inside FP64 refinement; n_iterations counts FP32 steps."""
         if isinstance(sources, (list, tuple)):
             sources = self.pack(sources)
         if _is_torch(sources):
@@ -132,6 +135,8 @@ class BatchSolver:
         c.max_iter = max_iter
         c.memory = mem
         c.use_graph = 1 if use_graph else 0
+        c.precision = {"FP64": _capi.CF_PREC_FP64, "mixed": _capi.CF_PREC_MIXED}[precision]
+        c.mixed_inner_rtol = inner_rtol
         cfg = cf_batch_config()
         cs, bt, order = config or self.config or (4, 256, 0)
         cfg.cluster_size, cfg.threads, cfg.order = cs, bt, order
@@ -156,11 +161,12 @@ class BatchSolver:
         return hashlib.sha1(key.encode()).hexdigest()[:16]
 
     def tune(self, sources, tolerance: float = 1e-6, max_iter: int = 1000, reps: int = 1,
-             candidates=None, use_cache: bool = True, verbose: bool = False):
+             candidates=None, use_cache: bool = True, verbose: bool = False,
+             precision: str = "FP64"):
         """Time every schedule candidate on this batch, keep the fastest and
         remember it per (device, size histogram) in a JSON cache."""
         path = _cache_path()
-        sig = self.signature()
+        sig = self.signature() + ("" if precision == "FP64" else "|" + precision)
         cache = {}
         if use_cache and os.path.exists(path):
             try:
@@ -174,7 +180,8 @@ class BatchSolver:
         for cand in candidates or CANDIDATES:
             best = None
             for _ in range(reps):
-                _, out, ms = self.solve(sources, tolerance=tolerance, max_iter=max_iter, config=cand)
+                _, out, ms = self.solve(sources, tolerance=tolerance, max_iter=max_iter, config=cand,
+                                        precision=precision)
                 best = ms if best is None else min(best, ms)
             timings[cand] = best
             if verbose:

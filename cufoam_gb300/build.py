@@ -16,7 +16,8 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libcufoam_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
-SOURCES = ["capi.cu", "matrix.cu", "solve_fp64.cu", "solve_fast.cu", "mixed.cu", "adjoint.cu", "batched.cu", "noalloc.cu"]
+SOURCES = ["capi.cu", "matrix.cu", "solve_fp64.cu", "solve_fast.cu", "mixed.cu", "adjoint.cu", "batched.cu",
+           "noalloc.cu", "formats.cpp"]
 HEADERS = ["internal.h", "device.cuh", "solver_common.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -29,8 +30,12 @@ def nvcc() -> str:
 
 
 def _flags() -> list[str]:
+    # CUFOAM_NVCC_DEFINES: extra -D definitions for the kernel tuning
+    # constants (CF_SELL_BATCH, CF_SPMV_MIN_BLOCKS, ...) when sweeping them
+    extra = os.environ.get("CUFOAM_NVCC_DEFINES", "").split()
     return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                   "-I" + INCLUDE, "-I" + CSRC, "--expt-relaxed-constexpr"]
+                   "-I" + INCLUDE, "-I" + CSRC, "--expt-relaxed-constexpr"] + \
+        [d for d in extra if d.startswith("-D")]
 
 
 def _newest(paths: list[str]) -> float:
@@ -107,7 +112,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     jobs = []
     for src in SOURCES:
         sp = os.path.join(CSRC, src)
-        op = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
+        op = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(op)
         if force or not os.path.exists(op) or os.path.getmtime(op) < max(os.path.getmtime(sp), hdr_time):
             jobs.append((sp, op))

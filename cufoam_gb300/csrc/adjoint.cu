@@ -36,6 +36,7 @@ void adjoint_gradients(Matrix *m, const double *lam, const double *x, double *d_
                        double *d_lower, double *d_upper)
 {
     Context *ctx = m->ctx;
+    require(!m->from_csr, CF_UNSUPPORTED, "gradients need an LDU matrix (this one was created from CSR)");
     const int g = ctx->sm_count * 8;
     if (m->nf > 0 && (d_lower || d_upper)) {
         k_adjoint_faces<<<g, kBlock, 0, ctx->stream>>>(m->nf, m->la.as<int32_t>(), m->ua.as<int32_t>(),

@@ -14,6 +14,12 @@
 // identical control flow.  Each right-hand side keeps its own CG scalars and
 // stopping test (the reference's loop, SolverSingleGPU.h:366-445, with its
 // normFactor, gis/gis.cu:106-123); a converged component is frozen.
+//
+// Mixed precision (k_batch_cg<R, BT, true>): after the FP64 normFactor and
+// residual, each refinement sweep solves A e = r / ||r|| by CG with FP32
+// values, FP32 vectors and FP32 per-thread sums (combined across CTAs in
+// FP64) to a relative inner tolerance, then adds ||r|| e to x and forms the
+// FP64 residual b - A x again; the FP64 tolerance decides convergence.
 #include <cooperative_groups.h>
 
 #include "device.cuh"
@@ -36,6 +42,7 @@ struct BatchSystem {
     const int32_t *ro;
     const int32_t *col;
     const double *val;
+    const float *val32;      // FP32 copy (mixed precision)
 };
 
 struct BatchResult {
@@ -54,6 +61,10 @@ struct BatchArgs {
     double *r, *p0, *p1, *q; // [rows][R] work
     int32_t *queue;          // next position in `order`
     BatchResult *out;        // [n_systems][R]
+    // mixed precision: FP32 inner CG on A32 e = r / ||r||, FP64 refinement
+    float *r32, *p32a, *p32b, *q32, *e32;   // [rows][R]
+    double inner_rtol;
+    int32_t max_outer;
 };
 
 // sum over the block (fixed order), then over the cluster in rank order
@@ -90,7 +101,38 @@ __device__ __forceinline__ void cluster_sum(cgp::cluster_group &cl, double (&v)[
     __syncthreads();
 }
 
+// FP64 residual r = b - A x and ||r||^2 per component over this CTA's rows,
+// summed over the cluster into tot[0..R)
 template <int R, int BT>
+__device__ __forceinline__ void batch_residual(cgp::cluster_group &cl, int lo, int hi, const int32_t *ro,
+                                               const int32_t *col, const double *val, const double *b,
+                                               const double *x, double *r, double *wsm, double *slot,
+                                               double *tot)
+{
+    double acc[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) acc[j] = 0.0;
+    for (int i = lo + threadIdx.x; i < hi; i += BT) {
+        double y[R];
+#pragma unroll
+        for (int j = 0; j < R; ++j) y[j] = 0.0;
+        for (int e = ro[i]; e < ro[i + 1]; ++e) {
+            const double v = val[e];
+            const int64_t c = (int64_t)col[e] * R;
+#pragma unroll
+            for (int j = 0; j < R; ++j) y[j] = fma_t(v, __ldcg(x + c + j), y[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            const double ri = b[(int64_t)i * R + j] - y[j];
+            r[(int64_t)i * R + j] = ri;
+            acc[j] = fma_t(ri, ri, acc[j]);
+        }
+    }
+    cluster_sum<R, BT>(cl, acc, wsm, slot, tot);
+}
+
+template <int R, int BT, bool MIXED>
 __global__ void __launch_bounds__(BT) k_batch_cg(const BatchArgs a)
 {
     cgp::cluster_group cl = cgp::this_cluster();
@@ -185,77 +227,218 @@ __global__ void __launch_bounds__(BT) k_batch_cg(const BatchArgs a)
             a.out[(int64_t)sid * R + j].norm0 = nrm[j];
         }
 
-        // ---- CG iterations, all components together ----------------------
-        for (int k = 1; any && k <= a.max_iter; ++k) {
-            const double *pin = pb[(k + 1) & 1];
-            double *pout = pb[k & 1];
-            double beta[R];
+        // ---- mixed precision: FP32 CG sweeps inside FP64 refinement -----
+        if constexpr (MIXED) {
+            float *r32 = a.r32 + S.vec_offset * R;
+            float *e32 = a.e32 + S.vec_offset * R;
+            float *q32 = a.q32 + S.vec_offset * R;
+            float *pb32[2] = {a.p32a + S.vec_offset * R, a.p32b + S.vec_offset * R};
+            const float *val32 = S.val32;
+            for (int sweep = 0; any && sweep < a.max_outer; ++sweep) {
+                // inner right-hand side r / ||r||, e = 0
+                float inv[R], eta[R];
+                bool act[R];
+                bool any_in = false;
 #pragma unroll
-            for (int j = 0; j < R; ++j) beta[j] = (k > 1) ? rho0[j] / rho1[j] : 0.0;
-            // phase A: p = r + beta p_old (on the fly), q = A p, (p, q)
-            double acc[R];
+                for (int j = 0; j < R; ++j) {
+                    act[j] = active[j];
+                    inv[j] = active[j] ? (float)(1.0 / nrm[j]) : 0.f;
+                    // the last sweep only has to reach the FP64 target
+                    eta[j] = (float)fmax(a.inner_rtol, fmin(0.5, 0.5 * tolj[j] / nrm[j]));
+                    any_in = any_in || act[j];
+                }
+                double acc0[R];
 #pragma unroll
-            for (int j = 0; j < R; ++j) acc[j] = 0.0;
-            for (int i = lo + threadIdx.x; i < hi; i += BT) {
-                double y[R];
-#pragma unroll
-                for (int j = 0; j < R; ++j) y[j] = 0.0;
-                for (int e = ro[i]; e < ro[i + 1]; ++e) {
-                    const double v = val[e];
-                    const int64_t c = (int64_t)col[e] * R;
+                for (int j = 0; j < R; ++j) acc0[j] = 0.0;
+                for (int i = lo + threadIdx.x; i < hi; i += BT)
 #pragma unroll
                     for (int j = 0; j < R; ++j) {
-                        const double pc = (k > 1) ? fma_t(beta[j], __ldcg(pin + c + j), __ldcg(r + c + j))
-                                                  : __ldcg(r + c + j);
-                        y[j] = fma_t(v, active[j] ? pc : 0.0, y[j]);
+                        const int64_t o = (int64_t)i * R + j;
+                        const float v = (float)(r[o] * (double)inv[j]);
+                        r32[o] = v;
+                        e32[o] = 0.f;
+                        acc0[j] += (double)(v * v);
                     }
-                }
+                cluster_sum<R, BT>(cl, acc0, wsm, slot[parity], tot);
+                parity ^= 1;
+                float rho0f[R], rho1f[R];
 #pragma unroll
                 for (int j = 0; j < R; ++j) {
-                    const int64_t o = (int64_t)i * R + j;
-                    const double pi = (k > 1) ? fma_t(beta[j], __ldcg(pin + o), __ldcg(r + o)) : __ldcg(r + o);
-                    pout[o] = active[j] ? pi : __ldcg(pin + o);
-                    q[o] = y[j];
-                    acc[j] = fma_t(pi, y[j], acc[j]);
+                    rho0f[j] = (float)tot[j];
+                    rho1f[j] = 0.f;
                 }
-            }
-            cluster_sum<R, BT>(cl, acc, wsm, slot[parity], tot);
-            parity ^= 1;
-            double xi[R];
+                __syncthreads();
+                int kin = 0;
+                for (int k = 1; any_in; ++k) {
+                    const float *pin = pb32[(k + 1) & 1];
+                    float *pout = pb32[k & 1];
+                    float beta[R];
 #pragma unroll
-            for (int j = 0; j < R; ++j) xi[j] = active[j] ? rho0[j] / tot[j] : 0.0;
-            __syncthreads();
-            // phase B: x += xi p, r -= xi q, (r, r)
-            double acc2[R];
+                    for (int j = 0; j < R; ++j) beta[j] = (k > 1) ? rho0f[j] / rho1f[j] : 0.f;
+                    double acc[R];
 #pragma unroll
-            for (int j = 0; j < R; ++j) acc2[j] = 0.0;
-            for (int i = lo + threadIdx.x; i < hi; i += BT) {
+                    for (int j = 0; j < R; ++j) acc[j] = 0.0;
+                    for (int i = lo + threadIdx.x; i < hi; i += BT) {
+                        float y[R], part[R];
+#pragma unroll
+                        for (int j = 0; j < R; ++j) y[j] = 0.f;
+                        for (int e = ro[i]; e < ro[i + 1]; ++e) {
+                            const float v = val32[e];
+                            const int64_t c = (int64_t)col[e] * R;
+#pragma unroll
+                            for (int j = 0; j < R; ++j) {
+                                const float pc = (k > 1) ? fma_t(beta[j], __ldcg(pin + c + j), __ldcg(r32 + c + j))
+                                                         : __ldcg(r32 + c + j);
+                                y[j] = fma_t(v, act[j] ? pc : 0.f, y[j]);
+                            }
+                        }
+#pragma unroll
+                        for (int j = 0; j < R; ++j) {
+                            const int64_t o = (int64_t)i * R + j;
+                            const float pi = (k > 1) ? fma_t(beta[j], __ldcg(pin + o), __ldcg(r32 + o))
+                                                     : __ldcg(r32 + o);
+                            pout[o] = act[j] ? pi : __ldcg(pin + o);
+                            q32[o] = y[j];
+                            part[j] = pi * y[j];
+                            acc[j] += (double)part[j];
+                        }
+                    }
+                    cluster_sum<R, BT>(cl, acc, wsm, slot[parity], tot);
+                    parity ^= 1;
+                    float xi[R];
+#pragma unroll
+                    for (int j = 0; j < R; ++j) xi[j] = act[j] ? rho0f[j] / (float)tot[j] : 0.f;
+                    __syncthreads();
+                    double acc2[R];
+#pragma unroll
+                    for (int j = 0; j < R; ++j) acc2[j] = 0.0;
+                    for (int i = lo + threadIdx.x; i < hi; i += BT) {
+#pragma unroll
+                        for (int j = 0; j < R; ++j) {
+                            const int64_t o = (int64_t)i * R + j;
+                            if (act[j]) {
+                                e32[o] = fma_t(xi[j], pout[o], e32[o]);
+                                const float ri = fma_t(-xi[j], q32[o], r32[o]);
+                                r32[o] = ri;
+                                acc2[j] += (double)(ri * ri);
+                            }
+                        }
+                    }
+                    cluster_sum<R, BT>(cl, acc2, wsm, slot[parity], tot);
+                    parity ^= 1;
+                    any_in = false;
+#pragma unroll
+                    for (int j = 0; j < R; ++j) {
+                        if (act[j]) {
+                            rho1f[j] = rho0f[j];
+                            rho0f[j] = (float)tot[j];
+                            iters[j] += 1;
+                            const float nin = sqrtf(rho0f[j]);
+                            act[j] = isfinite(nin) && nin > eta[j] && iters[j] < a.max_iter;
+                        }
+                        any_in = any_in || act[j];
+                    }
+                    kin = k;
+                    __syncthreads();
+                }
+                (void)kin;
+                // x += ||r|| e in FP64, then the FP64 residual
+                for (int i = lo + threadIdx.x; i < hi; i += BT)
+#pragma unroll
+                    for (int j = 0; j < R; ++j) {
+                        const int64_t o = (int64_t)i * R + j;
+                        if (active[j]) x[o] = fma_t(nrm[j], (double)e32[o], x[o]);
+                    }
+                cl.sync(); // every CTA's x rows are written before anyone gathers them
+                batch_residual<R, BT>(cl, lo, hi, ro, col, val, b, x, r, wsm, slot[parity], tot);
+                parity ^= 1;
+                any = false;
 #pragma unroll
                 for (int j = 0; j < R; ++j) {
-                    const int64_t o = (int64_t)i * R + j;
                     if (active[j]) {
-                        x[o] = fma_t(xi[j], pout[o], x[o]);
-                        const double ri = fma_t(-xi[j], q[o], r[o]);
-                        r[o] = ri;
-                        acc2[j] = fma_t(ri, ri, acc2[j]);
+                        const double nn = sqrt(tot[j]);
+                        // a sweep that does not reduce the FP64 residual ends the solve
+                        const bool progress = nn < nrm[j];
+                        nrm[j] = nn;
+                        active[j] = isfinite(nn) && nn > tolj[j] && progress && iters[j] < a.max_iter;
+                    }
+                    any = any || active[j];
+                }
+                __syncthreads();
+            }
+        } else {
+            // ---- CG iterations, all components together ----------------------
+            for (int k = 1; any && k <= a.max_iter; ++k) {
+                const double *pin = pb[(k + 1) & 1];
+                double *pout = pb[k & 1];
+                double beta[R];
+    #pragma unroll
+                for (int j = 0; j < R; ++j) beta[j] = (k > 1) ? rho0[j] / rho1[j] : 0.0;
+                // phase A: p = r + beta p_old (on the fly), q = A p, (p, q)
+                double acc[R];
+    #pragma unroll
+                for (int j = 0; j < R; ++j) acc[j] = 0.0;
+                for (int i = lo + threadIdx.x; i < hi; i += BT) {
+                    double y[R];
+    #pragma unroll
+                    for (int j = 0; j < R; ++j) y[j] = 0.0;
+                    for (int e = ro[i]; e < ro[i + 1]; ++e) {
+                        const double v = val[e];
+                        const int64_t c = (int64_t)col[e] * R;
+    #pragma unroll
+                        for (int j = 0; j < R; ++j) {
+                            const double pc = (k > 1) ? fma_t(beta[j], __ldcg(pin + c + j), __ldcg(r + c + j))
+                                                      : __ldcg(r + c + j);
+                            y[j] = fma_t(v, active[j] ? pc : 0.0, y[j]);
+                        }
+                    }
+    #pragma unroll
+                    for (int j = 0; j < R; ++j) {
+                        const int64_t o = (int64_t)i * R + j;
+                        const double pi = (k > 1) ? fma_t(beta[j], __ldcg(pin + o), __ldcg(r + o)) : __ldcg(r + o);
+                        pout[o] = active[j] ? pi : __ldcg(pin + o);
+                        q[o] = y[j];
+                        acc[j] = fma_t(pi, y[j], acc[j]);
                     }
                 }
-            }
-            cluster_sum<R, BT>(cl, acc2, wsm, slot[parity], tot);
-            parity ^= 1;
-            any = false;
-#pragma unroll
-            for (int j = 0; j < R; ++j) {
-                if (active[j]) {
-                    rho1[j] = rho0[j];
-                    rho0[j] = tot[j];
-                    nrm[j] = sqrt(rho0[j]);
-                    iters[j] = k;
-                    active[j] = isfinite(nrm[j]) && k < a.max_iter && nrm[j] > tolj[j];
+                cluster_sum<R, BT>(cl, acc, wsm, slot[parity], tot);
+                parity ^= 1;
+                double xi[R];
+    #pragma unroll
+                for (int j = 0; j < R; ++j) xi[j] = active[j] ? rho0[j] / tot[j] : 0.0;
+                __syncthreads();
+                // phase B: x += xi p, r -= xi q, (r, r)
+                double acc2[R];
+    #pragma unroll
+                for (int j = 0; j < R; ++j) acc2[j] = 0.0;
+                for (int i = lo + threadIdx.x; i < hi; i += BT) {
+    #pragma unroll
+                    for (int j = 0; j < R; ++j) {
+                        const int64_t o = (int64_t)i * R + j;
+                        if (active[j]) {
+                            x[o] = fma_t(xi[j], pout[o], x[o]);
+                            const double ri = fma_t(-xi[j], q[o], r[o]);
+                            r[o] = ri;
+                            acc2[j] = fma_t(ri, ri, acc2[j]);
+                        }
+                    }
                 }
-                any = any || active[j];
+                cluster_sum<R, BT>(cl, acc2, wsm, slot[parity], tot);
+                parity ^= 1;
+                any = false;
+    #pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    if (active[j]) {
+                        rho1[j] = rho0[j];
+                        rho0[j] = tot[j];
+                        nrm[j] = sqrt(rho0[j]);
+                        iters[j] = k;
+                        active[j] = isfinite(nrm[j]) && k < a.max_iter && nrm[j] > tolj[j];
+                    }
+                    any = any || active[j];
+                }
+                __syncthreads();
             }
-            __syncthreads();
         }
         if (rank == 0 && threadIdx.x < R) {
             const int j = threadIdx.x;
@@ -277,6 +460,8 @@ struct Batch {
     std::vector<int64_t> offsets;   // first row of each system
     int64_t rows = 0;
     DeviceBuffer d_sys, d_order, d_queue, d_out, d_b, d_x, d_r, d_p0, d_p1, d_q;
+    DeviceBuffer d_r32, d_p32a, d_p32b, d_q32, d_e32;
+    bool have_32 = false;
     std::vector<int32_t> order;
     ~Batch()
     {
@@ -324,7 +509,7 @@ Batch *batch_create(Context *ctx, int n_systems, const cf_ldu_view *views)
 
 void batch_destroy(Batch *B) { delete B; }
 
-template <int R, int BT>
+template <int R, int BT, bool MIXED>
 static void launch_batch(Context *ctx, const BatchArgs &args, int cs, int max_clusters, cudaStream_t s)
 {
     cudaLaunchConfig_t cfg = {};
@@ -340,20 +525,28 @@ static void launch_batch(Context *ctx, const BatchArgs &args, int cs, int max_cl
     cfg.numAttrs = 1;
     int nclusters = 0;
     cfg.gridDim = dim3(cs);
-    CF_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, (void *)k_batch_cg<R, BT>, &cfg));
+    CF_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, (void *)k_batch_cg<R, BT, MIXED>, &cfg));
     if (nclusters < 1) nclusters = 1;
     if (max_clusters > 0 && nclusters > max_clusters) nclusters = max_clusters;
     cfg.gridDim = dim3(nclusters * cs);
-    CF_CUDA(cudaLaunchKernelEx(&cfg, k_batch_cg<R, BT>, args));
+    CF_CUDA(cudaLaunchKernelEx(&cfg, k_batch_cg<R, BT, MIXED>, args));
+}
+
+template <int R, bool MIXED>
+static void launch_batch_m(Context *ctx, const BatchArgs &args, int cs, int bt, int max_clusters,
+                           cudaStream_t s)
+{
+    if (bt == 128) launch_batch<R, 128, MIXED>(ctx, args, cs, max_clusters, s);
+    else if (bt == 512) launch_batch<R, 512, MIXED>(ctx, args, cs, max_clusters, s);
+    else launch_batch<R, 256, MIXED>(ctx, args, cs, max_clusters, s);
 }
 
 template <int R>
-static void launch_batch_r(Context *ctx, const BatchArgs &args, int cs, int bt, int max_clusters,
+static void launch_batch_r(Context *ctx, const BatchArgs &args, bool mixed, int cs, int bt, int max_clusters,
                            cudaStream_t s)
 {
-    if (bt == 128) launch_batch<R, 128>(ctx, args, cs, max_clusters, s);
-    else if (bt == 512) launch_batch<R, 512>(ctx, args, cs, max_clusters, s);
-    else launch_batch<R, 256>(ctx, args, cs, max_clusters, s);
+    if (mixed) launch_batch_m<R, true>(ctx, args, cs, bt, max_clusters, s);
+    else launch_batch_m<R, false>(ctx, args, cs, bt, max_clusters, s);
 }
 
 // Solve all systems for `nrhs` right-hand sides (b, x: [rows][nrhs]).
@@ -362,8 +555,30 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
 {
     Context *ctx = B->ctx;
     require(nrhs >= 1 && nrhs <= kBatchMaxR, CF_BAD_INPUT, "1..4 right-hand sides per system");
-    require(c.precision == CF_PREC_FP64, CF_UNSUPPORTED, "batched solves are FP64 CG");
+    require(c.precision == CF_PREC_FP64 || c.precision == CF_PREC_MIXED, CF_BAD_INPUT, "bad precision");
+    const bool mixed = c.precision == CF_PREC_MIXED;
     const int S = (int)B->mats.size();
+    if (mixed && !B->have_32) {
+        // FP32 value copies, then the system table with their pointers
+        std::vector<BatchSystem> hs(S);
+        CF_CUDA(cudaMemcpy(hs.data(), B->d_sys.ptr, sizeof(BatchSystem) * S, cudaMemcpyDeviceToHost));
+        for (int s2 = 0; s2 < S; ++s2) {
+            matrix_ensure_fp32(B->mats[s2], false);
+            hs[s2].val32 = B->mats[s2]->val32.as<float>();
+        }
+        CF_CUDA(cudaMemcpyAsync(B->d_sys.ptr, hs.data(), sizeof(BatchSystem) * S, cudaMemcpyHostToDevice,
+                                ctx->stream));
+        CF_CUDA(cudaStreamSynchronize(ctx->stream));
+        B->have_32 = true;
+    }
+    if (mixed) {
+        const size_t fb = sizeof(float) * (size_t)(B->rows * nrhs + 8);
+        B->d_r32.ensure(fb);
+        B->d_p32a.ensure(fb);
+        B->d_p32b.ensure(fb);
+        B->d_q32.ensure(fb);
+        B->d_e32.ensure(fb);
+    }
     const size_t vb = sizeof(double) * (size_t)(B->rows * nrhs + 8);
     B->d_r.ensure(vb);
     B->d_p0.ensure(vb);
@@ -402,6 +617,13 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
     a.q = B->d_q.as<double>();
     a.queue = B->d_queue.as<int32_t>();
     a.out = B->d_out.as<BatchResult>();
+    a.r32 = mixed ? B->d_r32.as<float>() : nullptr;
+    a.p32a = mixed ? B->d_p32a.as<float>() : nullptr;
+    a.p32b = mixed ? B->d_p32b.as<float>() : nullptr;
+    a.q32 = mixed ? B->d_q32.as<float>() : nullptr;
+    a.e32 = mixed ? B->d_e32.as<float>() : nullptr;
+    a.inner_rtol = (c.mixed_inner_rtol > 0 && c.mixed_inner_rtol < 1) ? c.mixed_inner_rtol : 1e-4;
+    a.max_outer = c.mixed_max_outer > 0 ? c.mixed_max_outer : 50;
     const int cs = cfg && cfg->cluster_size > 0 ? cfg->cluster_size : 4;
     const int bt = cfg && cfg->threads > 0 ? cfg->threads : 256;
     const int maxc = cfg ? cfg->max_clusters : 0;
@@ -421,10 +643,10 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
             CF_CUDA(cudaStreamBeginCapture(cs_stream, cudaStreamCaptureModeThreadLocal));
             CF_CUDA(cudaMemsetAsync(B->d_queue.ptr, 0, sizeof(int32_t), cs_stream));
             switch (nrhs) {
-            case 1: launch_batch_r<1>(ctx, a, cs, bt, maxc, cs_stream); break;
-            case 2: launch_batch_r<2>(ctx, a, cs, bt, maxc, cs_stream); break;
-            case 3: launch_batch_r<3>(ctx, a, cs, bt, maxc, cs_stream); break;
-            default: launch_batch_r<4>(ctx, a, cs, bt, maxc, cs_stream); break;
+            case 1: launch_batch_r<1>(ctx, a, mixed, cs, bt, maxc, cs_stream); break;
+            case 2: launch_batch_r<2>(ctx, a, mixed, cs, bt, maxc, cs_stream); break;
+            case 3: launch_batch_r<3>(ctx, a, mixed, cs, bt, maxc, cs_stream); break;
+            default: launch_batch_r<4>(ctx, a, mixed, cs, bt, maxc, cs_stream); break;
             }
             CF_CUDA(cudaStreamEndCapture(cs_stream, &g));
             CF_CUDA(cudaGraphInstantiate(&ge, g, 0));
@@ -441,10 +663,10 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
         }
     } else {
         switch (nrhs) {
-        case 1: launch_batch_r<1>(ctx, a, cs, bt, maxc, ctx->stream); break;
-        case 2: launch_batch_r<2>(ctx, a, cs, bt, maxc, ctx->stream); break;
-        case 3: launch_batch_r<3>(ctx, a, cs, bt, maxc, ctx->stream); break;
-        default: launch_batch_r<4>(ctx, a, cs, bt, maxc, ctx->stream); break;
+        case 1: launch_batch_r<1>(ctx, a, mixed, cs, bt, maxc, ctx->stream); break;
+        case 2: launch_batch_r<2>(ctx, a, mixed, cs, bt, maxc, ctx->stream); break;
+        case 3: launch_batch_r<3>(ctx, a, mixed, cs, bt, maxc, ctx->stream); break;
+        default: launch_batch_r<4>(ctx, a, mixed, cs, bt, maxc, ctx->stream); break;
         }
     }
     CF_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));

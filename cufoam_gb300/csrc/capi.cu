@@ -77,7 +77,7 @@ Context::~Context()
     if (ev_stop) cudaEventDestroy(ev_stop);
     if (ev_mid) cudaEventDestroy(ev_mid);
     for (cudaEvent_t e : prof_events) cudaEventDestroy(e);
-    if (stream) cudaStreamDestroy(stream);
+    if (stream && own_stream) cudaStreamDestroy(stream);
 }
 
 Context *context_create(int device)
@@ -93,6 +93,7 @@ Context *context_create(int device)
     try {
         ctx->device = device;
         CF_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ctx->own_stream = true;
         CF_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
         CF_CUDA(cudaDeviceGetAttribute(&ctx->max_threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, device));
         int l2 = 0;
@@ -168,9 +169,94 @@ static cf_status guarded(cf_context *ctx, F f)
     }
 }
 
+// file calls have no context: their errors go to a per-thread message
+static thread_local std::string g_file_error;
+
+template <class F>
+static cf_status file_guarded(F f)
+{
+    try {
+        g_file_error.clear();
+        f();
+        return CF_OK;
+    } catch (const Error &e) {
+        g_file_error = e.msg;
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        g_file_error = "host allocation failed";
+        return CF_OUT_OF_MEMORY;
+    } catch (...) {
+        g_file_error = "unexpected internal error";
+        return CF_CUDA_ERROR;
+    }
+}
+
 extern "C" {
 
 int32_t cf_abi_version(void) { return CF_ABI_VERSION; }
+
+const char *cf_file_last_error(void) { return g_file_error.c_str(); }
+
+cf_status cf_csr_file_info(const char *path, int32_t *rows, int32_t *cols, int64_t *nnz)
+{
+    if (!path) return CF_BAD_INPUT;
+    return file_guarded([&] {
+        cf::HostCsr A;
+        cf::read_csr_file(path, A);
+        if (rows) *rows = A.rows;
+        if (cols) *cols = A.cols;
+        if (nnz) *nnz = (int64_t)A.values.size();
+    });
+}
+
+cf_status cf_csr_file_read(const char *path, int32_t *row_offsets, int32_t *cols, double *vals)
+{
+    if (!path || !row_offsets) return CF_BAD_INPUT;
+    return file_guarded([&] {
+        cf::HostCsr A;
+        cf::read_csr_file(path, A);
+        cf::require(A.values.empty() || (cols && vals), CF_BAD_INPUT, "null output array");
+        std::memcpy(row_offsets, A.row_offsets.data(), sizeof(int32_t) * A.row_offsets.size());
+        if (!A.values.empty()) {
+            std::memcpy(cols, A.cols_idx.data(), sizeof(int32_t) * A.cols_idx.size());
+            std::memcpy(vals, A.values.data(), sizeof(double) * A.values.size());
+        }
+    });
+}
+
+cf_status cf_csr_file_save(const char *path, int32_t rows, int32_t cols, int64_t nnz,
+                           const int32_t *row_offsets, const int32_t *cols_idx, const double *vals)
+{
+    if (!path || (rows > 0 && !row_offsets) || (nnz > 0 && (!cols_idx || !vals))) return CF_BAD_INPUT;
+    return file_guarded([&] { cf::save_csr_file(path, rows, cols, nnz, row_offsets, cols_idx, vals); });
+}
+
+cf_status cf_vector_file_info(const char *path, int32_t *size)
+{
+    if (!path) return CF_BAD_INPUT;
+    return file_guarded([&] {
+        std::vector<double> v;
+        cf::read_vector_file(path, v);
+        if (size) *size = (int32_t)v.size();
+    });
+}
+
+cf_status cf_vector_file_read(const char *path, double *values)
+{
+    if (!path) return CF_BAD_INPUT;
+    return file_guarded([&] {
+        std::vector<double> v;
+        cf::read_vector_file(path, v);
+        cf::require(v.empty() || values, CF_BAD_INPUT, "null output array");
+        if (!v.empty()) std::memcpy(values, v.data(), sizeof(double) * v.size());
+    });
+}
+
+cf_status cf_vector_file_save(const char *path, int32_t size, const double *values)
+{
+    if (!path || (size > 0 && !values)) return CF_BAD_INPUT;
+    return file_guarded([&] { cf::save_vector_file(path, size, values); });
+}
 
 const char *cf_status_string(int32_t s)
 {
@@ -256,11 +342,14 @@ cf_status cf_context_set_stream(cf_context *ctx, void *stream)
     return guarded(ctx, [&] {
         cf::Context *c = ctx->impl;
         CF_CUDA(cudaStreamSynchronize(c->stream));
-        if (stream) {
-            c->stream = static_cast<cudaStream_t>(stream);
-        } else {
-            CF_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        cudaStream_t next = static_cast<cudaStream_t>(stream);
+        if (!stream) {
+            if (c->own_stream) return;   // already on a private stream
+            CF_CUDA(cudaStreamCreateWithFlags(&next, cudaStreamNonBlocking));
         }
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        c->stream = next;
+        c->own_stream = stream == nullptr;
     });
 }
 
@@ -299,6 +388,42 @@ cf_status cf_matrix_create_ldu(cf_context *ctx, const cf_ldu_view *ldu, cf_matri
                     "bad memory kind");
         m = cf::matrix_create(ctx->impl, *ldu);
         CF_CUDA(cudaStreamSynchronize(ctx->impl->stream));
+    });
+    if (st != CF_OK) return st;
+    *out = new (std::nothrow) cf_matrix{m, ctx};
+    if (!*out) {
+        delete m;
+        return CF_OUT_OF_MEMORY;
+    }
+    return CF_OK;
+}
+
+cf_status cf_matrix_create_csr(cf_context *ctx, int32_t n, int64_t nnz, const int32_t *row_offsets,
+                               const int32_t *cols, const double *vals, int32_t memory, cf_matrix **out)
+{
+    if (!ctx || !out || !row_offsets || (nnz > 0 && (!cols || !vals))) return CF_BAD_INPUT;
+    *out = nullptr;
+    cf::Matrix *m = nullptr;
+    cf_status st = guarded(ctx, [&] {
+        cf::require(memory == CF_MEM_HOST || memory == CF_MEM_DEVICE, CF_BAD_INPUT, "bad memory kind");
+        cf::require(n > 0 && nnz >= 0 && nnz < INT32_MAX, CF_BAD_INPUT, "bad CSR size");
+        cf::Context *c = ctx->impl;
+        if (memory == CF_MEM_HOST) {
+            cf::DeviceBuffer dro, dcol, dval;
+            dro.ensure(sizeof(int32_t) * ((size_t)n + 1));
+            dcol.ensure(sizeof(int32_t) * ((size_t)nnz + 1));
+            dval.ensure(sizeof(double) * ((size_t)nnz + 1));
+            cf::upload(c, dro.ptr, row_offsets, sizeof(int32_t) * ((size_t)n + 1), CF_MEM_HOST);
+            if (nnz > 0) {
+                cf::upload(c, dcol.ptr, cols, sizeof(int32_t) * (size_t)nnz, CF_MEM_HOST);
+                cf::upload(c, dval.ptr, vals, sizeof(double) * (size_t)nnz, CF_MEM_HOST);
+            }
+            m = cf::matrix_from_csr(c, n, nnz, dro.as<int32_t>(), dcol.as<int32_t>(), dval.as<double>());
+            CF_CUDA(cudaStreamSynchronize(c->stream));
+        } else {
+            m = cf::matrix_from_csr(c, n, nnz, row_offsets, cols, vals);
+            CF_CUDA(cudaStreamSynchronize(c->stream));
+        }
     });
     if (st != CF_OK) return st;
     *out = new (std::nothrow) cf_matrix{m, ctx};
@@ -384,6 +509,14 @@ cf_status cf_ldu2csr(cf_context *ctx, const cf_ldu_view *ldu, int32_t *row_offse
 {
     if (!ctx || !ldu || !row_offsets || !cols || !vals) return CF_BAD_INPUT;
     return guarded(ctx, [&] { cf::ldu2csr_into(ctx->impl, *ldu, row_offsets, cols, vals, memory); });
+}
+
+cf_status cf_spmv_async(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t row_order)
+{
+    if (!m || !x || !y) return CF_BAD_INPUT;
+    return guarded(m->owner, [&] {
+        cf::spmv(m->impl, transpose != 0, x, y, row_order == CF_REDUCE_REFERENCE);
+    });
 }
 
 cf_status cf_spmv(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t memory,

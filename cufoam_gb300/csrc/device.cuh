@@ -66,6 +66,37 @@ __device__ __forceinline__ void block_tree(T (&v)[NV], T *sm)
     }
 }
 
+// The fast reduction order's block stage: the shuffle tree below
+// (CF_FAST_BLOCK_SUM 1) or the reference's tree (0).
+#ifndef CF_FAST_BLOCK_SUM
+#define CF_FAST_BLOCK_SUM 1
+#endif
+
+// Fast-order block sum (result valid in thread 0): an xor-shuffle tree in
+// every warp, the eight warp sums through shared memory, and a shuffle tree
+// over them in warp 0 -- one block barrier instead of three.
+template <int NV, class T>
+__device__ __forceinline__ void block_sum_fast(T (&v)[NV], T *sm)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v[i] = v[i] + __shfl_xor_sync(kFull, v[i], o);
+        if (lane == 0) sm[i * kWarps + warp] = v[i];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            T x = lane < kWarps ? sm[i * kWarps + lane] : T(0);
+#pragma unroll
+            for (int o = kWarps / 2; o; o >>= 1) x = x + __shfl_xor_sync(kFull, x, o);
+            v[i] = x;
+        }
+    }
+}
+
 // Single-pass grid reduction.  Every block publishes its NV partials; the
 // block that arrives last sums them in a fixed order (sequentially in block
 // order for the reference order, else a strided sum + block tree), so the
@@ -79,7 +110,11 @@ __device__ __forceinline__ bool grid_reduce(T (&acc)[NV], T *partials, int strid
     __shared__ T sm[NV * kBlock];
     __shared__ bool s_last;
     pdl_trigger();
-    block_tree<NV, T>(acc, sm);
+#if CF_FAST_BLOCK_SUM
+    if (!ref_order) block_sum_fast<NV, T>(acc, sm);
+    else
+#endif
+        block_tree<NV, T>(acc, sm);
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int i = 0; i < NV; ++i) partials[i * stride + blockIdx.x] = acc[i];
@@ -109,7 +144,11 @@ __device__ __forceinline__ bool grid_reduce(T (&acc)[NV], T *partials, int strid
             v[i] = s;
         }
         __syncthreads();
+#if CF_FAST_BLOCK_SUM
+        block_sum_fast<NV, T>(v, sm);
+#else
         block_tree<NV, T>(v, sm);
+#endif
         if (threadIdx.x == 0) {
 #pragma unroll
             for (int i = 0; i < NV; ++i) out[i] = v[i];

@@ -162,6 +162,7 @@ struct GraphEntry {
 struct Context {
     int device = 0;
     cudaStream_t stream = nullptr;
+    bool own_stream = false;   // created (and destroyed) by the library
     int sm_count = 0;
     int max_threads_sm = 0;
     int ref_grid = 0;          // the reference's LaunchConfig grid on this GPU
@@ -248,6 +249,18 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
 int64_t batch_rows(const Batch *B);
 int batch_systems(const Batch *B);
 int64_t batch_offset(const Batch *B, int s);
+
+// host CSR / vector files (formats.cpp)
+struct HostCsr {
+    int rows = 0, cols = 0;
+    std::vector<int32_t> row_offsets, cols_idx;
+    std::vector<double> values;
+};
+void read_csr_file(const std::string &path, HostCsr &out);
+void save_csr_file(const std::string &path, int rows, int cols, int64_t nnz, const int32_t *ro,
+                   const int32_t *col, const double *val);
+void read_vector_file(const std::string &path, std::vector<double> &out);
+void save_vector_file(const std::string &path, int size, const double *v);
 
 void adjoint_gradients(Matrix *m, const double *lam, const double *x, double *d_diag,
                        double *d_lower, double *d_upper);

@@ -560,6 +560,7 @@ void matrix_update_values(Matrix *m, const double *diag, const double *lower, co
                           int memory)
 {
     Context *ctx = m->ctx;
+    require(!m->from_csr, CF_UNSUPPORTED, "the matrix was created from CSR arrays (no LDU coefficients)");
     require(diag && (m->nf == 0 || (lower && upper)), CF_BAD_INPUT, "null coefficient array");
     upload(ctx, m->diag.ptr, diag, sizeof(double) * m->n, memory);
     upload(ctx, m->lower.ptr, lower, sizeof(double) * m->nf, memory);

@@ -15,6 +15,10 @@
 #include <climits>
 #include <cmath>
 
+#ifndef CF_MX_MIN_BLOCKS
+#define CF_MX_MIN_BLOCKS CF_SPMV_MIN_BLOCKS
+#endif
+
 namespace cf {
 
 // ---------------------------------------------------------------------------
@@ -32,7 +36,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_correct(const SolveArgs *__restri
 
 // r = b - A x, ||r|| (FP64); records the outer step.
 template <int FMT>
-__global__ void __launch_bounds__(kBlock) k_mx_residual(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_residual(const SolveArgs *__restrict__ a)
 {
     const double *x = a->x, *b = a->b;
     double *r = a->r[0];
@@ -102,7 +106,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_setup(const SolveArgs *__restrict
 
 // CG: K1 p = r + beta p_old (on the fly), q = A32 p, (p, q); deferred d update
 template <int FMT>
-__global__ void __launch_bounds__(kBlock) k_mx_cg_spmv(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_cg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     CF_EXIT_IF_DONE(a, st, false);
@@ -170,7 +174,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_flush(const SolveArgs *__restrict
 
 // BiCG: q = A32 p and q* = A32^T p* over the shared pattern
 template <int FMT>
-__global__ void __launch_bounds__(kBlock) k_mx_bicg_spmv(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS - 1) k_mx_bicg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     CF_EXIT_IF_DONE(a, st, false);
@@ -255,45 +259,50 @@ __global__ void __launch_bounds__(kBlock) k_mx_bicg_update(const SolveArgs *__re
     }
 }
 
-// MR: K1 y = A32 r, (r, y), (y, y); K2 d += w r, r -= w y
+// MR, one kernel per step.  Kernel k finishes step k-1 and starts step k:
+//   r_{k-1} = r_{k-2} - w y_{k-2},  d += w r_{k-2},  ||r_{k-1}||  (own rows)
+//   y_{k-1} = A r_{k-1} with r_{k-1} formed on the fly for every gathered
+//   column (FP32 FMAs are cheap), (r_{k-1}, y_{k-1}), (y_{k-1}, y_{k-1}).
+// The first kernel of an inner solve only forms y_0 = A r_0.  r and y are
+// double-buffered by step parity (r: fr / frs, y: fq / fqs); x_pending
+// marks that y_{k-2} and w exist.
 template <int FMT>
-__global__ void __launch_bounds__(kBlock) k_mx_mr_spmv(const SolveArgs *__restrict__ a)
-{
-    DevState *st = a->st_in;
-    CF_EXIT_IF_DONE(a, st, false);
-    const float *r = a->fr;
-    float *y = a->fq;
-    float acc[2] = {0.f, 0.f};
-    for_rows<FMT, float>(a, a->val32, a->s_val32, [&](int c) { return r[c]; }, [&](int row, float v) {
-        y[row] = v;
-        acc[0] = fma_t(r[row], v, acc[0]);
-        acc[1] = fma_t(v, v, acc[1]);
-    });
-    float tot[2];
-    if (grid_reduce<2, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
-                              tot) && threadIdx.x == 0)
-        st->omega = tot[0] / tot[1];
-}
-
-__global__ void __launch_bounds__(kBlock) k_mx_mr_update(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_mr_step(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     CF_EXIT_IF_DONE(a, st, true);
-    const int n = a->n;
-    const float w = (float)ld_cg(&st->omega);
-    float *r = a->fr, *d = a->fx;
-    const float *y = a->fq;
-    float acc[1] = {0.f};
-    CF_FOR_ELEMS(i, n) {
-        d[i] = fma_t(w, r[i], d[i]);
-        const float ri = fma_t(-w, y[i], r[i]);
-        r[i] = ri;
-        acc[0] = fma_t(ri, ri, acc[0]);
+    const bool first = ld_cg(&st->x_pending) == 0;
+    const int cur = ld_cg(&st->k) & 1;
+    const float w = first ? 0.f : (float)ld_cg(&st->omega);
+    float *rb[2] = {a->fr, a->frs}, *yb[2] = {a->fq, a->fqs};
+    const float *rin = rb[cur], *yin = yb[cur];
+    float *rout = first ? rb[cur] : rb[cur ^ 1];
+    float *yout = first ? yb[cur] : yb[cur ^ 1];
+    float *d = a->fx;
+    auto g = [&](int c) { return first ? rin[c] : fma_t(-w, yin[c], rin[c]); };
+    float acc[3] = {0.f, 0.f, 0.f};
+    for_rows<FMT, float>(a, a->val32, a->s_val32, g, [&](int row, float v) {
+        const float ri = g(row);
+        if (!first) {
+            rout[row] = ri;
+            d[row] = fma_t(w, rin[row], d[row]);
+        }
+        yout[row] = v;
+        acc[0] = fma_t(ri, v, acc[0]);
+        acc[1] = fma_t(v, v, acc[1]);
+        acc[2] = fma_t(ri, ri, acc[2]);
+    });
+    float tot[3];
+    if (grid_reduce<3, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
+                              tot) && threadIdx.x == 0) {
+        st->omega = tot[0] / tot[1];
+        if (first) {
+            st->x_pending = 1;
+            set_loop_condition(a, true);
+        } else {
+            finish_step(a, st, sqrtf(tot[2]));
+        }
     }
-    float tot[1];
-    if (grid_reduce<1, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_B], false,
-                              tot) && threadIdx.x == 0)
-        finish_step(a, st, sqrtf(tot[0]));
 }
 
 // ---------------------------------------------------------------------------
@@ -307,7 +316,7 @@ static Kernels inner_kernels_t(int solver)
     switch (solver) {
     case CF_CG: k.k1 = (const void *)k_mx_cg_spmv<FMT>; k.k2 = (const void *)k_mx_cg_update; break;
     case CF_BICG: k.k1 = (const void *)k_mx_bicg_spmv<FMT>; k.k2 = (const void *)k_mx_bicg_update; break;
-    case CF_MR: k.k1 = (const void *)k_mx_mr_spmv<FMT>; k.k2 = (const void *)k_mx_mr_update; break;
+    case CF_MR: k.k1 = (const void *)k_mx_mr_step<FMT>; break;
     default: break;
     }
     k.k1_spmv = FMT == kCsr;   // the SELL passes stage nothing
@@ -386,6 +395,15 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
     const int64_t max_total = c.max_iter <= 0 ? INT_MAX : c.max_iter;
     const int max_outer = c.mixed_max_outer > 0 ? c.mixed_max_outer : 50;
     const double eta = (c.mixed_inner_rtol > 0 && c.mixed_inner_rtol < 1) ? c.mixed_inner_rtol : 1e-4;
+    // BiCG's residual is not monotone, so its FP32 sweeps are kept short;
+    // CG and MR sweeps run to the inner tolerance
+    int inner_cap = c.mixed_inner_max > 0 ? c.mixed_inner_max : (solver == CF_BICG ? 400 : INT_MAX);
+    // x and r before each correction, to undo a sweep that made things worse
+    // (workspace vectors 12 and 13: unused by the mixed path otherwise)
+    const size_t vb = sizeof(double) * (size_t)m->n;
+    ctx->vec[12].ensure(vb);
+    ctx->vec[13].ensure(vb);
+    double *x_keep = ctx->vec[12].as<double>(), *r_keep = ctx->vec[13].as<double>();
     double prev_norm = ctx->h_state->norm;
     int64_t total = 0;
     int outer = 0;
@@ -393,8 +411,10 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
     DevState &SI = *ctx->h_state_in;
     while (!ctx->h_state->done && outer < max_outer && total < max_total) {
         SI = DevState{};
-        SI.tolerance = eta;
-        SI.max_steps = (int)std::min<int64_t>(max_total - total, INT_MAX);
+        // the last sweep only has to reach the FP64 target (with a margin
+        // for the FP32 / FP64 residual gap), not eta below it
+        SI.tolerance = std::max(eta, std::min(0.5, 0.5 * ctx->h_state->tol / prev_norm));
+        SI.max_steps = (int)std::min<int64_t>(std::min<int64_t>(max_total - total, (int64_t)inner_cap), INT_MAX);
         SI.int_bound = c.bicg_int_bound;
         SI.hist_cap = 0;
         CF_CUDA(cudaMemcpyAsync(A.st_in, &SI, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
@@ -415,6 +435,8 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
         if (solver != CF_MR)
             launch(ctx, ctx->stream, (const void *)k_mx_flush,
                    launch_cfg(ctx, (const void *)k_mx_flush, false, cap, false), args1);
+        CF_CUDA(cudaMemcpyAsync(x_keep, A.x, vb, cudaMemcpyDeviceToDevice, ctx->stream));
+        CF_CUDA(cudaMemcpyAsync(r_keep, A.r[0], vb, cudaMemcpyDeviceToDevice, ctx->stream));
         launch(ctx, ctx->stream, (const void *)k_mx_correct,
                launch_cfg(ctx, (const void *)k_mx_correct, false, cap, false), args1);
         launch(ctx, ctx->stream, k_residual, launch_cfg(ctx, k_residual, !sell, cap, false), args1);
@@ -424,13 +446,30 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
         total += SI.k;
         ++outer;
         const double nrm = ctx->h_state->norm;
-        if (ctx->h_state->done) {
-            status = ctx->h_state->status;
+        if (ctx->h_state->done && ctx->h_state->status == CF_OK) {
+            status = CF_OK;
             break;
         }
-        if (SI.status == CF_NONFINITE || !(nrm < prev_norm)) {
-            // the FP32 inner solve stopped making progress on the FP64 residual
-            status = (SI.status == CF_NONFINITE) ? CF_NONFINITE : CF_NOT_CONVERGED;
+        if (!(nrm < prev_norm)) {
+            // The FP32 sweep raised the FP64 residual (a non-finite inner
+            // solve included): undo it and retry with a shorter sweep.
+            CF_CUDA(cudaMemcpyAsync(A.x, x_keep, vb, cudaMemcpyDeviceToDevice, ctx->stream));
+            CF_CUDA(cudaMemcpyAsync(A.r[0], r_keep, vb, cudaMemcpyDeviceToDevice, ctx->stream));
+            DevState &S = *ctx->h_state;
+            S.norm = prev_norm;
+            S.done = 0;
+            S.status = CF_NOT_CONVERGED;
+            CF_CUDA(cudaMemcpyAsync(A.st, &S, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
+            CF_CUDA(cudaStreamSynchronize(ctx->stream));
+            inner_cap /= 2;
+            if (inner_cap < 8) {
+                status = CF_NOT_CONVERGED;
+                break;
+            }
+            continue;
+        }
+        if (ctx->h_state->done) {
+            status = ctx->h_state->status;
             break;
         }
         if (SI.status == CF_BREAKDOWN && SI.k == 0) {

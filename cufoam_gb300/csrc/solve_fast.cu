@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(kBlock) k_f_cg_prep(const SolveArgs *__restric
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(kBlock) k_f_cg_spmv(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_cg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, false);
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(kBlock) k_f_bicg_prep(const SolveArgs *__restr
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(kBlock) k_f_bicg_spmv(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS - 1) k_f_bicg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, false);
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kBlock) k_f_jac_prep(const SolveArgs *__restri
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(kBlock) k_f_jac_spmv(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_jac_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, true);
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(kBlock) k_f_rich_prep(const SolveArgs *__restr
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(kBlock) k_f_rich_spmv(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_rich_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, true);
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(kBlock) k_f_mr_prep(const SolveArgs *__restric
 }
 
 template <int KIND, int FMT>
-__global__ void __launch_bounds__(kBlock) k_f_mr_spmv(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_mr_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, false);

@@ -23,16 +23,31 @@ namespace cf {
 // ---------------------------------------------------------------------------
 enum { kCsr = 0, kSell = 1 };
 
-// SELL passes take two entries per thread per batch: 48 registers, five
-// 256-thread blocks per SM (measured on the 7-point 128^3 system: within a
-// few percent of the best batch / occupancy pairing, with no spills).
-constexpr int kSellBatch = 2;
+// SELL passes take CF_SELL_BATCH entries per thread per batch: all their
+// loads and gathers are issued before the first FMA.  With five resident
+// blocks per SM (48 registers) four measured best on the 7-point 128^3 CG
+// step: SpMV 49.8 us in the solve, against 52-68 us for batches of 2 or 8
+// and for 3, 4 or 6 blocks per SM.
+#ifndef CF_SELL_BATCH
+#define CF_SELL_BATCH 4
+#endif
+// Resident blocks per SM the SpMV passes ask nvcc for (it sizes their
+// register budget from it); the two-value BiCG passes ask for one fewer.
+#ifndef CF_SPMV_MIN_BLOCKS
+#define CF_SPMV_MIN_BLOCKS 5
+#endif
+constexpr int kSellBatch = CF_SELL_BATCH;
+// the same for the FP32 passes of the mixed-precision inner solves
+#ifndef CF_SELL_BATCH32
+#define CF_SELL_BATCH32 4
+#endif
+constexpr int kSellBatch32 = CF_SELL_BATCH32;
 
 template <int FMT, class V, class G, class F>
 __device__ __forceinline__ void for_rows(const SolveArgs *a, const V *val, const V *sval, G g, F f)
 {
     if constexpr (FMT == kSell) {
-        sell_rows<V, kSellBatch>(a->n, a->n_slices, a->s_off, a->s_col, sval, g, f);
+        sell_rows<V, sizeof(V) == 4 ? kSellBatch32 : kSellBatch>(a->n, a->n_slices, a->s_off, a->s_col, sval, g, f);
     } else {
         const int n = a->n, cap = a->stage_cap;
         CF_STAGE(V, cap);

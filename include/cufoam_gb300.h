@@ -124,7 +124,11 @@ typedef struct cf_controls {
     int32_t history_time;    /* 1: history holds seconds since the initial residual
                                 at the end of each step (device clock), the
                                 reference's DetailType::Time, instead of ||r||_2 */
-    int32_t reserved[4];
+    int32_t mixed_inner_max; /* mixed: FP32 steps per refinement sweep; 0 = 400
+                                for BiCG, no limit for CG and MR.  A sweep that
+                                raises the FP64 residual is undone and retried
+                                with half as many steps. */
+    int32_t reserved[3];
 } cf_controls;
 
 /* solverPerformance plus diagnostics. */
@@ -171,11 +175,21 @@ void cf_controls_init(cf_controls *c);
 
 cf_status cf_context_create(int32_t device, cf_context **out);
 void cf_context_destroy(cf_context *ctx);
+/* Orders the context's work on `cuda_stream` (a cudaStream_t the caller
+ * keeps alive; cudaStreamLegacy and cudaStreamPerThread are accepted), or on
+ * a private non-blocking stream of the library when it is NULL. */
 cf_status cf_context_set_stream(cf_context *ctx, void *cuda_stream);
 const char *cf_context_last_error(const cf_context *ctx);
 cf_status cf_device_query(cf_context *ctx, cf_device_info *out);
 
 /* ---- matrices ---------------------------------------------------------- */
+/* A matrix given as a square CSR matrix (host or device arrays; copied).
+ * The diagonal is found as the reference's FindDiag does
+ * (gis/SparseSystem/kernels.h:447-464).  The transpose solve and BiCG need
+ * a structurally symmetric pattern.  Replaces the SingleGPU::SparseCSR
+ * upload of a CPU::SparseCSR (gis/SparseSystem/SparseSingleGPU.h:51-80). */
+cf_status cf_matrix_create_csr(cf_context *ctx, int32_t n, int64_t nnz, const int32_t *row_offsets,
+                               const int32_t *cols, const double *vals, int32_t memory, cf_matrix **out);
 /* Uploads an LDU matrix and converts it on the device to the reference's
  * CSR (replaces getSparseCSRMat, gis/ldu2csr.h:7-40, plus the
  * SingleGPU::SparseCSR upload, gis/SparseSystem/SparseSingleGPU.h:51-80). */
@@ -214,6 +228,10 @@ cf_status cf_ldu2csr(cf_context *ctx, const cf_ldu_view *ldu, int32_t *row_offse
  * sums it as one FMA chain. */
 cf_status cf_spmv(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t memory,
                   int32_t row_order);
+/* The same on device pointers, enqueued on the context's stream without
+ * waiting for it (for callers that chain their own kernels or time the
+ * SpMV with events).  No reference counterpart (SpMv is internal to libGIS). */
+cf_status cf_spmv_async(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t row_order);
 /* normFactor(source, psi) (gis/gis.cu:106-123 for CF_NORM_REFERENCE_L2). */
 cf_status cf_norm_factor(cf_matrix *m, const double *source, const double *psi,
                          int32_t memory, int32_t norm_type, int32_t reduction, double *out);
@@ -260,6 +278,25 @@ cf_status cf_adjoint_gradients(cf_matrix *m, const double *lambda, const double 
 cf_status cf_norm_factor_noalloc(int32_t n_rows, const int32_t *row_offsets, const int32_t *cols,
                                  const double *vals, const double *source, const double *psi,
                                  int32_t reduction, double *norm_factor, void *cuda_stream);
+
+/* ---- files (host only; no context) --------------------------------------
+ * The reference's formats (gis/SparseSystem/SparseCPU.h): a name ending in
+ * ".rb" is a Rutherford-Boeing matrix (real / integer, assembled;
+ * unsymmetric, symmetric or skew; :149-297), anything else the binary CSR
+ * file of CPU::SparseCSR::load/save (:105-147: int32 rows, cols, nnz; f64
+ * values; int32 row offsets without the last; int32 columns).  Vectors: a
+ * name ending in ".mtx" is a Matrix Market array (:661-678), anything else
+ * the binary file of CPU::Vector::load/save (int32 size, f64 values).
+ * _info gives the sizes, _read fills caller arrays of those sizes. */
+cf_status cf_csr_file_info(const char *path, int32_t *rows, int32_t *cols, int64_t *nnz);
+cf_status cf_csr_file_read(const char *path, int32_t *row_offsets, int32_t *cols, double *vals);
+cf_status cf_csr_file_save(const char *path, int32_t rows, int32_t cols, int64_t nnz,
+                           const int32_t *row_offsets, const int32_t *cols_idx, const double *vals);
+cf_status cf_vector_file_info(const char *path, int32_t *size);
+cf_status cf_vector_file_read(const char *path, double *values);
+cf_status cf_vector_file_save(const char *path, int32_t size, const double *values);
+/* The message of the last failed file call of this thread. */
+const char *cf_file_last_error(void);
 
 /* ---- batched solves ---------------------------------------------------- */
 /* Many independent LDU systems, each with n_rhs right-hand sides sharing its

@@ -3,6 +3,9 @@
 * ``oracle/_build/liboracle.so`` -- the plain-C restatement (oracle.c),
   compiled with ``-ffp-contract=off`` so it gives the same bits on x86 and
   Arm, with OpenMP for the timed CPU baseline.
+* ``oracle/_ref/libref_formats.so`` -- the reference's own matrix / vector
+  file readers and writers (``gis/SparseSystem/SparseCPU.h``), compiled the
+  same way, for the file-format golden fixtures.
 * ``oracle/_ref/libref_ldu2csr.so`` -- the reference's own
   ``gis/ldu2csr.h`` compiled from its source file against the
   ``refstub/lduMatrix.H`` stand-in.  Built only where the reference sources
@@ -18,6 +21,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "liboracle.so")
 REF_LDU2CSR_SO = os.path.join(REF_DIR, "libref_ldu2csr.so")
+REF_FORMATS_SO = os.path.join(REF_DIR, "libref_formats.so")
 REFERENCE_ROOT = os.environ.get("CUFOAM_REFERENCE_ROOT", "/root/reference")
 
 
@@ -58,9 +62,26 @@ def build_ref_ldu2csr(force: bool = False) -> str | None:
     return REF_LDU2CSR_SO
 
 
+def build_ref_formats(force: bool = False) -> str | None:
+    """Compile the reference's file readers / writers
+    (gis/SparseSystem/SparseCPU.h), if the reference sources exist."""
+    gis = os.path.join(REFERENCE_ROOT, "gis")
+    hdr = os.path.join(gis, "SparseSystem", "SparseCPU.h")
+    if not os.path.exists(hdr):
+        return REF_FORMATS_SO if os.path.exists(REF_FORMATS_SO) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    drv = os.path.join(HERE, "refstub", "ref_formats.cpp")
+    if force or _stale(REF_FORMATS_SO, [drv, hdr]):
+        tmp = REF_FORMATS_SO + f".tmp{os.getpid()}"
+        subprocess.check_call(["g++", "-O2", "-std=c++14", "-fPIC", "-shared", "-I" + gis, drv, "-o", tmp])
+        os.replace(tmp, REF_FORMATS_SO)
+    return REF_FORMATS_SO
+
+
 def build_all(force: bool = False) -> None:
     build_oracle(force)
     build_ref_ldu2csr(force)
+    build_ref_formats(force)
 
 
 if __name__ == "__main__":

@@ -70,3 +70,26 @@ def test_autotuner_picks_and_caches(ctx, tmp_path, monkeypatch):
     B2 = BatchSolver(systems, n_rhs=3, context=ctx)
     cfg2, _ = B2.tune(rhs, tolerance=1e-8, max_iter=2000, candidates=cands)
     assert cfg2 == cfg  # served from the cache
+
+
+@pytest.mark.parametrize("config", [(1, 256, 0), (4, 256, 0), (8, 128, 0)])
+def test_batched_mixed_precision_reaches_fp64_tolerance(ctx, config):
+    """FP32 CG sweeps inside FP64 refinement: every (system, rhs) reaches the
+    FP64 tolerance on its true residual, and the answer agrees with the FP64
+    batched answer to the accuracy the tolerance allows."""
+    systems, rhs = _small_batch()
+    tol, maxit = 1e-10, 20000
+    B = BatchSolver(systems, n_rhs=3, context=ctx)
+    x64, r64, _ = B.solve(rhs, tolerance=tol, max_iter=maxit, config=config)
+    x32, r32, _ = B.solve(rhs, tolerance=tol, max_iter=maxit, config=config, precision="mixed")
+    xs64, xs32 = B.unpack(x64), B.unpack(x32)
+    for s, L in enumerate(systems):
+        A = O.ldu2csr(L)
+        for j in range(3):
+            res = r32[s * 3 + j]
+            assert res["status"] == 0 and res["final_residual"] <= tol, (s, j, res)
+            assert res["norm_factor"] == r64[s * 3 + j]["norm_factor"]
+            true_rel = O.true_residual_norm(A, rhs[s][j], xs32[s][j]) / res["norm_factor"]
+            assert true_rel <= 1.5 * tol
+            err = np.linalg.norm(xs32[s][j] - xs64[s][j]) / np.linalg.norm(xs64[s][j])
+            assert err < 1e-6, (s, j, err)

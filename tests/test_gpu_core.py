@@ -8,6 +8,7 @@ import pytest
 
 import cufoam_gb300 as cf
 import oracle as O
+from conftest import fast_order_iteration_slack
 
 pytestmark = pytest.mark.gpu
 
@@ -232,7 +233,7 @@ def test_solver_fast_order_parity(ctx, name, case, fmt):
     psi = np.zeros(L.n)
     perf = cf._TABLE["cuFoam" + name]("p", M, {"tolerance": tol, "maxIter": maxit}).solve(
         psi, b, history=maxit + 1)
-    assert abs(perf.n_iterations - want.n_iterations) <= 1
+    assert abs(perf.n_iterations - want.n_iterations) <= fast_order_iteration_slack(want.n_iterations)
     assert abs(perf.norm_factor - want.norm_factor) <= 1e-14 * want.norm_factor
     h0 = want.history[0]
     early = min(10, len(want.history), len(perf.history))
@@ -321,3 +322,21 @@ def test_repeated_solves_reuse_workspace(ctx):
         res[-1].psi = psi
     assert all(r.n_iterations == res[0].n_iterations for r in res)
     assert all(r.psi.tobytes() == res[0].psi.tobytes() for r in res)
+
+
+def test_spmv_async_into_device_buffer(ctx):
+    import torch
+    L = O.grid_lognormal(20, 17, 9, 3)
+    M = _matrix(ctx, L)
+    x = O.uniform(7, L.n)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.full_like(xd, float("nan"))
+    out = M.spmv(xd, row_order="fast", out=yd)
+    torch.cuda.synchronize()
+    assert out is yd
+    assert np.array_equal(yd.cpu().numpy(), M.spmv(x, row_order="fast"))
+    M.spmv(xd, transpose=True, row_order="reference", out=yd)
+    torch.cuda.synchronize()
+    assert yd.cpu().numpy().tobytes() == O.ref_spmv(O.ldu2csr(L.transposed()), x).tobytes()
+    with pytest.raises(ValueError):
+        M.spmv(x, out=yd)

@@ -9,6 +9,7 @@ import pytest
 
 import oracle as O
 from cufoam_gb300.compat import GisError, GisHarness
+from conftest import fast_order_iteration_slack
 
 pytestmark = pytest.mark.gpu
 
@@ -58,7 +59,7 @@ def test_gis_solver_fast_order(gis, name):
     want = O.solve(KIND[name], A, b, x0, error, 5000, At=At)
     x, det, _ = gis.solve(name, A.row_offsets, A.cols, A.vals, b, x0, error, 5000,
                           p_real=1e-10 if name.startswith("BiCG") else 0.0)
-    assert abs((len(det) - 1) - want.n_iterations) <= 1
+    assert abs((len(det) - 1) - want.n_iterations) <= fast_order_iteration_slack(want.n_iterations)
     assert det[0] == pytest.approx(want.history[0], rel=1e-13)
     assert det[-1] <= error
     if name == "JMR":   # JMR stops on the D^-1/2-scaled residual

@@ -245,3 +245,36 @@ def test_max_iter_cap_and_loop_semantics():
         assert r.n_iterations == 0
     r = O.plugin_solve(O.BICG, L, b, x, 1e-3, 7)
     assert r.n_iterations == 1
+
+
+def test_fp32_bicg_diverges_on_upwind_convection_diffusion():
+    """Why the mixed-precision BiCG cannot meet the FP64 tolerance on the
+    convection-diffusion workload: BiCG's residual grows transiently on this
+    non-normal system before it converges; in FP64 it recovers, with FP32
+    vectors and accumulation it stalls far above the FP64 level (numpy,
+    48^3, cell Peclet 10; at 64^3 and above FP32 BiCG diverges outright)."""
+    import scipy.sparse as sp
+    L, _ = O.grid_convdiff(48, 48, 48, 7, 10.0)
+    A = O.ldu2csr(L)
+    M = sp.csr_matrix((A.vals, A.cols, A.row_offsets), shape=(L.n, L.n))
+    b = O.uniform(8, L.n)
+
+    def bicg(dt, iters):
+        Ms, Mt = M.astype(dt), M.T.tocsr().astype(dt)
+        x = np.zeros(L.n, dt)
+        r = b.astype(dt)
+        rs, p, ps = r.copy(), r.copy(), r.copy()
+        rho = np.dot(r, rs)
+        for _ in range(iters):
+            q, qs = Ms @ p, Mt @ ps
+            xi = rho / np.dot(ps, q)
+            x += xi * p
+            r -= xi * q
+            rs -= xi * qs
+            rho, rho1 = np.dot(r, rs), rho
+            p = r + (rho / rho1) * p
+            ps = rs + (rho / rho1) * ps
+        return np.linalg.norm(b - M @ x.astype(np.float64)) / np.linalg.norm(b)
+
+    assert bicg(np.float64, 800) < 1e-8
+    assert bicg(np.float32, 800) > 1e-5
