@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(BT) k_batch_cg(const BatchArgs a)
                     act[j] = active[j];
                     inv[j] = active[j] ? (float)(1.0 / nrm[j]) : 0.f;
                     // the last sweep only has to reach the FP64 target
-                    eta[j] = (float)fmax(a.inner_rtol, fmin(0.5, 0.5 * tolj[j] / nrm[j]));
+                    eta[j] = (float)fmax(a.inner_rtol, fmin(0.5, 0.8 * tolj[j] / nrm[j]));
                     any_in = any_in || act[j];
                 }
                 double acc0[R];

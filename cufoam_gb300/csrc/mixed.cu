@@ -15,8 +15,11 @@
 #include <climits>
 #include <cmath>
 
+// Resident blocks per SM the FP32 SpMV passes ask for (five measured best
+// for the 256^3 MR inner solve: 276 us per step against 309 us with four
+// and 290 us with six).
 #ifndef CF_MX_MIN_BLOCKS
-#define CF_MX_MIN_BLOCKS CF_SPMV_MIN_BLOCKS
+#define CF_MX_MIN_BLOCKS 5
 #endif
 
 namespace cf {
@@ -36,7 +39,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_correct(const SolveArgs *__restri
 
 // r = b - A x, ||r|| (FP64); records the outer step.
 template <int FMT>
-__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_residual(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_mx_residual(const SolveArgs *__restrict__ a)
 {
     const double *x = a->x, *b = a->b;
     double *r = a->r[0];
@@ -259,50 +262,69 @@ __global__ void __launch_bounds__(kBlock) k_mx_bicg_update(const SolveArgs *__re
     }
 }
 
-// MR, one kernel per step.  Kernel k finishes step k-1 and starts step k:
-//   r_{k-1} = r_{k-2} - w y_{k-2},  d += w r_{k-2},  ||r_{k-1}||  (own rows)
-//   y_{k-1} = A r_{k-1} with r_{k-1} formed on the fly for every gathered
-//   column (FP32 FMAs are cheap), (r_{k-1}, y_{k-1}), (y_{k-1}, y_{k-1}).
-// The first kernel of an inner solve only forms y_0 = A r_0.  r and y are
-// double-buffered by step parity (r: fr / frs, y: fq / fqs); x_pending
-// marks that y_{k-2} and w exist.
+// MR: K1 y = A32 r, (r, y), (y, y); K2 d += w r, r -= w y, ||r||.  (A
+// single kernel that forms r - w y on the fly for every gathered column
+// measured slower at 256^3: two gathers per entry cost more than the
+// separate element-wise pass.)
 template <int FMT>
-__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_mr_step(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_mr_spmv(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st_in;
+    CF_EXIT_IF_DONE(a, st, false);
+    const float *__restrict__ r = a->fr;
+    float *__restrict__ y = a->fq;
+    float acc[2] = {0.f, 0.f};
+    for_rows<FMT, float>(a, a->val32, a->s_val32, [&](int c) { return r[c]; }, [&](int row, float v) {
+        y[row] = v;
+        acc[0] = fma_t(r[row], v, acc[0]);
+        acc[1] = fma_t(v, v, acc[1]);
+    });
+    float tot[2];
+    if (grid_reduce<2, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
+                              tot) && threadIdx.x == 0)
+        st->omega = tot[0] / tot[1];
+}
+
+// four consecutive elements per thread and step (16-byte loads)
+__global__ void __launch_bounds__(kBlock) k_mx_mr_update(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     CF_EXIT_IF_DONE(a, st, true);
-    const bool first = ld_cg(&st->x_pending) == 0;
-    const int cur = ld_cg(&st->k) & 1;
-    const float w = first ? 0.f : (float)ld_cg(&st->omega);
-    float *rb[2] = {a->fr, a->frs}, *yb[2] = {a->fq, a->fqs};
-    const float *rin = rb[cur], *yin = yb[cur];
-    float *rout = first ? rb[cur] : rb[cur ^ 1];
-    float *yout = first ? yb[cur] : yb[cur ^ 1];
-    float *d = a->fx;
-    auto g = [&](int c) { return first ? rin[c] : fma_t(-w, yin[c], rin[c]); };
-    float acc[3] = {0.f, 0.f, 0.f};
-    for_rows<FMT, float>(a, a->val32, a->s_val32, g, [&](int row, float v) {
-        const float ri = g(row);
-        if (!first) {
-            rout[row] = ri;
-            d[row] = fma_t(w, rin[row], d[row]);
-        }
-        yout[row] = v;
-        acc[0] = fma_t(ri, v, acc[0]);
-        acc[1] = fma_t(v, v, acc[1]);
-        acc[2] = fma_t(ri, ri, acc[2]);
-    });
-    float tot[3];
-    if (grid_reduce<3, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
-                              tot) && threadIdx.x == 0) {
-        st->omega = tot[0] / tot[1];
-        if (first) {
-            st->x_pending = 1;
-            set_loop_condition(a, true);
-        } else {
-            finish_step(a, st, sqrtf(tot[2]));
-        }
+    const int n = a->n;
+    const float w = (float)ld_cg(&st->omega);
+    float *__restrict__ r = a->fr;
+    float *__restrict__ d = a->fx;
+    const float *__restrict__ y = a->fq;
+    float4 *r4 = reinterpret_cast<float4 *>(r);
+    float4 *d4 = reinterpret_cast<float4 *>(d);
+    const float4 *y4 = reinterpret_cast<const float4 *>(y);
+    float acc[1] = {0.f};
+    const int n4 = n >> 2;
+    CF_FOR_ELEMS(i, n4) {
+        const float4 rv = r4[i], dv = d4[i], yv = y4[i];
+        float4 dn, rn;
+        dn.x = fma_t(w, rv.x, dv.x);
+        dn.y = fma_t(w, rv.y, dv.y);
+        dn.z = fma_t(w, rv.z, dv.z);
+        dn.w = fma_t(w, rv.w, dv.w);
+        rn.x = fma_t(-w, yv.x, rv.x);
+        rn.y = fma_t(-w, yv.y, rv.y);
+        rn.z = fma_t(-w, yv.z, rv.z);
+        rn.w = fma_t(-w, yv.w, rv.w);
+        d4[i] = dn;
+        r4[i] = rn;
+        acc[0] = fma_t(rn.x, rn.x, fma_t(rn.y, rn.y, fma_t(rn.z, rn.z, fma_t(rn.w, rn.w, acc[0]))));
     }
+    for (int i = 4 * n4 + blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
+        d[i] = fma_t(w, r[i], d[i]);
+        const float ri = fma_t(-w, y[i], r[i]);
+        r[i] = ri;
+        acc[0] = fma_t(ri, ri, acc[0]);
+    }
+    float tot[1];
+    if (grid_reduce<1, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_B], false,
+                              tot) && threadIdx.x == 0)
+        finish_step(a, st, sqrtf(tot[0]));
 }
 
 // ---------------------------------------------------------------------------
@@ -316,7 +338,7 @@ static Kernels inner_kernels_t(int solver)
     switch (solver) {
     case CF_CG: k.k1 = (const void *)k_mx_cg_spmv<FMT>; k.k2 = (const void *)k_mx_cg_update; break;
     case CF_BICG: k.k1 = (const void *)k_mx_bicg_spmv<FMT>; k.k2 = (const void *)k_mx_bicg_update; break;
-    case CF_MR: k.k1 = (const void *)k_mx_mr_step<FMT>; break;
+    case CF_MR: k.k1 = (const void *)k_mx_mr_spmv<FMT>; k.k2 = (const void *)k_mx_mr_update; break;
     default: break;
     }
     k.k1_spmv = FMT == kCsr;   // the SELL passes stage nothing
@@ -362,6 +384,10 @@ void mixed_prepare(Context *ctx, Matrix *m, int solver, SolveArgs &A)
     A.partials32 = ctx->partials32.as<float>();
     A.st_in = ctx->state_in.as<DevState>();
 }
+
+// Fraction of the remaining FP64 reduction the last refinement sweep aims
+// for (the FP32 recursive residual tracks the FP64 one to ~1e-6 relative).
+constexpr double kLastSweepMargin = 0.8;
 
 // Runs after the FP64 normFactor and initial residual (st holds ||r_0||,
 // tol = tolerance * normFactor).  Returns the total inner iterations.
@@ -413,7 +439,7 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
         SI = DevState{};
         // the last sweep only has to reach the FP64 target (with a margin
         // for the FP32 / FP64 residual gap), not eta below it
-        SI.tolerance = std::max(eta, std::min(0.5, 0.5 * ctx->h_state->tol / prev_norm));
+        SI.tolerance = std::max(eta, std::min(0.5, kLastSweepMargin * ctx->h_state->tol / prev_norm));
         SI.max_steps = (int)std::min<int64_t>(std::min<int64_t>(max_total - total, (int64_t)inner_cap), INT_MAX);
         SI.int_bound = c.bicg_int_bound;
         SI.hist_cap = 0;

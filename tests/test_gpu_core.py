@@ -340,3 +340,4 @@ def test_spmv_async_into_device_buffer(ctx):
     assert yd.cpu().numpy().tobytes() == O.ref_spmv(O.ldu2csr(L.transposed()), x).tobytes()
     with pytest.raises(ValueError):
         M.spmv(x, out=yd)
+
