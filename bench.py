@@ -546,6 +546,25 @@ def run_profile(args):
     return 0
 
 
+def run_profile_mr(args):
+    """A short run for ncu: MR on the 256^3 upwind convection-diffusion
+    system, FP64 and mixed precision, 300 steps each, host-driven launches."""
+    import torch
+
+    import cufoam_gb300 as cf
+    from cufoam_gb300 import workloads as W
+    ctx = cf.Context(0)
+    L, _ = W.grid_convdiff(256, 256, 256, 7, 10.0)
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    src = torch.from_numpy(W.uniform(8, L.n)).cuda()
+    for prec in ("FP64", "mixed"):
+        psi = torch.zeros(L.n, dtype=torch.float64, device="cuda")
+        perf = cf.cuFoamMR("U", M, {"tolerance": 1e-10, "maxIter": 300, "precision": prec,
+                                    "innerMaxIter": 300, "useGraph": 0}).solve(psi, src)
+        print(f"profile run ok: MR {prec} {perf.n_iterations} steps")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -556,7 +575,11 @@ def main():
                     help="skip the mixed-vs-FP64 and batched-vs-sequential comparisons")
     ap.add_argument("--profile", action="store_true",
                     help="short host-driven run for an ncu capture (prints no JSON)")
+    ap.add_argument("--profile-mr", action="store_true",
+                    help="short host-driven MR run (FP64 and mixed, 256^3) for an ncu capture")
     args = ap.parse_args()
+    if args.profile_mr:
+        return run_profile_mr(args)
     if args.profile:
         return run_profile(args)
     if args.impl == "reference":
