@@ -18,11 +18,12 @@ import numpy as np
 
 from . import _capi
 from ._capi import (CF_BICG, CF_CG, CF_JACOBI, CF_JMR, CF_MR, CF_MRJACOBI, CF_MRS,
-                    CF_RICHARDSON, CufoamError)
+                    CF_RICHARDSON, CF_PCG, CufoamError)
 
 __all__ = ["Context", "LduMatrix", "SolverPerformance", "New", "solver_names",
            "cuFoamCG", "cuFoamBiCG", "cuFoamJacobi", "cuFoamMR", "cuFoamMRJacobi",
-           "cuFoamMRS", "cuFoamJMR", "cuFoamRichardson", "CufoamError"]
+           "cuFoamMRS", "cuFoamJMR", "cuFoamRichardson", "cuFoamPCG", "CufoamError", "CsrMatrix",
+           "read_csr", "save_csr", "read_vector", "save_vector"]
 
 
 def _is_torch(a) -> bool:
@@ -491,9 +492,13 @@ cuFoamMRJacobi = _plugin("cuFoamMRJacobi", CF_MRJACOBI)
 cuFoamMRS = _plugin("cuFoamMRS", CF_MRS)
 cuFoamJMR = _plugin("cuFoamJMR", CF_JMR)
 cuFoamRichardson = _plugin("cuFoamRichardson", CF_RICHARDSON, True, False)
+# Jacobi-preconditioned CG: no reference counterpart (the reference's
+# roadmap, README.md:71-73); symmetric matrices, like cuFoamCG
+cuFoamPCG = _plugin("cuFoamPCG", CF_PCG, True, False)
 
 _TABLE = {c.type_name: c for c in (cuFoamCG, cuFoamBiCG, cuFoamJacobi, cuFoamMR,
-                                   cuFoamMRJacobi, cuFoamMRS, cuFoamJMR, cuFoamRichardson)}
+                                   cuFoamMRJacobi, cuFoamMRS, cuFoamJMR, cuFoamRichardson,
+                                   cuFoamPCG)}
 
 
 def solver_names(symmetric: bool = True) -> list[str]:

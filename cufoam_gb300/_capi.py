@@ -13,7 +13,7 @@ from . import build as _build
 
 CF_OK, CF_NOT_CONVERGED, CF_BREAKDOWN, CF_NONFINITE, CF_BAD_INPUT, CF_CUDA_ERROR, \
     CF_TIMEOUT, CF_NO_DEVICE, CF_UNSUPPORTED, CF_OUT_OF_MEMORY = range(10)
-CF_CG, CF_BICG, CF_JACOBI, CF_MR, CF_MRJACOBI, CF_MRS, CF_JMR, CF_RICHARDSON = range(8)
+CF_CG, CF_BICG, CF_JACOBI, CF_MR, CF_MRJACOBI, CF_MRS, CF_JMR, CF_RICHARDSON, CF_PCG = range(9)
 CF_MEM_HOST, CF_MEM_DEVICE = 0, 1
 CF_PREC_FP64, CF_PREC_MIXED = 0, 1
 CF_REDUCE_FAST, CF_REDUCE_REFERENCE = 0, 1

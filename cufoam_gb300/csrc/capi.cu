@@ -280,7 +280,8 @@ cf_status cf_solver_from_name(const char *name, int32_t *solver)
     if (!name || !solver) return CF_BAD_INPUT;
     static const struct { const char *name; int32_t kind; } table[] = {
         {"CG", CF_CG}, {"BiCG", CF_BICG}, {"Jacobi", CF_JACOBI}, {"MR", CF_MR},
-        {"MRJacobi", CF_MRJACOBI}, {"MRS", CF_MRS}, {"JMR", CF_JMR}, {"Richardson", CF_RICHARDSON}};
+        {"MRJacobi", CF_MRJACOBI}, {"MRS", CF_MRS}, {"JMR", CF_JMR}, {"Richardson", CF_RICHARDSON},
+        {"PCG", CF_PCG}};
     const char *s = name;
     if (std::strncmp(s, "cuFoam", 6) == 0) s += 6;
     for (const auto &t : table)

@@ -386,6 +386,32 @@ __global__ void k_sort_rows(int n, const int32_t *__restrict__ ro, int32_t *col,
     }
 }
 
+// one thread per row i: for the k-th occurrence of column j in row i, the
+// value of the k-th occurrence of column i in row j (err = 1 if missing)
+__global__ void k_transpose_on_pattern(int n, const int32_t *__restrict__ ro, const int32_t *__restrict__ col,
+                                       const double *__restrict__ val, double *valT, int *err)
+{
+    CF_FOR_ELEMS(i, n) {
+        for (int e = ro[i]; e < ro[i + 1]; ++e) {
+            const int j = col[e];
+            int k = 0;
+            for (int t = ro[i]; t < e; ++t) k += col[t] == j;
+            int found = -1;
+            for (int t = ro[j]; t < ro[j + 1]; ++t)
+                if (col[t] == i && k-- == 0) {
+                    found = t;
+                    break;
+                }
+            if (found < 0) {
+                atomicOr(err, 1);
+                valT[e] = 0.0;
+            } else {
+                valT[e] = val[found];
+            }
+        }
+    }
+}
+
 __global__ void k_same_pattern(int64_t m, const int32_t *__restrict__ a, const int32_t *__restrict__ b,
                                int *diff)
 {
@@ -767,14 +793,25 @@ void matrix_set_transpose_csr(Matrix *m, const int32_t *roT, const int32_t *colT
 
 static void matrix_transpose_from_csr(Matrix *m)
 {
+    // A^T values on A's own pattern, whatever the order of A's rows: the
+    // k-th entry (i, j) of row i takes the k-th entry (j, i) of row j
     Context *ctx = m->ctx;
-    DeviceBuffer roT, colT, valT;
-    roT.ensure(sizeof(int32_t) * ((size_t)m->n + 1));
-    colT.ensure(sizeof(int32_t) * ((size_t)m->nnz + 1));
-    valT.ensure(sizeof(double) * ((size_t)m->nnz + 1));
-    csr_transpose(ctx, m->n, m->n, m->nnz, m->ro.as<int32_t>(), m->col.as<int32_t>(), m->val.as<double>(),
-                  roT.as<int32_t>(), colT.as<int32_t>(), valT.as<double>());
-    matrix_set_transpose_csr(m, roT.as<int32_t>(), colT.as<int32_t>(), valT.as<double>());
+    m->valT.ensure(sizeof(double) * ((size_t)m->nnz + 4));
+    CF_CUDA(cudaMemsetAsync(m->valT.as<double>() + m->nnz, 0, sizeof(double) * 4, ctx->stream));
+    DeviceBuffer flag;
+    flag.ensure(sizeof(int));
+    CF_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
+    if (m->n > 0) {
+        k_transpose_on_pattern<<<grid_for(ctx, m->n), kBlock, 0, ctx->stream>>>(
+            m->n, m->ro.as<int32_t>(), m->col.as<int32_t>(), m->val.as<double>(), m->valT.as<double>(),
+            flag.as<int>());
+        CF_CHECK_LAUNCH();
+    }
+    require(read_flag(ctx, flag.as<int>()) == 0, CF_UNSUPPORTED,
+            "A^T needs a structurally symmetric matrix (every (i, j) entry matched by a (j, i) entry)");
+    m->have_valT = true;
+    m->have_T32 = false;
+    m->have_svalT = m->have_svalT32 = false;
 }
 
 // Decide the fast kernels' format (once per pattern) and bring the SELL-32

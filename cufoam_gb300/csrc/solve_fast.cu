@@ -144,6 +144,95 @@ __global__ void __launch_bounds__(kBlock) k_f_flush_x(const SolveArgs *__restric
 }
 
 // ---------------------------------------------------------------------------
+// Jacobi-preconditioned CG (no reference counterpart): CG on the same three
+// passes with z = D^-1 r formed where it is used --
+//   prep:   x += xi_{k-1} p_{k-1} (deferred);  p_k = z + beta p_{k-1}
+//   spmv:   k_f_cg_spmv (q = A p_k, (p_k, q) -> xi_k = (r, z) / (p, q))
+//   update: r -= xi_k q, (r, r) for the stopping test, (r, z) -> beta
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_f_pcg_prep(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n;
+    const int k = ld_cg(&st->k) + 1;
+    double *__restrict__ p = a->p[0];
+    const double *__restrict__ r = a->r[0];
+    const double *__restrict__ dinv = a->dinv;
+    double *__restrict__ x = a->x;
+    if (k == 1) {
+        CF_FOR_ELEMS(i, n) p[i] = __dmul_rn(dinv[i], r[i]);
+        return;
+    }
+    const double beta = ld_cg(&st->beta);
+    const double xi = ld_cg(&st->xi);
+    CF_X4_LOOP(i, n) {
+        double pv[4], xv[4], rv[4], dv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            pv[u] = p[CF_X4_IDX(i, u)];
+            xv[u] = x[CF_X4_IDX(i, u)];
+            rv[u] = r[CF_X4_IDX(i, u)];
+            dv[u] = dinv[CF_X4_IDX(i, u)];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            x[CF_X4_IDX(i, u)] = fma_t(xi, pv[u], xv[u]);
+            p[CF_X4_IDX(i, u)] = fma_t(beta, pv[u], __dmul_rn(dv[u], rv[u]));
+        }
+    }
+    CF_X4_TAIL(i, n) {
+        const double pi = p[i];
+        x[i] = fma_t(xi, pi, x[i]);
+        p[i] = fma_t(beta, pi, __dmul_rn(dinv[i], r[i]));
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_f_pcg_update(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st;
+    CF_EXIT_IF_DONE(a, st, true);
+    const int n = a->n;
+    const double xi = ld_cg(&st->xi);
+    double *__restrict__ r = a->r[0];
+    const double *__restrict__ q = a->q;
+    const double *__restrict__ dinv = a->dinv;
+    double rr[4] = {0.0, 0.0, 0.0, 0.0}, rz[4] = {0.0, 0.0, 0.0, 0.0};
+    CF_X4_LOOP(i, n) {
+        double qv[4], rv[4], dv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            qv[u] = q[CF_X4_IDX(i, u)];
+            rv[u] = r[CF_X4_IDX(i, u)];
+            dv[u] = dinv[CF_X4_IDX(i, u)];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double ri = fma_t(-xi, qv[u], rv[u]);
+            r[CF_X4_IDX(i, u)] = ri;
+            rr[u] = fma_t(ri, ri, rr[u]);
+            rz[u] = fma_t(ri, __dmul_rn(dv[u], ri), rz[u]);
+        }
+    }
+    CF_X4_TAIL(i, n) {
+        const double ri = fma_t(-xi, q[i], r[i]);
+        r[i] = ri;
+        rr[0] = fma_t(ri, ri, rr[0]);
+        rz[0] = fma_t(ri, __dmul_rn(dinv[i], ri), rz[0]);
+    }
+    double acc[2] = {(rr[0] + rr[1]) + (rr[2] + rr[3]), (rz[0] + rz[1]) + (rz[2] + rz[3])};
+    double tot[2];
+    if (grid_reduce<2, double>(acc, a->partials, a->partial_stride, &st->counters[SLOT_B], false, tot) &&
+        threadIdx.x == 0) {
+        st->rho1 = st->rho0;
+        st->rho0 = tot[1];
+        st->beta = st->rho0 / st->rho1;
+        st->x_pending = 1;
+        finish_step(a, st, sqrt(tot[0]));
+    }
+}
+
+// ---------------------------------------------------------------------------
 // BiCG with A^T (SolverSingleGPU.h:568-675):
 //   prep:   x += xi p (deferred); p = r + theta p; p* = r* + theta p*
 //   spmv:   q = A p, q* = A^T p* (one pass over the shared pattern),
@@ -504,6 +593,11 @@ static Kernels fast_kernels(int solver)
     case CF_JACOBI:
         k.k0 = (const void *)k_f_jac_prep;
         k.k1 = (const void *)k_f_jac_spmv<FMT>;
+        break;
+    case CF_PCG:
+        k.k0 = (const void *)k_f_pcg_prep;
+        k.k1 = (const void *)k_f_cg_spmv<FMT>;
+        k.k2 = (const void *)k_f_pcg_update;
         break;
     case CF_RICHARDSON:
         k.k0 = (const void *)k_f_rich_prep;

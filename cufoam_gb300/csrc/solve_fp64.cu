@@ -82,9 +82,9 @@ __global__ void __launch_bounds__(kBlock) k_res_init(const SolveArgs *__restrict
     const int n = a->n, cap = a->stage_cap;
     CF_STAGE(double, cap);
     const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val, *x = a->x, *b = a->b, *sD = a->dinv_sqrt;
+    const double *val = a->val, *x = a->x, *b = a->b, *sD = a->dinv_sqrt, *dinv = a->dinv;
     double *r = a->r[0], *rs = a->rs;
-    double acc[1] = {0.0};
+    double acc[2] = {0.0, 0.0};
     CF_FOR_CHUNKS(base, n) {
         const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
@@ -95,13 +95,16 @@ __global__ void __launch_bounds__(kBlock) k_res_init(const SolveArgs *__restrict
             r[row] = ri;
             if (mode == 2) rs[row] = ri;
             acc[0] = fma_t(ri, ri, acc[0]);
+            if (mode == 3) acc[1] = fma_t(ri, __dmul_rn(dinv[row], ri), acc[1]);
         }
         __syncwarp();
     }
-    double tot[1];
-    if (grid_reduce<1, double>(acc, a->partials, a->partial_stride, &a->st->counters[SLOT_INIT],
-                               a->ref_order, tot) && threadIdx.x == 0)
+    double tot[2];
+    if (grid_reduce<2, double>(acc, a->partials, a->partial_stride, &a->st->counters[SLOT_INIT],
+                               a->ref_order, tot) && threadIdx.x == 0) {
         finish_init(a, a->st, tot[0], mode == 2);
+        if (mode == 3) a->st->rho0 = tot[1]; // PCG: (r, D^-1 r)
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -573,7 +576,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
            cf_perf *perf)
 {
     Context *ctx = m->ctx;
-    require(solver >= CF_CG && solver <= CF_RICHARDSON, CF_BAD_INPUT, "unknown solver");
+    require(solver >= CF_CG && solver <= CF_PCG, CF_BAD_INPUT, "unknown solver");
     require(b_in && x_io, CF_BAD_INPUT, "source and psi must not be null");
     require(c.memory == CF_MEM_HOST || c.memory == CF_MEM_DEVICE, CF_BAD_INPUT, "bad memory kind");
     require(c.reduction == CF_REDUCE_FAST || c.reduction == CF_REDUCE_REFERENCE, CF_BAD_INPUT,
@@ -584,6 +587,10 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     require(c.precision == CF_PREC_FP64 || mixed, CF_BAD_INPUT, "bad precision");
     require(!mixed || mixed_supported(solver), CF_UNSUPPORTED,
             "mixed precision is implemented for CG, BiCG and MR");
+    require(solver != CF_PCG || (!mixed && c.transpose == 0), CF_UNSUPPORTED,
+            "the preconditioned CG is FP64 only");
+    require(solver != CF_PCG || c.reduction == CF_REDUCE_FAST, CF_UNSUPPORTED,
+            "the preconditioned CG has no reference summation order (no reference counterpart)");
     const bool ref = c.reduction == CF_REDUCE_REFERENCE && !mixed;
     const int cap = stage_cap_for(m);
     const bool tr = c.transpose != 0;
@@ -720,7 +727,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     }
     // ---- initial residual ----------------------------------------------
     {
-        int mode = mixed ? 0 : (solver == CF_JMR ? 1 : (solver == CF_BICG ? 2 : 0));
+        int mode = mixed ? 0 : (solver == CF_JMR ? 1 : (solver == CF_BICG ? 2 : (solver == CF_PCG ? 3 : 0)));
         void *a2[] = {&d_args, &mode};
         launch(ctx, ctx->stream, (const void *)k_res_init,
                launch_cfg(ctx, (const void *)k_res_init, true, cap, ref), a2);
@@ -792,7 +799,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
         }
     }
     // ---- deferred updates ------------------------------------------------
-    if ((solver == CF_CG || solver == CF_BICG) && !mixed) {
+    if ((solver == CF_CG || solver == CF_BICG || solver == CF_PCG) && !mixed) {
         const void *flush = ref ? (const void *)k_flush_x : fast_flush_kernel();
         launch(ctx, ctx->stream, flush, launch_cfg(ctx, flush, false, cap, false), args1);
         k_clear_pending<<<1, 32, 0, ctx->stream>>>(A.st);

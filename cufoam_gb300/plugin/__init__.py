@@ -24,6 +24,13 @@ def lib():
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                C.c_double, C.c_int, C.c_int, C.POINTER(C.c_char_p),
                                C.POINTER(C.c_char_p), C.c_void_p, C.c_char_p, C.c_int]
+        L.mf_solve_coupled.restype = C.c_int
+        L.mf_solve_coupled.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_double, C.c_double, C.c_int, C.c_int,
+                                       C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_void_p, C.c_char_p, C.c_int]
         _lib = L
     return _lib
 
@@ -33,10 +40,13 @@ class FoamError(RuntimeError):
 
 
 def foam_solve(solver: str, ldu, source, psi, tolerance: float = 1e-6, rel_tol: float = 0.0,
-               max_iter: int = 1000, symmetric: bool | None = None, **controls):
+               max_iter: int = 1000, symmetric: bool | None = None, cyclic=None,
+               processor_patch: bool = False, **controls):
     """Run the plugin `solver` on an LDU matrix through the OpenFOAM-style
     interface; psi (float64 array) is updated in place.  Returns the
-    solverPerformance fields as a dict."""
+    solverPerformance fields as a dict.  cyclic = (faceCellsA, faceCellsB,
+    coeffsA, coeffsB) adds a cyclic patch pair (interfaceBouCoeffs coeffs);
+    processor_patch adds a processor interface."""
     if symmetric is None:
         symmetric = np.array_equal(ldu.lower, ldu.upper)
     d = np.ascontiguousarray(ldu.diag, np.float64)
@@ -53,10 +63,23 @@ def foam_solve(solver: str, ldu, source, psi, tolerance: float = 1e-6, rel_tol: 
     cv = (C.c_char_p * max(1, len(vals)))(*vals)
     out = np.zeros(4)
     err = C.create_string_buffer(1024)
-    rc = lib().mf_solve(solver.encode(), ldu.n, lo.shape[0], d.ctypes.data,
-                        None if symmetric else lo.ctypes.data, up.ctypes.data, la.ctypes.data,
-                        ua.ctypes.data, b.ctypes.data, psi.ctypes.data, tolerance, rel_tol,
-                        max_iter, len(keys), ck, cv, out.ctypes.data, err, 1024)
+    if cyclic is None and not processor_patch:
+        rc = lib().mf_solve(solver.encode(), ldu.n, lo.shape[0], d.ctypes.data,
+                            None if symmetric else lo.ctypes.data, up.ctypes.data, la.ctypes.data,
+                            ua.ctypes.data, b.ctypes.data, psi.ctypes.data, tolerance, rel_tol,
+                            max_iter, len(keys), ck, cv, out.ctypes.data, err, 1024)
+    else:
+        fa, fb, ca, cb = cyclic if cyclic is not None else ([], [], [], [])
+        fa, fb = np.ascontiguousarray(fa, np.int32), np.ascontiguousarray(fb, np.int32)
+        ca, cb = np.ascontiguousarray(ca, np.float64), np.ascontiguousarray(cb, np.float64)
+        if not (fa.shape == fb.shape == ca.shape == cb.shape):
+            raise ValueError("cyclic patch arrays must have one length")
+        rc = lib().mf_solve_coupled(solver.encode(), ldu.n, lo.shape[0], d.ctypes.data,
+                                    None if symmetric else lo.ctypes.data, up.ctypes.data,
+                                    la.ctypes.data, ua.ctypes.data, b.ctypes.data, psi.ctypes.data,
+                                    tolerance, rel_tol, max_iter, len(keys), ck, cv, int(fa.shape[0]),
+                                    fa.ctypes.data, fb.ctypes.data, ca.ctypes.data, cb.ctypes.data,
+                                    1 if processor_patch else 0, out.ctypes.data, err, 1024)
     if rc != 0:
         raise FoamError(err.value.decode())
     return {"initialResidual": out[0], "finalResidual": out[1], "nIterations": int(out[2]),

@@ -19,6 +19,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
+#include <vector>
 
 namespace Foam {
 
@@ -132,14 +134,93 @@ cf_controls cuFoamGB300Solver::gb300Controls() const
     return c;
 }
 
+cf_matrix *cuFoamGB300Solver::coupledMatrix() const
+{
+    // couplings of the cyclic patches: (faceCell, neighbour faceCell, -coeff)
+    std::vector<std::vector<std::pair<label, scalar>>> extra;
+    bool any = false;
+    const lduInterfaceFieldPtrsList &ifs = interfaces();
+    for (label patchi = 0; patchi < ifs.size(); ++patchi) {
+        if (!ifs.set(patchi)) continue;
+        const lduInterface &ifc = ifs[patchi].interface();
+        if (!isA<cyclicLduInterface>(ifc)) {
+            FatalErrorInFunction << type() << ": patch " << patchi
+                                 << " is a coupled interface other than cyclic (e.g. a processor "
+                                    "patch); only cyclic interfaces are solved on one GPU"
+                                 << exit(FatalError);
+        }
+        const cyclicLduInterface &cyc = refCast<const cyclicLduInterface>(ifc);
+        const labelList &fc = cyc.faceCells();
+        const labelList &nfc = cyc.neighbPatch().faceCells();
+        const scalarField &coeffs = interfaceBouCoeffs()[patchi];
+        if (nfc.size() != fc.size() || coeffs.size() != fc.size()) {
+            FatalErrorInFunction << type() << ": cyclic patch " << patchi
+                                 << " does not match its neighbour" << exit(FatalError);
+        }
+        if (extra.empty()) extra.resize(matrix().diag().size());
+        for (label f = 0; f < fc.size(); ++f) extra[fc[f]].push_back({nfc[f], -coeffs[f]});
+        any = any || fc.size() > 0;
+    }
+    if (!any) return nullptr;
+    // the LDU part as the reference's CSR (device ldu2csr), then each row's
+    // interface entries after its own
+    const lduMatrix &M = matrix();
+    const lduAddressing &A = M.lduAddr();
+    const label n = M.diag().size(), nf = A.lowerAddr().size();
+    cf_ldu_view v;
+    std::memset(&v, 0, sizeof(v));
+    v.n_cells = n;
+    v.n_faces = nf;
+    v.diag = M.diag().cdata();
+    v.lower = M.lower().cdata();
+    v.upper = M.upper().cdata();
+    v.lower_addr = A.lowerAddr().cdata();
+    v.upper_addr = A.upperAddr().cdata();
+    v.losort = A.losortAddr().cdata();
+    v.losort_start = A.losortStartAddr().cdata();
+    v.owner_start = A.ownerStartAddr().cdata();
+    v.memory = CF_MEM_HOST;
+    std::vector<int32_t> ro((size_t)n + 1), col((size_t)n + 2 * (size_t)nf);
+    std::vector<double> val(col.size());
+    cf_context *ctx = gb300Context();
+    cf_status st = cf_ldu2csr(ctx, &v, ro.data(), col.data(), val.data(), CF_MEM_HOST);
+    std::vector<int32_t> ro2((size_t)n + 1), col2;
+    std::vector<double> val2;
+    if (st == CF_OK) {
+        col2.reserve(col.size() + 2 * (size_t)n);
+        val2.reserve(col.size() + 2 * (size_t)n);
+        for (label i = 0; i < n; ++i) {
+            ro2[(size_t)i] = (int32_t)col2.size();
+            for (int32_t j = ro[(size_t)i]; j < ro[(size_t)i + 1]; ++j) {
+                col2.push_back(col[(size_t)j]);
+                val2.push_back(val[(size_t)j]);
+            }
+            for (const auto &e : extra[(size_t)i]) {
+                col2.push_back(e.first);
+                val2.push_back(e.second);
+            }
+        }
+        ro2[(size_t)n] = (int32_t)col2.size();
+        cf_matrix *m = nullptr;
+        st = cf_matrix_create_csr(ctx, n, (int64_t)col2.size(), ro2.data(), col2.data(), val2.data(),
+                                  CF_MEM_HOST, &m);
+        if (st == CF_OK) return m;
+    }
+    FatalErrorInFunction << "cuFoamGB300: cannot load the coupled matrix: " << cf_status_string(st)
+                         << ": " << cf_context_last_error(ctx) << exit(FatalError);
+    return nullptr;
+}
+
 solverPerformance cuFoamGB300Solver::solve(scalarField &psi, const scalarField &source,
                                            const direction) const
 {
-    cf_matrix *m = deviceMatrix(matrix());
+    cf_matrix *coupled = coupledMatrix();
+    cf_matrix *m = coupled ? coupled : deviceMatrix(matrix());
     const cf_controls c = gb300Controls();
     cf_perf perf;
     std::memset(&perf, 0, sizeof(perf));
     const cf_status st = cf_solve(m, kind_, &c, source.cdata(), psi.data(), &perf);
+    if (coupled) cf_matrix_destroy(coupled);
     if (st != CF_OK) {
         FatalErrorInFunction << type() << ": solve failed: " << cf_status_string(st) << ": "
                              << cf_context_last_error(gb300Context()) << exit(FatalError);
@@ -186,5 +267,7 @@ CUFOAM_GB300_ASYMMETRIC(cuFoamMRS)
 CUFOAM_GB300_DEFINE_SOLVER(cuFoamJMR, CF_JMR)
 CUFOAM_GB300_ASYMMETRIC(cuFoamJMR)
 CUFOAM_GB300_DEFINE_SOLVER(cuFoamRichardson, CF_RICHARDSON)
+// Jacobi-preconditioned CG (no reference counterpart), symmetric matrices
+CUFOAM_GB300_DEFINE_SOLVER(cuFoamPCG, CF_PCG)
 
 } // namespace Foam

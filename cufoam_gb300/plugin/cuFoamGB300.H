@@ -16,6 +16,13 @@
  *     normType    reference | openfoam
  *     useRelTol   false               (true: honour relTol_/minIter_ like OpenFOAM)
  *
+ * Coupled interfaces: cyclic patches are folded into the device matrix
+ * (OpenFOAM's interface update, result -= interfaceBouCoeffs * psi of the
+ * neighbour patch's face cells, becomes the CSR entries (faceCell,
+ * neighbour faceCell) = -coeff appended to each row); processor patches
+ * couple to other ranks and are rejected.  The reference ignores all
+ * interfaces.
+ *
  * Residuals in the returned solverPerformance are normalised by normFactor
  * (OpenFOAM's convention); the stopping test is the reference's
  * ||r||_2 <= tolerance * normFactor.
@@ -27,6 +34,8 @@
 #define CUFOAM_GB300_PLUGIN_H
 
 #include "lduMatrix.H"
+#include "cyclicLduInterface.H"
+#include "processorLduInterface.H"
 #include "cufoam_gb300.h"
 
 namespace Foam {
@@ -36,6 +45,10 @@ protected:
     const int32_t kind_;
 
     cf_controls gb300Controls() const;
+
+    // The matrix with this solver's cyclic interfaces folded in (a new
+    // device matrix, owned by the caller), or nullptr without coupling.
+    cf_matrix *coupledMatrix() const;
 
 public:
     cuFoamGB300Solver(int32_t kind, const word &fieldName, const lduMatrix &matrix,
@@ -69,6 +82,7 @@ CUFOAM_GB300_DECLARE_SOLVER(cuFoamMRJacobi)
 CUFOAM_GB300_DECLARE_SOLVER(cuFoamMRS)
 CUFOAM_GB300_DECLARE_SOLVER(cuFoamJMR)
 CUFOAM_GB300_DECLARE_SOLVER(cuFoamRichardson)
+CUFOAM_GB300_DECLARE_SOLVER(cuFoamPCG)
 
 #undef CUFOAM_GB300_DECLARE_SOLVER
 

@@ -56,8 +56,67 @@ typedef Field<scalar> scalarField;
 template <template <class> class F, class T>
 class FieldField : public std::vector<F<T>> {};
 
-class lduInterfaceField;
-typedef std::vector<const lduInterfaceField *> lduInterfaceFieldPtrsList;
+// ---- coupled interfaces (OpenFOAM's lduInterface / lduInterfaceField) -----
+class lduInterface {
+public:
+    virtual ~lduInterface() {}
+    virtual const labelList &faceCells() const = 0;
+};
+
+// a cyclic patch couples its face cells to the face cells of its
+// neighbour patch (cyclicLduInterface::neighbPatch)
+class cyclicLduInterface : public lduInterface {
+    labelList faceCells_;
+    const cyclicLduInterface *nbr_ = nullptr;
+
+public:
+    explicit cyclicLduInterface(const labelList &faceCells) : faceCells_(faceCells) {}
+    void setNeighbPatch(const cyclicLduInterface &n) { nbr_ = &n; }
+    const labelList &faceCells() const override { return faceCells_; }
+    const cyclicLduInterface &neighbPatch() const { return *nbr_; }
+};
+
+// a processor patch couples to cells of another MPI rank
+class processorLduInterface : public lduInterface {
+    labelList faceCells_;
+
+public:
+    explicit processorLduInterface(const labelList &faceCells) : faceCells_(faceCells) {}
+    const labelList &faceCells() const override { return faceCells_; }
+};
+
+class lduInterfaceField {
+    const lduInterface &interface_;
+
+public:
+    explicit lduInterfaceField(const lduInterface &i) : interface_(i) {}
+    virtual ~lduInterfaceField() {}
+    const lduInterface &interface() const { return interface_; }
+};
+
+// UPtrList<const lduInterfaceField>: null entries for uncoupled patches
+class lduInterfaceFieldPtrsList : public std::vector<const lduInterfaceField *> {
+public:
+    using std::vector<const lduInterfaceField *>::vector;
+    label size() const { return (label)std::vector<const lduInterfaceField *>::size(); }
+    bool set(label i) const { return (*this).std::vector<const lduInterfaceField *>::operator[](i) != nullptr; }
+    const lduInterfaceField &operator[](label i) const
+    {
+        return *std::vector<const lduInterfaceField *>::operator[](i);
+    }
+};
+
+template <class T, class U>
+bool isA(const U &u)
+{
+    return dynamic_cast<const T *>(&u) != nullptr;
+}
+
+template <class To, class From>
+To &refCast(From &f)
+{
+    return dynamic_cast<To &>(f);
+}
 
 // ---- errors ----------------------------------------------------------------
 struct ExitTag {};
@@ -213,6 +272,9 @@ public:
     protected:
         word fieldName_;
         const lduMatrix &matrix_;
+        const FieldField<Field, scalar> &interfaceBouCoeffs_;
+        const FieldField<Field, scalar> &interfaceIntCoeffs_;
+        const lduInterfaceFieldPtrsList &interfaces_;
         dictionary controlDict_;
         label maxIter_, minIter_;
         scalar tolerance_, relTol_;
@@ -248,10 +310,12 @@ public:
             addasymMatrixConstructorToTable() { asymMatrixConstructorTable()[T::typeName] = &make<T>; }
         };
 
-        solver(const word &fieldName, const lduMatrix &matrix, const FieldField<Field, scalar> &,
-               const FieldField<Field, scalar> &, const lduInterfaceFieldPtrsList &,
-               const dictionary &solverControls)
-            : fieldName_(fieldName), matrix_(matrix), controlDict_(solverControls)
+        solver(const word &fieldName, const lduMatrix &matrix,
+               const FieldField<Field, scalar> &interfaceBouCoeffs,
+               const FieldField<Field, scalar> &interfaceIntCoeffs,
+               const lduInterfaceFieldPtrsList &interfaces, const dictionary &solverControls)
+            : fieldName_(fieldName), matrix_(matrix), interfaceBouCoeffs_(interfaceBouCoeffs),
+              interfaceIntCoeffs_(interfaceIntCoeffs), interfaces_(interfaces), controlDict_(solverControls)
         {
             maxIter_ = controlDict_.lookupOrDefault<label>("maxIter", 1000);
             minIter_ = controlDict_.lookupOrDefault<label>("minIter", 0);
@@ -263,6 +327,9 @@ public:
         const word &fieldName() const { return fieldName_; }
         const lduMatrix &matrix() const { return matrix_; }
         const dictionary &controlDict() const { return controlDict_; }
+        const FieldField<Field, scalar> &interfaceBouCoeffs() const { return interfaceBouCoeffs_; }
+        const FieldField<Field, scalar> &interfaceIntCoeffs() const { return interfaceIntCoeffs_; }
+        const lduInterfaceFieldPtrsList &interfaces() const { return interfaces_; }
         virtual solverPerformance solve(scalarField &psi, const scalarField &source,
                                         const direction cmpt = 0) const = 0;
 

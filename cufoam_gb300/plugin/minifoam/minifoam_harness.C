@@ -14,17 +14,21 @@ namespace Foam {
 FatalErrorType FatalError;
 }
 
-extern "C" {
+namespace {
 
-/* Solve with the plugin `solver_name` ("cuFoamCG", ...).  lower == NULL
- * means a symmetric matrix (OpenFOAM stores only upper then).  `keys` /
- * `values` are n_extra extra dictionary entries (e.g. "precision" "mixed").
- * out = {initialResidual, finalResidual, nIterations, converged}.
- * Returns 0, or -1 with the FatalError text in err. */
-int mf_solve(const char *solver_name, int n, int n_faces, const double *diag, const double *lower,
-             const double *upper, const int *lower_addr, const int *upper_addr, const double *source,
-             double *psi, double tolerance, double rel_tol, int max_iter, int n_extra,
-             const char *const *keys, const char *const *values, double *out, char *err, int err_len)
+// One cyclic patch pair (faces of patch A coupled to patch B, and back),
+// an optional processor patch; n_cyc = 0: no interfaces.
+struct Coupling {
+    int n_cyc = 0;
+    const int *fcA = nullptr, *fcB = nullptr;
+    const double *coeffA = nullptr, *coeffB = nullptr;
+    bool processor = false;
+};
+
+int run(const char *solver_name, int n, int n_faces, const double *diag, const double *lower,
+        const double *upper, const int *lower_addr, const int *upper_addr, const double *source,
+        double *psi, double tolerance, double rel_tol, int max_iter, int n_extra, const char *const *keys,
+        const char *const *values, const Coupling &cpl, double *out, char *err, int err_len)
 {
     try {
         using namespace Foam;
@@ -36,7 +40,6 @@ int mf_solve(const char *solver_name, int n, int n_faces, const double *diag, co
         lduMatrix matrix(addr, d, lower ? &lo : nullptr, &up);
         dictionary controls;
         controls.set("solver", solver_name);
-        controls.set("tolerance", std::to_string(tolerance));
         {
             // exact text of the doubles
             char buf[64];
@@ -49,6 +52,34 @@ int mf_solve(const char *solver_name, int n, int n_faces, const double *diag, co
         for (int i = 0; i < n_extra; ++i) controls.set(keys[i], values[i]);
         FieldField<Field, scalar> bou, intc;
         lduInterfaceFieldPtrsList interfaces;
+        // patch 0: an uncoupled wall; patches 1, 2: the cyclic pair; 3: processor
+        std::unique_ptr<cyclicLduInterface> cycA, cycB;
+        std::unique_ptr<processorLduInterface> proc;
+        std::vector<std::unique_ptr<lduInterfaceField>> fields;
+        bou.resize(1);
+        intc.resize(1);
+        interfaces.push_back(nullptr);
+        if (cpl.n_cyc > 0) {
+            cycA.reset(new cyclicLduInterface(labelList(cpl.fcA, cpl.fcA + cpl.n_cyc)));
+            cycB.reset(new cyclicLduInterface(labelList(cpl.fcB, cpl.fcB + cpl.n_cyc)));
+            cycA->setNeighbPatch(*cycB);
+            cycB->setNeighbPatch(*cycA);
+            fields.emplace_back(new lduInterfaceField(*cycA));
+            fields.emplace_back(new lduInterfaceField(*cycB));
+            interfaces.push_back(fields[0].get());
+            interfaces.push_back(fields[1].get());
+            bou.push_back(scalarField(cpl.coeffA, cpl.coeffA + cpl.n_cyc));
+            bou.push_back(scalarField(cpl.coeffB, cpl.coeffB + cpl.n_cyc));
+            intc.push_back(scalarField(cpl.coeffA, cpl.coeffA + cpl.n_cyc));
+            intc.push_back(scalarField(cpl.coeffB, cpl.coeffB + cpl.n_cyc));
+        }
+        if (cpl.processor) {
+            proc.reset(new processorLduInterface(labelList(1, 0)));
+            fields.emplace_back(new lduInterfaceField(*proc));
+            interfaces.push_back(fields.back().get());
+            bou.push_back(scalarField(1, 1.0));
+            intc.push_back(scalarField(1, 1.0));
+        }
         std::unique_ptr<lduMatrix::solver> s =
             lduMatrix::solver::New("psi", matrix, bou, intc, interfaces, controls);
         scalarField x(psi, psi + n), b(source, source + n);
@@ -67,6 +98,45 @@ int mf_solve(const char *solver_name, int n, int n_faces, const double *diag, co
         }
         return -1;
     }
+}
+
+} // namespace
+
+extern "C" {
+
+/* Solve with the plugin `solver_name` ("cuFoamCG", ...).  lower == NULL
+ * means a symmetric matrix (OpenFOAM stores only upper then).  `keys` /
+ * `values` are n_extra extra dictionary entries (e.g. "precision" "mixed").
+ * out = {initialResidual, finalResidual, nIterations, converged}.
+ * Returns 0, or -1 with the FatalError text in err. */
+int mf_solve(const char *solver_name, int n, int n_faces, const double *diag, const double *lower,
+             const double *upper, const int *lower_addr, const int *upper_addr, const double *source,
+             double *psi, double tolerance, double rel_tol, int max_iter, int n_extra,
+             const char *const *keys, const char *const *values, double *out, char *err, int err_len)
+{
+    return run(solver_name, n, n_faces, diag, lower, upper, lower_addr, upper_addr, source, psi, tolerance,
+               rel_tol, max_iter, n_extra, keys, values, Coupling(), out, err, err_len);
+}
+
+/* The same with a cyclic patch pair: face f of patch A (cell fcA[f])
+ * coupled to face f of patch B (cell fcB[f]) with interfaceBouCoeffs
+ * coeffA / coeffB; processor != 0 adds a processor patch. */
+int mf_solve_coupled(const char *solver_name, int n, int n_faces, const double *diag, const double *lower,
+                     const double *upper, const int *lower_addr, const int *upper_addr,
+                     const double *source, double *psi, double tolerance, double rel_tol, int max_iter,
+                     int n_extra, const char *const *keys, const char *const *values, int n_cyc,
+                     const int *fcA, const int *fcB, const double *coeffA, const double *coeffB,
+                     int processor, double *out, char *err, int err_len)
+{
+    Coupling c;
+    c.n_cyc = n_cyc;
+    c.fcA = fcA;
+    c.fcB = fcB;
+    c.coeffA = coeffA;
+    c.coeffB = coeffB;
+    c.processor = processor != 0;
+    return run(solver_name, n, n_faces, diag, lower, upper, lower_addr, upper_addr, source, psi, tolerance,
+               rel_tol, max_iter, n_extra, keys, values, c, out, err, err_len);
 }
 
 } // extern "C"

@@ -40,7 +40,9 @@ typedef enum cf_status {
     CF_OUT_OF_MEMORY = 9
 } cf_status;
 
-/* Solver selection: the eight cuFoam plugins (fvSolution `solver cuFoamX;`). */
+/* Solver selection: the eight cuFoam plugins (fvSolution `solver cuFoamX;`),
+ * plus a Jacobi-preconditioned CG (CF_PCG) the reference announces in its
+ * roadmap (README.md:71-73) but does not have. */
 typedef enum cf_solver {
     CF_CG = 0,         /* cuFoamCG         -> gis.h:11-17  CG */
     CF_BICG = 1,       /* cuFoamBiCG       -> gis.h:28-36  BiCG(A, At) */
@@ -49,7 +51,9 @@ typedef enum cf_solver {
     CF_MRJACOBI = 4,   /* cuFoamMRJacobi   -> gis.h:64-70  MRJacobi */
     CF_MRS = 5,        /* cuFoamMRS        -> gis.h:80-87  MRS with invM = D^-1 */
     CF_JMR = 6,        /* cuFoamJMR        -> gis.h:72-78  JMR */
-    CF_RICHARDSON = 7  /* cuFoamRichardson -> gis.h:38-46  Richardson */
+    CF_RICHARDSON = 7, /* cuFoamRichardson -> gis.h:38-46  Richardson */
+    CF_PCG = 8         /* cuFoamPCG: CG preconditioned by D^-1 (no reference
+                          counterpart; fast reduction order, FP64 only) */
 } cf_solver;
 
 enum { CF_MEM_HOST = 0, CF_MEM_DEVICE = 1 };

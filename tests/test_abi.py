@@ -83,12 +83,14 @@ class _FakeMatrix:
 
 
 def test_runtime_selection_tables():
-    # CG and Richardson register only for symmetric matrices
+    # CG and Richardson register only for symmetric matrices (and the
+    # Jacobi-preconditioned CG, which has no reference counterpart)
     assert cf.solver_names(True) == sorted(["cuFoamBiCG", "cuFoamCG", "cuFoamJMR", "cuFoamJacobi",
                                             "cuFoamMR", "cuFoamMRJacobi", "cuFoamMRS",
-                                            "cuFoamRichardson"])
+                                            "cuFoamRichardson", "cuFoamPCG"])
     assert "cuFoamCG" not in cf.solver_names(False)
     assert "cuFoamRichardson" not in cf.solver_names(False)
+    assert "cuFoamPCG" not in cf.solver_names(False)
     s = cf.New("p", _FakeMatrix(True), {"solver": "cuFoamCG", "tolerance": 1e-8})
     assert isinstance(s, cf.cuFoamCG) and s.type_name == "cuFoamCG"
     with pytest.raises(KeyError):
