@@ -467,7 +467,7 @@ def batched_vs_sequential(ctx, device, n_systems: int = 512, tol: float = 1e-8,
     B = BatchSolver(systems, n_rhs=3, context=ctx)
     dev = f"cuda:{device}"
     packed = torch.from_numpy(B.pack(rhs)).to(dev)
-    cands = [(1, 256, 0), (2, 256, 0), (4, 256, 0), (8, 256, 0), (4, 512, 0)]
+    cands = [(4, 256, 0), (8, 256, 0), (16, 256, 0), (16, 128, 0), (4, 512, 0)]
     cfg, entry = B.tune(packed, tolerance=tol, max_iter=max_iter, candidates=cands, use_cache=False)
     x, res, ms = B.solve(packed, tolerance=tol, max_iter=max_iter)
     torch.cuda.synchronize()
@@ -565,6 +565,89 @@ def run_profile_mr(args):
     return 0
 
 
+def run_profile_batch(args):
+    """A batched solve small enough for a full ncu capture: 256 lognormal
+    7-point boxes with sides uniform in 16..40, rows permuted, 3 right-hand
+    sides, CG to 1e-8 in FP64 and in mixed precision, default schedule."""
+    import torch
+
+    import cufoam_gb300 as cf
+    from cufoam_gb300 import workloads as W
+    from cufoam_gb300.batch import BatchSolver, c4_systems
+    ctx = cf.Context(0)
+    systems, _ = c4_systems(256, seed=4, lo=16, hi=40)
+    B = BatchSolver(systems, n_rhs=3, context=ctx)
+    rhs = [np.stack([W.uniform(10_000 + 3 * s + j, L.n) for j in range(3)])
+           for s, L in enumerate(systems)]
+    packed = torch.from_numpy(B.pack(rhs)).to("cuda")
+    for prec in ("FP64", "mixed"):
+        _, res, ms = B.solve(packed, tolerance=1e-8, max_iter=5000, precision=prec)
+        print(f"{prec}: {ms:.2f} ms, {sum(r['n_iterations'] for r in res)} iterations, "
+              f"{sum(r['status'] == 0 for r in res)}/{len(res)} converged")
+    B.close()
+    ctx.close()
+    return 0
+
+
+def run_profile_all(args):
+    """A short run for an ncu launch list of every kernel family: on 128^3
+    systems, 20 host-driven steps of each solver in both summation orders
+    (and in mixed precision where it exists), the plain SpMVs, normFactor,
+    the device ldu2csr, one adjoint gradient pass and a small batched solve
+    (64 systems x 3 right-hand sides, FP64 and mixed)."""
+    import torch
+
+    import cufoam_gb300 as cf
+    from cufoam_gb300 import workloads as W
+    from cufoam_gb300.batch import BatchSolver, c4_systems
+    ctx = cf.Context(0)
+    dev = "cuda"
+    n3 = 128
+    sym = W.grid_lognormal(n3, n3, n3, 2)
+    asym, _ = W.grid_convdiff(n3, n3, n3, 3, 10.0)
+    Ms = cf.LduMatrix.from_ldu(sym, ctx)
+    Ma = cf.LduMatrix.from_ldu(asym, ctx)
+    b = torch.from_numpy(W.uniform(3, sym.n)).to(dev)
+    steps = 20
+    for name in ("cuFoamCG", "cuFoamPCG", "cuFoamJacobi", "cuFoamRichardson", "cuFoamMR",
+                 "cuFoamMRJacobi", "cuFoamMRS", "cuFoamJMR", "cuFoamBiCG"):
+        M = Ma if name == "cuFoamBiCG" else Ms
+        orders = ("fast",) if name == "cuFoamPCG" else ("fast", "reference")
+        for red in orders:
+            psi = torch.zeros(sym.n, dtype=torch.float64, device=dev)
+            cf._TABLE[name]("p", M, {"tolerance": 1e-30, "maxIter": steps, "useGraph": 0,
+                                     "reduction": red}).solve(psi, b)
+        if name in ("cuFoamCG", "cuFoamMR", "cuFoamBiCG"):
+            psi = torch.zeros(sym.n, dtype=torch.float64, device=dev)
+            cf._TABLE[name]("p", M, {"tolerance": 1e-30, "maxIter": steps, "useGraph": 0,
+                                     "precision": "mixed", "innerMaxIter": steps,
+                                     "maxRefinements": 2}).solve(psi, b)
+    x = torch.from_numpy(W.uniform(5, sym.n)).to(dev)
+    y = torch.empty_like(x)
+    for row_order in ("fast", "reference"):
+        Ms.spmv(x, row_order=row_order, out=y)
+        Ms.spmv(x, transpose=True, row_order=row_order, out=y)
+    for red in ("fast", "reference"):
+        Ms.norm_factor(b, x, reduction=red)
+    cf.LduMatrix.from_ldu(asym, ctx).close()     # one more device ldu2csr, asymmetric
+    lam = torch.from_numpy(W.uniform(7, sym.n)).to(dev)
+    dd, dl, du = (torch.empty(k, dtype=torch.float64, device=dev)
+                  for k in (sym.n, Ms.n_faces, Ms.n_faces))
+    torch.cuda.synchronize()
+    ctx.check(Ms._lib.cf_adjoint_gradients(Ms.handle, lam.data_ptr(), x.data_ptr(), dd.data_ptr(),
+                                           dl.data_ptr(), du.data_ptr(), 1), "cf_adjoint_gradients")
+    systems, _ = c4_systems(64, seed=4)
+    B = BatchSolver(systems, n_rhs=3, context=ctx)
+    rhs = [np.stack([W.uniform(10_000 + 3 * s + j, L.n) for j in range(3)])
+           for s, L in enumerate(systems)]
+    packed = torch.from_numpy(B.pack(rhs)).to(dev)
+    for prec in ("FP64", "mixed"):
+        B.solve(packed, tolerance=1e-8, max_iter=200, config=(4, 256, 0), precision=prec)
+    torch.cuda.synchronize()
+    print("profile run ok: all kernel families")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -575,11 +658,19 @@ def main():
                     help="skip the mixed-vs-FP64 and batched-vs-sequential comparisons")
     ap.add_argument("--profile", action="store_true",
                     help="short host-driven run for an ncu capture (prints no JSON)")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="one FP64 and one mixed batched solve of 256 small systems, for ncu")
+    ap.add_argument("--profile-all", action="store_true",
+                    help="short run launching every kernel family once, for an ncu launch list")
     ap.add_argument("--profile-mr", action="store_true",
                     help="short host-driven MR run (FP64 and mixed, 256^3) for an ncu capture")
     args = ap.parse_args()
     if args.profile_mr:
         return run_profile_mr(args)
+    if args.profile_all:
+        return run_profile_all(args)
+    if args.profile_batch:
+        return run_profile_batch(args)
     if args.profile:
         return run_profile(args)
     if args.impl == "reference":

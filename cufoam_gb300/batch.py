@@ -47,7 +47,7 @@ def _bind(lib):
 
 
 # schedule candidates of the autotuner: (cluster size, threads per CTA, order)
-CANDIDATES = [(cs, bt, 0) for cs in (1, 2, 4, 8) for bt in (128, 256, 512)] + [(4, 256, 1)]
+CANDIDATES = [(cs, bt, 0) for cs in (1, 2, 4, 8, 16) for bt in (128, 256, 512)] + [(4, 256, 1)]
 
 
 def _cache_path() -> str:
@@ -138,7 +138,7 @@ class BatchSolver:
         c.precision = {"FP64": _capi.CF_PREC_FP64, "mixed": _capi.CF_PREC_MIXED}[precision]
         c.mixed_inner_rtol = inner_rtol
         cfg = cf_batch_config()
-        cs, bt, order = config or self.config or (4, 256, 0)
+        cs, bt, order = config or self.config or (0, 256, 0)   # cluster 0: the library picks 16 or 8
         cfg.cluster_size, cfg.threads, cfg.order = cs, bt, order
         res = (cf_batch_result * (len(self.systems) * self.n_rhs))()
         ms = C.c_double()

@@ -4,21 +4,28 @@
 //
 // Schedule: the grid is one wave of thread-block clusters of CS CTAs.  A
 // cluster takes the next system from a global work queue (systems ordered
-// largest first), splits its rows over its CTAs, and runs the whole solve
-// for all R right-hand sides at once: every matrix entry is read once per
-// iteration for R vectors (R-wide SpMM), vectors are stored row-major with
-// the R components adjacent.  The two dot products per CG step are reduced
-// inside each CTA and then across the cluster through distributed shared
-// memory, after a hardware cluster barrier; every CTA sums the per-CTA
-// partials in rank order, so all CTAs reach bit-identical scalars and take
-// identical control flow.  Each right-hand side keeps its own CG scalars and
-// stopping test (the reference's loop, SolverSingleGPU.h:366-445, with its
-// normFactor, gis/gis.cu:106-123); a converged component is frozen.
+// largest first), splits its 32-row slices over its CTAs, and runs the whole
+// solve for all R right-hand sides at once: every matrix entry is read once
+// per iteration for R vectors (R-wide SpMM, from the system's SELL-32 copy:
+// one warp per slice, coalesced entry loads streamed with an L2 evict-first
+// hint), vectors are stored row-major with the R components adjacent.  A
+// thread owns the same rows in every phase.  One CG step is three passes:
+//   P  x += alpha_{k-1} p (the previous step, deferred), p = r + beta p
+//   A  q = A p, (p, q)          (gathers p only)
+//   B  r -= alpha q, (r, r)
+// with a cluster barrier after P and a cluster reduction after A and B.
+// Dot products are reduced inside each CTA and then across the cluster
+// through distributed shared memory, after a hardware cluster barrier;
+// every CTA sums the per-CTA partials in rank order, so all CTAs reach
+// bit-identical scalars and take identical control flow.  Each right-hand
+// side keeps its own CG scalars and stopping test (the reference's loop,
+// SolverSingleGPU.h:366-445, with its normFactor, gis/gis.cu:106-123); a
+// converged component is frozen after its last step reaches x.
 //
 // Mixed precision (k_batch_cg<R, BT, true>): after the FP64 normFactor and
 // residual, each refinement sweep solves A e = r / ||r|| by CG with FP32
-// values, FP32 vectors and FP32 per-thread sums (combined across CTAs in
-// FP64) to a relative inner tolerance, then adds ||r|| e to x and forms the
+// values, FP32 vectors and FP32 per-thread sums (combined across threads
+// and CTAs in FP64) to a relative inner tolerance, then adds ||r|| e to x and forms the
 // FP64 residual b - A x again; the FP64 tolerance decides convergence.
 #include <cooperative_groups.h>
 
@@ -34,15 +41,33 @@ namespace cgp = cooperative_groups;
 namespace cf {
 
 constexpr int kBatchMaxR = 4;
+// SELL entries loaded (and their R gathers issued) before the first FMA
+#ifndef CF_BATCH_ENTRY_BATCH
+#define CF_BATCH_ENTRY_BATCH 1
+#endif
+constexpr int kBatchEntryBatch = CF_BATCH_ENTRY_BATCH;
+// 1: matrix entries loaded with an L2 evict-first hint (they are re-read
+// only in the next step), 0: plain read-only loads
+#ifndef CF_BATCH_STREAM_HINT
+#define CF_BATCH_STREAM_HINT 1
+#endif
+// resident threads per SM the register budget is sized for
+#ifndef CF_BATCH_THREADS_PER_SM
+#define CF_BATCH_THREADS_PER_SM 1024
+#endif
 
 struct BatchSystem {
     int32_t n;
-    int32_t pad;
+    int32_t sell;            // 1: the SELL-32 copy below, 0: CSR rows
     int64_t vec_offset;      // first row of this system in the batch vectors
-    const int32_t *ro;
+    const int32_t *ro;       // CSR
     const int32_t *col;
     const double *val;
-    const float *val32;      // FP32 copy (mixed precision)
+    const float *val32;      // FP32 CSR values (mixed precision)
+    const int32_t *s_off;    // SELL-32: slice offsets, entry-major columns / values
+    const int32_t *s_col;
+    const double *s_val;
+    const float *s_val32;
 };
 
 struct BatchResult {
@@ -58,11 +83,11 @@ struct BatchArgs {
     double tolerance;
     const double *b;         // [rows][R]
     double *x;               // [rows][R]
-    double *r, *p0, *p1, *q; // [rows][R] work
+    double *r, *p, *q;       // [rows][R] work
     int32_t *queue;          // next position in `order`
     BatchResult *out;        // [n_systems][R]
     // mixed precision: FP32 inner CG on A32 e = r / ||r||, FP64 refinement
-    float *r32, *p32a, *p32b, *q32, *e32;   // [rows][R]
+    float *r32, *p32, *q32, *e32;   // [rows][R]
     double inner_rtol;
     int32_t max_outer;
 };
@@ -101,47 +126,204 @@ __device__ __forceinline__ void cluster_sum(cgp::cluster_group &cl, double (&v)[
     __syncthreads();
 }
 
-// FP64 residual r = b - A x and ||r||^2 per component over this CTA's rows,
+// Row stride of the gathered search direction p: the R components of a
+// cell padded to 4 when R = 3, so that one gather is one 32-byte (FP64) or
+// 16-byte (FP32) load.  A random gather costs the L1 one wavefront per
+// lane and instruction whatever its width, so fewer, wider gathers are
+// what speeds up the SpMM pass.
+template <int R> constexpr int pad_r() { return R == 3 ? 4 : R; }
+
+// the R components of padded row c of p (L2 only: other CTAs write p)
+template <int R>
+__device__ __forceinline__ void ld_row(const double *p, int64_t c, double (&o)[R])
+{
+    if constexpr (R == 1) {
+        o[0] = __ldcg(p + c);
+    } else if constexpr (R == 2) {
+        const double2 t = __ldcg(reinterpret_cast<const double2 *>(p) + c);
+        o[0] = t.x;
+        o[1] = t.y;
+    } else {
+        double t[4];
+        asm volatile("ld.global.cg.v4.f64 {%0, %1, %2, %3}, [%4];"
+                     : "=d"(t[0]), "=d"(t[1]), "=d"(t[2]), "=d"(t[3])
+                     : "l"(p + 4 * c));
+#pragma unroll
+        for (int j = 0; j < R; ++j) o[j] = t[j];
+    }
+}
+template <int R>
+__device__ __forceinline__ void ld_row(const float *p, int64_t c, float (&o)[R])
+{
+    if constexpr (R == 1) {
+        o[0] = __ldcg(p + c);
+    } else if constexpr (R == 2) {
+        const float2 t = __ldcg(reinterpret_cast<const float2 *>(p) + c);
+        o[0] = t.x;
+        o[1] = t.y;
+    } else {
+        const float4 t = __ldcg(reinterpret_cast<const float4 *>(p) + c);
+        o[0] = t.x;
+        o[1] = t.y;
+        o[2] = t.z;
+        if constexpr (R == 4) o[3] = t.w;
+    }
+}
+template <int R>
+__device__ __forceinline__ void st_row(double *p, int64_t c, const double (&v)[R])
+{
+    if constexpr (R == 1) {
+        p[c] = v[0];
+    } else if constexpr (R == 2) {
+        reinterpret_cast<double2 *>(p)[c] = make_double2(v[0], v[1]);
+    } else {
+        asm volatile("st.global.v4.f64 [%0], {%1, %2, %3, %4};" ::"l"(p + 4 * c), "d"(v[0]), "d"(v[1]),
+                     "d"(v[2]), "d"(R == 4 ? v[R - 1] : 0.0)
+                     : "memory");
+    }
+}
+template <int R>
+__device__ __forceinline__ void st_row(float *p, int64_t c, const float (&v)[R])
+{
+    if constexpr (R == 1) {
+        p[c] = v[0];
+    } else if constexpr (R == 2) {
+        reinterpret_cast<float2 *>(p)[c] = make_float2(v[0], v[1]);
+    } else {
+        reinterpret_cast<float4 *>(p)[c] = make_float4(v[0], v[1], v[2], R == 4 ? v[R - 1] : 0.f);
+    }
+}
+
+// The R-wide product of row `row` (this lane's row of 32-row slice s):
+// y[j] = sum_e a_e g(col_e)[j] over the components j with on[j], where
+// g(c, out) gathers the R components of row c; ys = sum_e a_e.
+// SELL-32: the slice's entries, kBatchEntryBatch loaded (streamed, L2
+// evict-first) before their gathers; CSR: the row's own range.
+template <int R, class V, class T, class G>
+__device__ __forceinline__ void row_product(const BatchSystem &S, const V *__restrict__ sval,
+                                            const V *__restrict__ cval, int s, int row, const bool (&on)[R],
+                                            G g, T (&y)[R], T &ys)
+{
+#pragma unroll
+    for (int j = 0; j < R; ++j) y[j] = T(0);
+    ys = T(0);
+    if (S.sell) {
+        constexpr int B = kBatchEntryBatch;
+#if CF_BATCH_STREAM_HINT
+        const uint64_t pol = l2_evict_first_policy();
+#define CF_BATCH_LD(ptr) ld_stream(ptr, pol)
+#else
+#define CF_BATCH_LD(ptr) __ldg(ptr)
+#endif
+        const int lane = threadIdx.x & 31;
+        const int b = __ldg(S.s_off + s);
+        const int len = (__ldg(S.s_off + s + 1) - b) >> 5;
+        const int32_t *cp = S.s_col + b + lane;
+        const V *vp = sval + b + lane;
+        for (int t0 = 0; t0 < len; t0 += B) {
+            int c[B];
+            V v[B];
+            T xv[B][R];
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (t0 + u < len) {
+                    c[u] = CF_BATCH_LD(cp + 32 * (t0 + u));
+                    v[u] = CF_BATCH_LD(vp + 32 * (t0 + u));
+                }
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (t0 + u < len) g(c[u], xv[u]);
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (t0 + u < len) {
+#pragma unroll
+                    for (int j = 0; j < R; ++j) y[j] = fma_t((T)v[u], on[j] ? xv[u][j] : T(0), y[j]);
+                    ys += (T)v[u];
+                }
+        }
+#undef CF_BATCH_LD
+    } else if (row < S.n) {
+        const int e1 = __ldg(S.ro + row + 1);
+        for (int e = __ldg(S.ro + row); e < e1; ++e) {
+            const T v = (T)__ldg(cval + e);
+            T xv[R];
+            g(__ldg(S.col + e), xv);
+#pragma unroll
+            for (int j = 0; j < R; ++j) y[j] = fma_t(v, on[j] ? xv[j] : T(0), y[j]);
+            ys += v;
+        }
+    }
+}
+
+// Per-component CG state, identical in every CTA of the cluster (each CTA
+// derives it from the same cluster sums).
+template <int R>
+struct CompState {
+    double rho[R], rho_old[R], nrm[R], tol[R], nf[R];
+    double alpha[R];          // step length not yet applied to x (or e)
+    float rho32[R], rho32_old[R], eta[R];
+    int act[R], act_in[R], iters[R];
+};
+
+// FP64 residual r = b - A x and ||r||^2 per component over this CTA's slices,
 // summed over the cluster into tot[0..R)
 template <int R, int BT>
-__device__ __forceinline__ void batch_residual(cgp::cluster_group &cl, int lo, int hi, const int32_t *ro,
-                                               const int32_t *col, const double *val, const double *b,
-                                               const double *x, double *r, double *wsm, double *slot,
-                                               double *tot)
+__device__ __forceinline__ void batch_residual(cgp::cluster_group &cl, const BatchSystem &S, int s_lo, int s_hi,
+                                               const double *b, const double *x, double *r, double *wsm,
+                                               double *slot, double *tot)
 {
+    constexpr int W = BT / 32;
+    const int lane = threadIdx.x & 31;
+    bool on[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) on[j] = true;
     double acc[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) acc[j] = 0.0;
-    for (int i = lo + threadIdx.x; i < hi; i += BT) {
-        double y[R];
+    for (int s = s_lo + (threadIdx.x >> 5); s < s_hi; s += W) {
+        const int row = s * 32 + lane;
+        double y[R], ys;
+        row_product<R, double, double>(S, S.s_val, S.val, s, row, on,
+                                       [&](int c, double(&o)[R]) {
 #pragma unroll
-        for (int j = 0; j < R; ++j) y[j] = 0.0;
-        for (int e = ro[i]; e < ro[i + 1]; ++e) {
-            const double v = val[e];
-            const int64_t c = (int64_t)col[e] * R;
+                                                   for (int j = 0; j < R; ++j) o[j] = __ldcg(x + (int64_t)c * R + j);
+                                               }, y, ys);
+        if (row < S.n)
 #pragma unroll
-            for (int j = 0; j < R; ++j) y[j] = fma_t(v, __ldcg(x + c + j), y[j]);
-        }
-#pragma unroll
-        for (int j = 0; j < R; ++j) {
-            const double ri = b[(int64_t)i * R + j] - y[j];
-            r[(int64_t)i * R + j] = ri;
-            acc[j] = fma_t(ri, ri, acc[j]);
-        }
+            for (int j = 0; j < R; ++j) {
+                const int64_t o = (int64_t)row * R + j;
+                const double ri = b[o] - y[j];
+                r[o] = ri;
+                acc[j] = fma_t(ri, ri, acc[j]);
+            }
     }
     cluster_sum<R, BT>(cl, acc, wsm, slot, tot);
 }
 
+// Minimum CTAs per SM for the register budget (1,024 threads: 64
+// registers).  Measured on the 512-system Poisson batch: occupancy beats
+// deeper entry batching (1 entry at 1,024 threads per SM: 2.20 s; 2 at 768:
+// 2.66 s; 4 at 512: 2.93 s).
+template <int BT> constexpr int batch_min_blocks()
+{
+    return CF_BATCH_THREADS_PER_SM / BT > 0 ? CF_BATCH_THREADS_PER_SM / BT : 1;
+}
+
 template <int R, int BT, bool MIXED>
-__global__ void __launch_bounds__(BT) k_batch_cg(const BatchArgs a)
+__global__ void __launch_bounds__(BT, batch_min_blocks<BT>()) k_batch_cg(const BatchArgs a)
 {
     cgp::cluster_group cl = cgp::this_cluster();
     const int cs = (int)cl.num_blocks();
     const int rank = (int)cl.block_rank();
     constexpr int W = BT / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ double wsm[3 * R * W];
     __shared__ double slot[2][3 * R]; // double-buffered cluster slots
     __shared__ double tot[3 * R];
+    __shared__ CompState<R> st;
+    // the system being solved; its fields are read where they are used, so
+    // that they do not hold registers through the row loops
+    __shared__ BatchSystem S;
     __shared__ int32_t s_next;
     int parity = 0;
 
@@ -152,290 +334,376 @@ __global__ void __launch_bounds__(BT) k_batch_cg(const BatchArgs a)
         cl.sync();
         if (pos >= a.n_systems) break;
         const int sid = a.order[pos];
-        const BatchSystem S = a.sys[sid];
+        if (threadIdx.x == 0) S = a.sys[sid];
+        __syncthreads();
         const int n = S.n;
-        const int lo = (int)((int64_t)n * rank / cs), hi = (int)((int64_t)n * (rank + 1) / cs);
-        const double *b = a.b + S.vec_offset * R;
-        double *x = a.x + S.vec_offset * R;
-        double *r = a.r + S.vec_offset * R;
-        double *q = a.q + S.vec_offset * R;
-        double *pb[2] = {a.p0 + S.vec_offset * R, a.p1 + S.vec_offset * R};
-        const int32_t *ro = S.ro, *col = S.col;
-        const double *val = S.val;
+        const int ns = (n + 31) >> 5;
+        // this CTA's slices; a thread owns rows s * 32 + lane of the slices
+        // s = s_lo + warp + k W in every phase
+        const int s_lo = (int)((int64_t)ns * rank / cs), s_hi = (int)((int64_t)ns * (rank + 1) / cs);
 
         // ---- normFactor part 1: mean of psi per component ----------------
-        double acc1[R];
+        {
+            const double *x = a.x + S.vec_offset * R;
+            double acc1[R];
 #pragma unroll
-        for (int j = 0; j < R; ++j) acc1[j] = 0.0;
-        for (int i = lo + threadIdx.x; i < hi; i += BT)
+            for (int j = 0; j < R; ++j) acc1[j] = 0.0;
+            for (int s = s_lo + warp; s < s_hi; s += W) {
+                const int row = s * 32 + lane;
+                if (row < n)
 #pragma unroll
-            for (int j = 0; j < R; ++j) acc1[j] += x[(int64_t)i * R + j];
-        cluster_sum<R, BT>(cl, acc1, wsm, slot[parity], tot);
-        parity ^= 1;
-        double xbar[R];
-#pragma unroll
-        for (int j = 0; j < R; ++j) xbar[j] = tot[j] / n;
-        __syncthreads();
-
+                    for (int j = 0; j < R; ++j) acc1[j] += x[(int64_t)row * R + j];
+            }
+            cluster_sum<R, BT>(cl, acc1, wsm, slot[parity], tot);
+            parity ^= 1;
+        }
         // ---- normFactor part 2 + initial residual r = b - A x ------------
-        double acc3[3 * R];
+        {
+            const double *x = a.x + S.vec_offset * R, *b = a.b + S.vec_offset * R;
+            double *r = a.r + S.vec_offset * R;
+            double xbar[R];
 #pragma unroll
-        for (int j = 0; j < 3 * R; ++j) acc3[j] = 0.0;
-        for (int i = lo + threadIdx.x; i < hi; i += BT) {
-            double y[R], ys = 0.0;
+            for (int j = 0; j < R; ++j) xbar[j] = tot[j] / n;
+            bool on[R];
 #pragma unroll
-            for (int j = 0; j < R; ++j) y[j] = 0.0;
-            for (int e = ro[i]; e < ro[i + 1]; ++e) {
-                const double v = val[e];
-                const int64_t c = (int64_t)col[e] * R;
+            for (int j = 0; j < R; ++j) on[j] = true;
+            double acc3[3 * R];
 #pragma unroll
-                for (int j = 0; j < R; ++j) y[j] = fma_t(v, __ldcg(x + c + j), y[j]);
-                ys += v;
-            }
+            for (int j = 0; j < 3 * R; ++j) acc3[j] = 0.0;
+            for (int s = s_lo + warp; s < s_hi; s += W) {
+                const int row = s * 32 + lane;
+                double y[R], ys;
+                row_product<R, double, double>(S, S.s_val, S.val, s, row, on,
+                                               [&](int c, double(&o)[R]) {
 #pragma unroll
-            for (int j = 0; j < R; ++j) {
-                const double yb = ys * xbar[j];
-                const double bi = b[(int64_t)i * R + j];
-                const double d1 = y[j] - yb, d2 = bi - yb, ri = bi - y[j];
-                r[(int64_t)i * R + j] = ri;
-                acc3[j] = fma_t(d1, d1, acc3[j]);
-                acc3[R + j] = fma_t(d2, d2, acc3[R + j]);
-                acc3[2 * R + j] = fma_t(ri, ri, acc3[2 * R + j]);
-            }
-        }
-        cluster_sum<3 * R, BT>(cl, acc3, wsm, slot[parity], tot);
-        parity ^= 1;
-        double tolj[R], rho0[R], rho1[R], nrm[R], nf[R];
-        bool active[R];
-        int iters[R];
-        bool any = false;
-#pragma unroll
-        for (int j = 0; j < R; ++j) {
-            nf[j] = sqrt(tot[j]) + sqrt(tot[R + j]) + 1e-20;
-            tolj[j] = a.tolerance * nf[j];
-            rho0[j] = tot[2 * R + j];
-            rho1[j] = 0.0;
-            nrm[j] = sqrt(rho0[j]);
-            active[j] = isfinite(nrm[j]) && nrm[j] > tolj[j] && a.max_iter >= 1;
-            iters[j] = 0;
-            any = any || active[j];
-        }
-        __syncthreads();
-        if (rank == 0 && threadIdx.x < R) {
-            const int j = threadIdx.x;
-            a.out[(int64_t)sid * R + j].nf = nf[j];
-            a.out[(int64_t)sid * R + j].norm0 = nrm[j];
-        }
-
-        // ---- mixed precision: FP32 CG sweeps inside FP64 refinement -----
-        if constexpr (MIXED) {
-            float *r32 = a.r32 + S.vec_offset * R;
-            float *e32 = a.e32 + S.vec_offset * R;
-            float *q32 = a.q32 + S.vec_offset * R;
-            float *pb32[2] = {a.p32a + S.vec_offset * R, a.p32b + S.vec_offset * R};
-            const float *val32 = S.val32;
-            for (int sweep = 0; any && sweep < a.max_outer; ++sweep) {
-                // inner right-hand side r / ||r||, e = 0
-                float inv[R], eta[R];
-                bool act[R];
-                bool any_in = false;
-#pragma unroll
-                for (int j = 0; j < R; ++j) {
-                    act[j] = active[j];
-                    inv[j] = active[j] ? (float)(1.0 / nrm[j]) : 0.f;
-                    // the last sweep only has to reach the FP64 target
-                    eta[j] = (float)fmax(a.inner_rtol, fmin(0.5, 0.8 * tolj[j] / nrm[j]));
-                    any_in = any_in || act[j];
-                }
-                double acc0[R];
-#pragma unroll
-                for (int j = 0; j < R; ++j) acc0[j] = 0.0;
-                for (int i = lo + threadIdx.x; i < hi; i += BT)
+                                                   for (int j = 0; j < R; ++j) o[j] = __ldcg(x + (int64_t)c * R + j);
+                                               },
+                                               y, ys);
+                if (row < n)
 #pragma unroll
                     for (int j = 0; j < R; ++j) {
-                        const int64_t o = (int64_t)i * R + j;
-                        const float v = (float)(r[o] * (double)inv[j]);
-                        r32[o] = v;
-                        e32[o] = 0.f;
-                        acc0[j] += (double)(v * v);
+                        const int64_t o = (int64_t)row * R + j;
+                        const double yb = ys * xbar[j];
+                        const double bi = b[o];
+                        const double d1 = y[j] - yb, d2 = bi - yb, ri = bi - y[j];
+                        r[o] = ri;
+                        acc3[j] = fma_t(d1, d1, acc3[j]);
+                        acc3[R + j] = fma_t(d2, d2, acc3[R + j]);
+                        acc3[2 * R + j] = fma_t(ri, ri, acc3[2 * R + j]);
                     }
-                cluster_sum<R, BT>(cl, acc0, wsm, slot[parity], tot);
-                parity ^= 1;
-                float rho0f[R], rho1f[R];
+            }
+            cluster_sum<3 * R, BT>(cl, acc3, wsm, slot[parity], tot);
+            parity ^= 1;
+        }
+        if (threadIdx.x < R) {
+            const int j = threadIdx.x;
+            st.nf[j] = sqrt(tot[j]) + sqrt(tot[R + j]) + 1e-20;
+            st.tol[j] = a.tolerance * st.nf[j];
+            st.rho[j] = tot[2 * R + j];
+            st.rho_old[j] = 0.0;
+            st.nrm[j] = sqrt(st.rho[j]);
+            st.alpha[j] = 0.0;
+            st.act[j] = isfinite(st.nrm[j]) && st.nrm[j] > st.tol[j] && a.max_iter >= 1;
+            st.iters[j] = 0;
+            if (rank == 0) {
+                a.out[(int64_t)sid * R + j].nf = st.nf[j];
+                a.out[(int64_t)sid * R + j].norm0 = st.nrm[j];
+            }
+        }
+        __syncthreads();
+
+        if constexpr (MIXED) {
+            // ---- FP32 CG sweeps on A e = r / ||r|| inside FP64 refinement ----
+            for (int sweep = 0; sweep < a.max_outer; ++sweep) {
+                bool act[R], any = false;
 #pragma unroll
                 for (int j = 0; j < R; ++j) {
-                    rho0f[j] = (float)tot[j];
-                    rho1f[j] = 0.f;
+                    act[j] = st.act[j];
+                    any = any || act[j];
                 }
-                __syncthreads();
-                int kin = 0;
-                for (int k = 1; any_in; ++k) {
-                    const float *pin = pb32[(k + 1) & 1];
-                    float *pout = pb32[k & 1];
-                    float beta[R];
+                if (!any) break;
+                // inner right-hand side r / ||r||, e = 0, and its squared norm
+                {
+                    const double *r = a.r + S.vec_offset * R;
+                    float *r32 = a.r32 + S.vec_offset * R, *e32 = a.e32 + S.vec_offset * R;
+                    float inv[R];
 #pragma unroll
-                    for (int j = 0; j < R; ++j) beta[j] = (k > 1) ? rho0f[j] / rho1f[j] : 0.f;
-                    double acc[R];
+                    for (int j = 0; j < R; ++j) inv[j] = act[j] ? (float)(1.0 / st.nrm[j]) : 0.f;
+                    double acc0[R];
 #pragma unroll
-                    for (int j = 0; j < R; ++j) acc[j] = 0.0;
-                    for (int i = lo + threadIdx.x; i < hi; i += BT) {
-                        float y[R], part[R];
-#pragma unroll
-                        for (int j = 0; j < R; ++j) y[j] = 0.f;
-                        for (int e = ro[i]; e < ro[i + 1]; ++e) {
-                            const float v = val32[e];
-                            const int64_t c = (int64_t)col[e] * R;
+                    for (int j = 0; j < R; ++j) acc0[j] = 0.0;
+                    for (int s = s_lo + warp; s < s_hi; s += W) {
+                        const int row = s * 32 + lane;
+                        if (row < n)
 #pragma unroll
                             for (int j = 0; j < R; ++j) {
-                                const float pc = (k > 1) ? fma_t(beta[j], __ldcg(pin + c + j), __ldcg(r32 + c + j))
-                                                         : __ldcg(r32 + c + j);
-                                y[j] = fma_t(v, act[j] ? pc : 0.f, y[j]);
+                                const int64_t o = (int64_t)row * R + j;
+                                const float v = (float)(r[o] * (double)inv[j]);
+                                r32[o] = v;
+                                e32[o] = 0.f;
+                                acc0[j] += (double)(v * v);
                             }
-                        }
-#pragma unroll
-                        for (int j = 0; j < R; ++j) {
-                            const int64_t o = (int64_t)i * R + j;
-                            const float pi = (k > 1) ? fma_t(beta[j], __ldcg(pin + o), __ldcg(r32 + o))
-                                                     : __ldcg(r32 + o);
-                            pout[o] = act[j] ? pi : __ldcg(pin + o);
-                            q32[o] = y[j];
-                            part[j] = pi * y[j];
-                            acc[j] += (double)part[j];
-                        }
                     }
-                    cluster_sum<R, BT>(cl, acc, wsm, slot[parity], tot);
+                    cluster_sum<R, BT>(cl, acc0, wsm, slot[parity], tot);
                     parity ^= 1;
-                    float xi[R];
-#pragma unroll
-                    for (int j = 0; j < R; ++j) xi[j] = act[j] ? rho0f[j] / (float)tot[j] : 0.f;
-                    __syncthreads();
-                    double acc2[R];
-#pragma unroll
-                    for (int j = 0; j < R; ++j) acc2[j] = 0.0;
-                    for (int i = lo + threadIdx.x; i < hi; i += BT) {
-#pragma unroll
-                        for (int j = 0; j < R; ++j) {
-                            const int64_t o = (int64_t)i * R + j;
-                            if (act[j]) {
-                                e32[o] = fma_t(xi[j], pout[o], e32[o]);
-                                const float ri = fma_t(-xi[j], q32[o], r32[o]);
-                                r32[o] = ri;
-                                acc2[j] += (double)(ri * ri);
-                            }
-                        }
-                    }
-                    cluster_sum<R, BT>(cl, acc2, wsm, slot[parity], tot);
-                    parity ^= 1;
-                    any_in = false;
+                }
+                if (threadIdx.x < R) {
+                    const int j = threadIdx.x;
+                    st.rho32[j] = (float)tot[j];
+                    st.rho32_old[j] = 0.f;
+                    st.alpha[j] = 0.0;
+                    st.act_in[j] = st.act[j];
+                    // the last sweep only has to reach the FP64 target
+                    st.eta[j] = (float)fmax(a.inner_rtol, fmin(0.5, 0.8 * st.tol[j] / st.nrm[j]));
+                }
+                __syncthreads();
+                for (int k = 1;; ++k) {
+                    bool ain[R], any_in = false;
 #pragma unroll
                     for (int j = 0; j < R; ++j) {
-                        if (act[j]) {
-                            rho1f[j] = rho0f[j];
-                            rho0f[j] = (float)tot[j];
-                            iters[j] += 1;
-                            const float nin = sqrtf(rho0f[j]);
-                            act[j] = isfinite(nin) && nin > eta[j] && iters[j] < a.max_iter;
-                        }
-                        any_in = any_in || act[j];
+                        ain[j] = st.act_in[j];
+                        any_in = any_in || ain[j];
                     }
-                    kin = k;
+                    // P: e += alpha_{k-1} p (deferred), p = r + beta p
+                    {
+                        float beta[R], pend[R];
+#pragma unroll
+                        for (int j = 0; j < R; ++j) {
+                            beta[j] = (k > 1 && ain[j]) ? st.rho32[j] / st.rho32_old[j] : 0.f;
+                            pend[j] = (float)st.alpha[j];
+                        }
+                        const float *r32 = a.r32 + S.vec_offset * R;
+                        float *p32 = a.p32 + S.vec_offset * pad_r<R>(), *e32 = a.e32 + S.vec_offset * R;
+                        for (int s = s_lo + warp; s < s_hi; s += W) {
+                            const int row = s * 32 + lane;
+                            if (row < n) {
+                                float pv[R];
+                                if (k > 1) ld_row<R>(p32, row, pv);
+#pragma unroll
+                                for (int j = 0; j < R; ++j) {
+                                    const int64_t o = (int64_t)row * R + j;
+                                    if (k == 1) {
+                                        pv[j] = ain[j] ? r32[o] : 0.f;
+                                    } else {
+                                        if (pend[j] != 0.f) e32[o] = fma_t(pend[j], pv[j], e32[o]);
+                                        if (ain[j]) pv[j] = fma_t(beta[j], pv[j], r32[o]);
+                                    }
+                                }
+                                st_row<R>(p32, row, pv);
+                            }
+                        }
+                    }
+                    if (!any_in) break;
+                    cl.sync(); // p complete before any CTA gathers it
+                    // A: q = A p, (p, q)
+                    {
+                        const float *p32 = a.p32 + S.vec_offset * pad_r<R>();
+                        float *q32 = a.q32 + S.vec_offset * R;
+                        float accf[R];
+#pragma unroll
+                        for (int j = 0; j < R; ++j) accf[j] = 0.f;
+                        for (int s = s_lo + warp; s < s_hi; s += W) {
+                            const int row = s * 32 + lane;
+                            float y[R], ys;
+                            row_product<R, float, float>(
+                                S, S.s_val32, S.val32, s, row, ain,
+                                [&](int c, float(&o)[R]) { ld_row<R>(p32, c, o); }, y, ys);
+                            if (row < n) {
+                                float pv[R];
+                                ld_row<R>(p32, row, pv);
+#pragma unroll
+                                for (int j = 0; j < R; ++j)
+                                    if (ain[j]) {
+                                        q32[(int64_t)row * R + j] = y[j];
+                                        accf[j] = fma_t(pv[j], y[j], accf[j]);
+                                    }
+                            }
+                        }
+                        double acc[R];
+#pragma unroll
+                        for (int j = 0; j < R; ++j) acc[j] = accf[j];
+                        cluster_sum<R, BT>(cl, acc, wsm, slot[parity], tot);
+                        parity ^= 1;
+                    }
+                    // B: r -= alpha q, (r, r)
+                    {
+                        float alpha[R];
+#pragma unroll
+                        for (int j = 0; j < R; ++j) alpha[j] = ain[j] ? st.rho32[j] / (float)tot[j] : 0.f;
+                        const float *q32 = a.q32 + S.vec_offset * R;
+                        float *r32 = a.r32 + S.vec_offset * R;
+                        float accf[R];
+#pragma unroll
+                        for (int j = 0; j < R; ++j) accf[j] = 0.f;
+                        for (int s = s_lo + warp; s < s_hi; s += W) {
+                            const int row = s * 32 + lane;
+                            if (row < n)
+#pragma unroll
+                                for (int j = 0; j < R; ++j)
+                                    if (ain[j]) {
+                                        const int64_t o = (int64_t)row * R + j;
+                                        const float ri = fma_t(-alpha[j], q32[o], r32[o]);
+                                        r32[o] = ri;
+                                        accf[j] = fma_t(ri, ri, accf[j]);
+                                    }
+                        }
+                        double acc2[R];
+#pragma unroll
+                        for (int j = 0; j < R; ++j) acc2[j] = accf[j];
+                        if (threadIdx.x < R) st.alpha[threadIdx.x] = alpha[threadIdx.x];
+                        cluster_sum<R, BT>(cl, acc2, wsm, slot[parity], tot);
+                        parity ^= 1;
+                    }
+                    if (threadIdx.x < R) {
+                        const int j = threadIdx.x;
+                        if (st.act_in[j]) {
+                            st.rho32_old[j] = st.rho32[j];
+                            st.rho32[j] = (float)tot[j];
+                            st.iters[j] += 1;
+                            const float nin = sqrtf(st.rho32[j]);
+                            st.act_in[j] = isfinite(nin) && nin > st.eta[j] && st.iters[j] < a.max_iter;
+                        } else {
+                            st.alpha[j] = 0.0;
+                        }
+                    }
                     __syncthreads();
                 }
-                (void)kin;
-                // x += ||r|| e in FP64, then the FP64 residual
-                for (int i = lo + threadIdx.x; i < hi; i += BT)
+                // the inner loop ended with a P pass that applied every
+                // pending step to e: x += ||r|| e in FP64
+                {
+                    const float *e32 = a.e32 + S.vec_offset * R;
+                    double *x = a.x + S.vec_offset * R;
+                    for (int s = s_lo + warp; s < s_hi; s += W) {
+                        const int row = s * 32 + lane;
+                        if (row < n)
 #pragma unroll
-                    for (int j = 0; j < R; ++j) {
-                        const int64_t o = (int64_t)i * R + j;
-                        if (active[j]) x[o] = fma_t(nrm[j], (double)e32[o], x[o]);
+                            for (int j = 0; j < R; ++j)
+                                if (act[j]) {
+                                    const int64_t o = (int64_t)row * R + j;
+                                    x[o] = fma_t(st.nrm[j], (double)e32[o], x[o]);
+                                }
                     }
+                }
                 cl.sync(); // every CTA's x rows are written before anyone gathers them
-                batch_residual<R, BT>(cl, lo, hi, ro, col, val, b, x, r, wsm, slot[parity], tot);
+                batch_residual<R, BT>(cl, S, s_lo, s_hi, a.b + S.vec_offset * R, a.x + S.vec_offset * R,
+                                      a.r + S.vec_offset * R, wsm, slot[parity], tot);
                 parity ^= 1;
-                any = false;
-#pragma unroll
-                for (int j = 0; j < R; ++j) {
-                    if (active[j]) {
+                if (threadIdx.x < R) {
+                    const int j = threadIdx.x;
+                    if (st.act[j]) {
                         const double nn = sqrt(tot[j]);
                         // a sweep that does not reduce the FP64 residual ends the solve
-                        const bool progress = nn < nrm[j];
-                        nrm[j] = nn;
-                        active[j] = isfinite(nn) && nn > tolj[j] && progress && iters[j] < a.max_iter;
+                        const bool progress = nn < st.nrm[j];
+                        st.nrm[j] = nn;
+                        st.act[j] = isfinite(nn) && nn > st.tol[j] && progress && st.iters[j] < a.max_iter;
                     }
-                    any = any || active[j];
                 }
                 __syncthreads();
             }
         } else {
             // ---- CG iterations, all components together ----------------------
-            for (int k = 1; any && k <= a.max_iter; ++k) {
-                const double *pin = pb[(k + 1) & 1];
-                double *pout = pb[k & 1];
-                double beta[R];
-    #pragma unroll
-                for (int j = 0; j < R; ++j) beta[j] = (k > 1) ? rho0[j] / rho1[j] : 0.0;
-                // phase A: p = r + beta p_old (on the fly), q = A p, (p, q)
-                double acc[R];
-    #pragma unroll
-                for (int j = 0; j < R; ++j) acc[j] = 0.0;
-                for (int i = lo + threadIdx.x; i < hi; i += BT) {
-                    double y[R];
-    #pragma unroll
-                    for (int j = 0; j < R; ++j) y[j] = 0.0;
-                    for (int e = ro[i]; e < ro[i + 1]; ++e) {
-                        const double v = val[e];
-                        const int64_t c = (int64_t)col[e] * R;
-    #pragma unroll
-                        for (int j = 0; j < R; ++j) {
-                            const double pc = (k > 1) ? fma_t(beta[j], __ldcg(pin + c + j), __ldcg(r + c + j))
-                                                      : __ldcg(r + c + j);
-                            y[j] = fma_t(v, active[j] ? pc : 0.0, y[j]);
-                        }
-                    }
-    #pragma unroll
-                    for (int j = 0; j < R; ++j) {
-                        const int64_t o = (int64_t)i * R + j;
-                        const double pi = (k > 1) ? fma_t(beta[j], __ldcg(pin + o), __ldcg(r + o)) : __ldcg(r + o);
-                        pout[o] = active[j] ? pi : __ldcg(pin + o);
-                        q[o] = y[j];
-                        acc[j] = fma_t(pi, y[j], acc[j]);
-                    }
-                }
-                cluster_sum<R, BT>(cl, acc, wsm, slot[parity], tot);
-                parity ^= 1;
-                double xi[R];
-    #pragma unroll
-                for (int j = 0; j < R; ++j) xi[j] = active[j] ? rho0[j] / tot[j] : 0.0;
-                __syncthreads();
-                // phase B: x += xi p, r -= xi q, (r, r)
-                double acc2[R];
-    #pragma unroll
-                for (int j = 0; j < R; ++j) acc2[j] = 0.0;
-                for (int i = lo + threadIdx.x; i < hi; i += BT) {
-    #pragma unroll
-                    for (int j = 0; j < R; ++j) {
-                        const int64_t o = (int64_t)i * R + j;
-                        if (active[j]) {
-                            x[o] = fma_t(xi[j], pout[o], x[o]);
-                            const double ri = fma_t(-xi[j], q[o], r[o]);
-                            r[o] = ri;
-                            acc2[j] = fma_t(ri, ri, acc2[j]);
-                        }
-                    }
-                }
-                cluster_sum<R, BT>(cl, acc2, wsm, slot[parity], tot);
-                parity ^= 1;
-                any = false;
-    #pragma unroll
+            for (int k = 1;; ++k) {
+                bool act[R], any = false;
+#pragma unroll
                 for (int j = 0; j < R; ++j) {
-                    if (active[j]) {
-                        rho1[j] = rho0[j];
-                        rho0[j] = tot[j];
-                        nrm[j] = sqrt(rho0[j]);
-                        iters[j] = k;
-                        active[j] = isfinite(nrm[j]) && k < a.max_iter && nrm[j] > tolj[j];
+                    act[j] = st.act[j];
+                    any = any || act[j];
+                }
+                // P: x += alpha_{k-1} p (deferred), p = r + beta p
+                {
+                    double beta[R], pend[R];
+#pragma unroll
+                    for (int j = 0; j < R; ++j) {
+                        beta[j] = (k > 1 && act[j]) ? st.rho[j] / st.rho_old[j] : 0.0;
+                        pend[j] = st.alpha[j];
                     }
-                    any = any || active[j];
+                    const double *r = a.r + S.vec_offset * R;
+                    double *p = a.p + S.vec_offset * pad_r<R>(), *x = a.x + S.vec_offset * R;
+                    for (int s = s_lo + warp; s < s_hi; s += W) {
+                        const int row = s * 32 + lane;
+                        if (row < n) {
+                            double pv[R];
+                            if (k > 1) ld_row<R>(p, row, pv);
+#pragma unroll
+                            for (int j = 0; j < R; ++j) {
+                                const int64_t o = (int64_t)row * R + j;
+                                if (k == 1) {
+                                    pv[j] = act[j] ? r[o] : 0.0;
+                                } else {
+                                    if (pend[j] != 0.0) x[o] = fma_t(pend[j], pv[j], x[o]);
+                                    if (act[j]) pv[j] = fma_t(beta[j], pv[j], r[o]);
+                                }
+                            }
+                            st_row<R>(p, row, pv);
+                        }
+                    }
+                }
+                if (!any) break;
+                cl.sync(); // p complete before any CTA gathers it
+                // A: q = A p, (p, q)
+                {
+                    const double *p = a.p + S.vec_offset * pad_r<R>();
+                    double *q = a.q + S.vec_offset * R;
+                    double acc[R];
+#pragma unroll
+                    for (int j = 0; j < R; ++j) acc[j] = 0.0;
+                    for (int s = s_lo + warp; s < s_hi; s += W) {
+                        const int row = s * 32 + lane;
+                        double y[R], ys;
+                        row_product<R, double, double>(
+                            S, S.s_val, S.val, s, row, act,
+                            [&](int c, double(&o)[R]) { ld_row<R>(p, c, o); }, y, ys);
+                        if (row < n) {
+                            double pv[R];
+                            ld_row<R>(p, row, pv);
+#pragma unroll
+                            for (int j = 0; j < R; ++j)
+                                if (act[j]) {
+                                    q[(int64_t)row * R + j] = y[j];
+                                    acc[j] = fma_t(pv[j], y[j], acc[j]);
+                                }
+                        }
+                    }
+                    cluster_sum<R, BT>(cl, acc, wsm, slot[parity], tot);
+                    parity ^= 1;
+                }
+                // B: r -= alpha q, (r, r)
+                {
+                    double alpha[R];
+#pragma unroll
+                    for (int j = 0; j < R; ++j) alpha[j] = act[j] ? st.rho[j] / tot[j] : 0.0;
+                    const double *q = a.q + S.vec_offset * R;
+                    double *r = a.r + S.vec_offset * R;
+                    double acc2[R];
+#pragma unroll
+                    for (int j = 0; j < R; ++j) acc2[j] = 0.0;
+                    for (int s = s_lo + warp; s < s_hi; s += W) {
+                        const int row = s * 32 + lane;
+                        if (row < n)
+#pragma unroll
+                            for (int j = 0; j < R; ++j)
+                                if (act[j]) {
+                                    const int64_t o = (int64_t)row * R + j;
+                                    const double ri = fma_t(-alpha[j], q[o], r[o]);
+                                    r[o] = ri;
+                                    acc2[j] = fma_t(ri, ri, acc2[j]);
+                                }
+                    }
+                    if (threadIdx.x < R) st.alpha[threadIdx.x] = alpha[threadIdx.x];
+                    cluster_sum<R, BT>(cl, acc2, wsm, slot[parity], tot);
+                    parity ^= 1;
+                }
+                if (threadIdx.x < R) {
+                    const int j = threadIdx.x;
+                    if (st.act[j]) {
+                        st.rho_old[j] = st.rho[j];
+                        st.rho[j] = tot[j];
+                        st.nrm[j] = sqrt(st.rho[j]);
+                        st.iters[j] = k;
+                        st.act[j] = isfinite(st.nrm[j]) && k < a.max_iter && st.nrm[j] > st.tol[j];
+                    } else {
+                        st.alpha[j] = 0.0;
+                    }
                 }
                 __syncthreads();
             }
@@ -443,10 +711,11 @@ __global__ void __launch_bounds__(BT) k_batch_cg(const BatchArgs a)
         if (rank == 0 && threadIdx.x < R) {
             const int j = threadIdx.x;
             BatchResult &o = a.out[(int64_t)sid * R + j];
-            o.norm = nrm[j];
-            o.iters = iters[j];
-            o.status = !isfinite(nrm[j]) ? CF_NONFINITE : (nrm[j] > tolj[j] ? CF_NOT_CONVERGED : CF_OK);
+            o.norm = st.nrm[j];
+            o.iters = st.iters[j];
+            o.status = !isfinite(st.nrm[j]) ? CF_NONFINITE : (st.nrm[j] > st.tol[j] ? CF_NOT_CONVERGED : CF_OK);
         }
+        __syncthreads();
     }
     cl.sync(); // no CTA leaves while a peer may still read its shared memory
 }
@@ -459,8 +728,8 @@ struct Batch {
     std::vector<Matrix *> mats;
     std::vector<int64_t> offsets;   // first row of each system
     int64_t rows = 0;
-    DeviceBuffer d_sys, d_order, d_queue, d_out, d_b, d_x, d_r, d_p0, d_p1, d_q;
-    DeviceBuffer d_r32, d_p32a, d_p32b, d_q32, d_e32;
+    DeviceBuffer d_sys, d_order, d_queue, d_out, d_b, d_x, d_r, d_p, d_q;
+    DeviceBuffer d_r32, d_p32, d_q32, d_e32;
     bool have_32 = false;
     std::vector<int32_t> order;
     ~Batch()
@@ -485,6 +754,13 @@ Batch *batch_create(Context *ctx, int n_systems, const cf_ldu_view *views)
             hs[s].ro = m->ro.as<int32_t>();
             hs[s].col = m->col.as<int32_t>();
             hs[s].val = m->val.as<double>();
+            hs[s].val32 = nullptr;
+            // the SELL-32 copy, unless the rows are too uneven for it
+            hs[s].sell = matrix_ensure_sell(m, false, false) ? 1 : 0;
+            hs[s].s_off = hs[s].sell ? m->s_off.as<int32_t>() : nullptr;
+            hs[s].s_col = hs[s].sell ? m->s_col.as<int32_t>() : nullptr;
+            hs[s].s_val = hs[s].sell ? m->s_val.as<double>() : nullptr;
+            hs[s].s_val32 = nullptr;
             B->offsets.push_back(B->rows);
             B->rows += m->n;
         }
@@ -515,7 +791,6 @@ static void launch_batch(Context *ctx, const BatchArgs &args, int cs, int max_cl
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = cs;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.blockDim = dim3(BT);
@@ -523,13 +798,27 @@ static void launch_batch(Context *ctx, const BatchArgs &args, int cs, int max_cl
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    const auto kernel = k_batch_cg<R, BT, MIXED>;
+    // cs == 0: 16-CTA clusters where they fit on the device, else 8
+    const bool pick = cs == 0;
     int nclusters = 0;
-    cfg.gridDim = dim3(cs);
-    CF_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, (void *)k_batch_cg<R, BT, MIXED>, &cfg));
-    if (nclusters < 1) nclusters = 1;
+    for (int c = pick ? 16 : cs; c >= (pick ? 8 : cs); c /= 2) {
+        if (c > 8) // 16-CTA clusters are beyond the portable limit of 8
+            CF_CUDA(cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        attr[0].val.clusterDim.x = c;
+        cfg.gridDim = dim3(c);
+        nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, (void *)kernel, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            nclusters = 0;
+        }
+        cs = c;
+        if (nclusters >= 1) break;
+    }
+    require(nclusters >= 1, CF_UNSUPPORTED, "no cluster of this size and block size fits on the device");
     if (max_clusters > 0 && nclusters > max_clusters) nclusters = max_clusters;
     cfg.gridDim = dim3(nclusters * cs);
-    CF_CUDA(cudaLaunchKernelEx(&cfg, k_batch_cg<R, BT, MIXED>, args));
+    CF_CUDA(cudaLaunchKernelEx(&cfg, kernel, args));
 }
 
 template <int R, bool MIXED>
@@ -563,8 +852,13 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
         std::vector<BatchSystem> hs(S);
         CF_CUDA(cudaMemcpy(hs.data(), B->d_sys.ptr, sizeof(BatchSystem) * S, cudaMemcpyDeviceToHost));
         for (int s2 = 0; s2 < S; ++s2) {
-            matrix_ensure_fp32(B->mats[s2], false);
-            hs[s2].val32 = B->mats[s2]->val32.as<float>();
+            Matrix *m = B->mats[s2];
+            matrix_ensure_fp32(m, false);
+            hs[s2].val32 = m->val32.as<float>();
+            if (hs[s2].sell) {
+                matrix_ensure_sell(m, false, true);
+                hs[s2].s_val32 = m->s_val32.as<float>();
+            }
         }
         CF_CUDA(cudaMemcpyAsync(B->d_sys.ptr, hs.data(), sizeof(BatchSystem) * S, cudaMemcpyHostToDevice,
                                 ctx->stream));
@@ -574,15 +868,13 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
     if (mixed) {
         const size_t fb = sizeof(float) * (size_t)(B->rows * nrhs + 8);
         B->d_r32.ensure(fb);
-        B->d_p32a.ensure(fb);
-        B->d_p32b.ensure(fb);
+        B->d_p32.ensure(sizeof(float) * (size_t)(B->rows * 4 + 8));   // rows padded to 4 components
         B->d_q32.ensure(fb);
         B->d_e32.ensure(fb);
     }
     const size_t vb = sizeof(double) * (size_t)(B->rows * nrhs + 8);
     B->d_r.ensure(vb);
-    B->d_p0.ensure(vb);
-    B->d_p1.ensure(vb);
+    B->d_p.ensure(sizeof(double) * (size_t)(B->rows * 4 + 8));   // rows padded to 4 components
     B->d_q.ensure(vb);
     double *x, *b;
     if (memory == CF_MEM_HOST) {
@@ -612,22 +904,21 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
     a.b = b;
     a.x = x;
     a.r = B->d_r.as<double>();
-    a.p0 = B->d_p0.as<double>();
-    a.p1 = B->d_p1.as<double>();
+    a.p = B->d_p.as<double>();
     a.q = B->d_q.as<double>();
     a.queue = B->d_queue.as<int32_t>();
     a.out = B->d_out.as<BatchResult>();
     a.r32 = mixed ? B->d_r32.as<float>() : nullptr;
-    a.p32a = mixed ? B->d_p32a.as<float>() : nullptr;
-    a.p32b = mixed ? B->d_p32b.as<float>() : nullptr;
+    a.p32 = mixed ? B->d_p32.as<float>() : nullptr;
     a.q32 = mixed ? B->d_q32.as<float>() : nullptr;
     a.e32 = mixed ? B->d_e32.as<float>() : nullptr;
     a.inner_rtol = (c.mixed_inner_rtol > 0 && c.mixed_inner_rtol < 1) ? c.mixed_inner_rtol : 1e-4;
     a.max_outer = c.mixed_max_outer > 0 ? c.mixed_max_outer : 50;
-    const int cs = cfg && cfg->cluster_size > 0 ? cfg->cluster_size : 4;
+    const int cs = cfg && cfg->cluster_size > 0 ? cfg->cluster_size : 0;   // 0: 16, else 8
     const int bt = cfg && cfg->threads > 0 ? cfg->threads : 256;
     const int maxc = cfg ? cfg->max_clusters : 0;
-    require(cs == 1 || cs == 2 || cs == 4 || cs == 8, CF_BAD_INPUT, "cluster size must be 1, 2, 4 or 8");
+    require(cs == 0 || cs == 1 || cs == 2 || cs == 4 || cs == 8 || cs == 16, CF_BAD_INPUT,
+            "cluster size must be 1, 2, 4, 8 or 16");
     require(bt == 128 || bt == 256 || bt == 512, CF_BAD_INPUT, "threads must be 128, 256 or 512");
 
     // one persistent launch, captured in a CUDA graph together with the

@@ -311,7 +311,8 @@ const char *cf_file_last_error(void);
 typedef struct cf_batch cf_batch;
 
 typedef struct cf_batch_config {
-    int32_t cluster_size;   /* CTAs cooperating on one system: 1, 2, 4, 8 (0 = 4) */
+    int32_t cluster_size;   /* CTAs cooperating on one system: 1, 2, 4, 8, 16 (0 = 16 where it
+                               fits on the device, else 8) */
     int32_t threads;        /* threads per CTA: 128, 256, 512 (0 = 256) */
     int32_t order;          /* 0 = largest system first, 1 = given order */
     int32_t max_clusters;   /* 0 = one full wave */
@@ -335,7 +336,8 @@ cf_status cf_batch_shape(const cf_batch *b, int32_t *n_systems, int64_t *total_r
                          int64_t *row_offsets);
 /* sources / psi: [total_rows][n_rhs] (the n_rhs components of a cell are
  * adjacent), psi updated in place; results[n_systems * n_rhs].  solver must
- * be CF_CG and controls->precision CF_PREC_FP64. */
+ * be CF_CG; controls->precision CF_PREC_FP64, or CF_PREC_MIXED for FP32 CG
+ * sweeps inside FP64 refinement (controls->mixed_inner_rtol, mixed_max_outer). */
 cf_status cf_batch_solve(cf_batch *b, int32_t solver, const cf_controls *controls,
                          const cf_batch_config *config, int32_t n_rhs, const double *sources,
                          double *psi, cf_batch_result *results, double *device_ms);

@@ -1,6 +1,7 @@
 """Batched persistent-cluster CG: every (system, right-hand side) pair must
 match an independent FP64 solve of the same system (iteration count within
-one, final relative residual within 1e-12, true residual at tolerance)."""
+two, normFactor and initial residual to rounding, true residual at
+tolerance)."""
 import numpy as np
 import pytest
 
@@ -29,10 +30,12 @@ def test_batched_matches_independent_solves(ctx, config):
         for j in range(3):
             res = results[s * 3 + j]
             want = O.plugin_solve(O.CG, L, rhs[s][j], np.zeros(L.n), tol, maxit)
-            # a different summation order than the oracle: same iteration
-            # count within one, both at the tolerance, same normFactor and
-            # initial residual to rounding, true residual at the tolerance
-            assert abs(res["n_iterations"] - want.n_iterations) <= 1, (s, j)
+            # a different summation order than the oracle: iteration count
+            # within two (CG on system 2, component 2 of this batch takes
+            # 82, 83 or 84 steps over 30 random orders of its dot-product
+            # sums in plain numpy), both at the tolerance, same normFactor
+            # and initial residual to rounding, true residual at the tolerance
+            assert abs(res["n_iterations"] - want.n_iterations) <= 2, (s, j)
             assert res["status"] == 0 and res["final_residual"] <= tol
             assert abs(res["norm_factor"] - want.norm_factor) <= 1e-13 * want.norm_factor
             assert abs(res["initial_residual"] - want.initial_residual) <= 1e-13
