@@ -10,10 +10,12 @@ A step is one complete solve.  `value` is the solve's algorithmic HBM
 traffic (bytes every kernel of the fused schedule must move, see
 `solve_bytes`) divided by the device time, with the matrix and vectors
 resident in HBM (inputs exceed L2, so no flush is needed).  `e2e` is the
-same metric through the public API with host buffers: every step uploads
-the LDU matrix from pinned host memory, converts it on the device,
-solves with host psi/source and reads psi back (what a cuFoamCG::solve call
-does).  `--impl reference` times the CPU restatement of the reference's CG
+same metric through the public API with host buffers, as the plugin runs a
+time step on a mesh it has seen: every step uploads the new LDU
+coefficients from pinned host memory into the cached device matrix
+(refreshing its CSR and SELL-32 values on the device), solves with host
+psi/source and reads psi back; `e2e.first_call` adds the addressing upload
+and the device ldu2csr / SELL-32 build of a new mesh.  `--impl reference` times the CPU restatement of the reference's CG
 (the oracle, all host threads) on bounded samples of the same workload.
 """
 from __future__ import annotations
@@ -285,20 +287,36 @@ def run_ours(args):
     launches = sum(5 + 3 * k for k in its)  # nf_sum, nf_dist, res_init, 3/iter, flush, clear
 
     # ---- e2e through the public API with pinned host buffers -------------
+    # What the plugin does per cuFoamCG::solve in a running case (its device
+    # matrix is cached per mesh addressing, plugin/cuFoamGB300.C
+    # deviceMatrix()): upload the new coefficients, upload source and psi,
+    # solve, download psi.  The first call on a mesh also uploads the
+    # addressing and builds the CSR and SELL-32 copies: timed separately
+    # as `first_call`.
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     h = {k: pin(getattr(L, k)) for k in ("diag", "lower", "upper", "lower_addr", "upper_addr")}
     hb = pin(b)
     hpsi = pin(np.zeros(n))
-    h2d = sum(v.nbytes for v in h.values()) + hb.nbytes + hpsi.nbytes
+    h2d_first = sum(v.nbytes for v in h.values()) + hb.nbytes + hpsi.nbytes
+    h2d = h["diag"].nbytes + h["lower"].nbytes + h["upper"].nbytes + hb.nbytes + hpsi.nbytes
     d2h = hpsi.nbytes
+    ctrl = {"tolerance": TOL, "maxIter": MAX_ITER}
 
-    def e2e_step():
+    def first_call():
         hpsi[:] = 0.0
         m = cf.LduMatrix(L.n, h["diag"], h["lower"], h["upper"], h["lower_addr"],
                          h["upper_addr"], context=ctx)
-        p = cf.cuFoamCG("p", m, {"tolerance": TOL, "maxIter": MAX_ITER}).solve(hpsi, hb)
+        p = cf.cuFoamCG("p", m, ctrl).solve(hpsi, hb)
         m.close()
         return p
+
+    m_e2e = cf.LduMatrix(L.n, h["diag"], h["lower"], h["upper"], h["lower_addr"], h["upper_addr"],
+                         context=ctx)
+
+    def e2e_step():
+        hpsi[:] = 0.0
+        m_e2e.update_values(h["diag"], h["lower"], h["upper"])
+        return cf.cuFoamCG("p", m_e2e, ctrl).solve(hpsi, hb)
 
     for _ in range(2):
         e2e_step()
@@ -312,6 +330,11 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e_dt = float(t.item())
     e2e_value = sum(solve_bytes(mat_it, mat_csr, n, k) for k in e_its) * world / e_dt / 1e9
+    first_call()
+    t0 = time.perf_counter()
+    f_its = first_call().n_iterations
+    f_dt = time.perf_counter() - t0
+    m_e2e.close()
 
     # ---- dominant kernel: per-launch time with CUDA events (profiled solve)
     psi.zero_()
@@ -379,7 +402,13 @@ def run_ours(args):
         "csr_equivalent_gbs": round(csr_equiv / (ms * 1e-3) / 1e9, 2),
         "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
-                "ms_per_step": round(1e3 * e_dt / len(e_its), 3)},
+                "ms_per_step": round(1e3 * e_dt / len(e_its), 3),
+                "path": "cuFoamCG.solve with host arrays on the cached device matrix: "
+                        "coefficient, source and psi upload, solve, psi download",
+                "first_call": {"ms": round(1e3 * f_dt, 3), "h2d_bytes": int(h2d_first),
+                               "value": round(solve_bytes(mat_it, mat_csr, n, f_its) / f_dt / 1e9, 2),
+                               "path": "a new mesh: addressing upload, device ldu2csr and "
+                                       "SELL-32 build, then the solve"}},
         "roofline": {"bound": "hbm", "kernel": "k_f_cg_spmv", "achieved": round(k1_gbs, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(k1_gbs / peak, 4),
                      "peak_source": peak_kind,

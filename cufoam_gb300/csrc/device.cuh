@@ -127,14 +127,38 @@ __device__ __forceinline__ bool grid_reduce(T (&acc)[NV], T *partials, int strid
     __threadfence();
     const int G = gridDim.x;
     if (ref_order) {
-        if (threadIdx.x == 0) {
+        // the partials in block order, one sequential sum per value; the
+        // whole block stages them through shared memory a chunk at a time
+        // so that thread 0 adds from shared memory instead of waiting on
+        // one L2 load per partial
+        T run[NV];
 #pragma unroll
-            for (int i = 0; i < NV; ++i) {
-                T s = T(0);
-                for (int b = 0; b < G; ++b) s += ld_cg(partials + i * stride + b);
-                out[i] = s;
+        for (int i = 0; i < NV; ++i) run[i] = T(0);
+        for (int b0 = 0; b0 < G; b0 += kBlock) {
+            const int m = min(kBlock, G - b0);
+            __syncthreads(); // the previous chunk (or the block sum) is consumed
+            if (threadIdx.x < m)
+#pragma unroll
+                for (int i = 0; i < NV; ++i) sm[i * kBlock + threadIdx.x] = ld_cg(partials + i * stride + b0 + threadIdx.x);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                if (m == kBlock) {
+                    // a full chunk: a fixed trip count lets the shared
+                    // loads run ahead of the dependent additions
+#pragma unroll 32
+                    for (int b = 0; b < kBlock; ++b)
+#pragma unroll
+                        for (int i = 0; i < NV; ++i) run[i] += sm[i * kBlock + b];
+                } else {
+                    for (int b = 0; b < m; ++b)
+#pragma unroll
+                        for (int i = 0; i < NV; ++i) run[i] += sm[i * kBlock + b];
+                }
             }
         }
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int i = 0; i < NV; ++i) out[i] = run[i];
     } else {
         T v[NV];
 #pragma unroll

@@ -12,8 +12,10 @@ see ``oracle.h``) with numpy helpers, and exposes the reference's own
 ``gis/ldu2csr.h`` compiled from source (``oracle/_ref``) where available.
 
 Parity status: ldu2csr pinned to the reference's own code; the solver
-restatement is parity unpinned (no reference tests or runnable reference
-solver exist for it) and is cross-checked against direct solves instead.
+restatement's arithmetic is pinned on the GPU by running the same drivers
+through the reference's own kernels (``reference_kernels()``, used by
+``tests/test_gpu_refgpu.py``); it is also cross-checked against direct
+solves.
 """
 from __future__ import annotations
 
@@ -78,12 +80,63 @@ def lib():
         L.orc_true_residual_norm.argtypes = [C.POINTER(_Csr), _dp, _dp]
         L.orc_norm_factor.restype = C.c_double
         L.orc_norm_factor.argtypes = [C.POINTER(_Csr), _dp, _dp, C.c_int32]
+        L.orc_set_backend.argtypes = [C.c_void_p]
         L.orc_solve.restype = C.c_int32
         L.orc_solve.argtypes = [C.c_int32, C.POINTER(_Csr), C.POINTER(_Csr), _dp, _dp,
                                 C.c_double, C.c_int32, C.c_int32, C.c_double, C.c_double,
                                 C.c_int32, _dp, C.c_int32, C.POINTER(_Res)]
         _lib = L
     return _lib
+
+
+class reference_kernels:
+    """Within this context the oracle's drivers run on the reference's own
+    device kernels (gis/SparseSystem/kernels.h compiled into
+    oracle/_ref/ref_kernels.cubin) launched on `device`, instead of on the
+    CPU emulation of their arithmetic.  Needs a GPU and the cubin."""
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self._g = None
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(_build.REF_CUBIN) and os.path.exists(_build.REF_CUBIN_NAMES)
+
+    def __enter__(self):
+        g = C.CDLL(_build.build_refgpu())
+        g.rg_open.restype = C.c_int
+        g.rg_open.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
+        g.rg_backend.restype = C.c_void_p
+        g.rg_grid.restype = C.c_int
+        g.rg_launches.restype = C.c_long
+        g.rg_error.restype = C.c_int
+        g.rg_error.argtypes = [C.c_char_p, C.c_int]
+        err = C.create_string_buffer(256)
+        if g.rg_open(_build.REF_CUBIN.encode(), _build.REF_CUBIN_NAMES.encode(), self.device, err, 256):
+            raise RuntimeError("reference kernels unavailable: " + err.value.decode())
+        self._g = g
+        self.grid = int(g.rg_grid())
+        lib().orc_set_backend(g.rg_backend())
+        return self
+
+    def launches(self) -> int:
+        """Reference kernels launched since the context opened."""
+        return int(self._g.rg_launches())
+
+    def check(self) -> None:
+        """Raise if any driver call failed since the context opened."""
+        where = C.create_string_buffer(128)
+        e = self._g.rg_error(where, 128)
+        if e:
+            raise RuntimeError(f"CUDA driver error {e} in {where.value.decode()}")
+
+    def __exit__(self, *exc):
+        lib().orc_set_backend(None)
+        if self._g is not None:
+            self._g.rg_close()
+            self._g = None
+        return False
 
 
 def set_threads(n: int) -> None:

@@ -10,6 +10,14 @@
   ``gis/ldu2csr.h`` compiled from its source file against the
   ``refstub/lduMatrix.H`` stand-in.  Built only where the reference sources
   are mounted; the committed golden fixtures carry its outputs elsewhere.
+* ``oracle/_ref/ref_kernels.cubin`` (+ ``ref_kernels.names``) -- the
+  reference's own device kernels (``gis/SparseSystem/kernels.h``,
+  instantiated by ``refgpu/ref_kernels.cu``) compiled for sm_103a, with
+  their entry names as ptxas lists them.  Built where the reference
+  sources are mounted; the cubin is device code only, so the copy built
+  here serves the GPU machine too.
+* ``oracle/_build/librefgpu.so`` -- ``refgpu/ref_gpu.c``: the oracle
+  backend that launches those kernels through the CUDA driver API.
 """
 from __future__ import annotations
 
@@ -78,10 +86,72 @@ def build_ref_formats(force: bool = False) -> str | None:
     return REF_FORMATS_SO
 
 
+REF_CUBIN = os.path.join(REF_DIR, "ref_kernels.cubin")
+REF_CUBIN_NAMES = os.path.join(REF_DIR, "ref_kernels.names")
+REFGPU_SO = os.path.join(BUILD_DIR, "librefgpu.so")
+
+
+def _entry_key(mangled: str) -> str:
+    """The unqualified function name of an Itanium-mangled entry
+    (_Z<len><name>...)."""
+    i = 2
+    j = i
+    while j < len(mangled) and mangled[j].isdigit():
+        j += 1
+    n = int(mangled[i:j])
+    return mangled[j:j + n]
+
+
+def build_ref_kernels(force: bool = False) -> str | None:
+    """Compile the reference's device kernels into a cubin, if the
+    reference sources exist (otherwise keep a cubin built earlier)."""
+    gis = os.path.join(REFERENCE_ROOT, "gis")
+    hdr = os.path.join(gis, "SparseSystem", "kernels.h")
+    if not os.path.exists(hdr):
+        return REF_CUBIN if os.path.exists(REF_CUBIN) and os.path.exists(REF_CUBIN_NAMES) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    shim = os.path.join(HERE, "refgpu", "ref_kernels.cu")
+    if force or _stale(REF_CUBIN, [shim, hdr]) or not os.path.exists(REF_CUBIN_NAMES):
+        tmp = REF_CUBIN + f".tmp{os.getpid()}"
+        # the reference's own flags (gis/CMakeLists.txt: -O3), one sm_103a target
+        r = subprocess.run(["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                            "-I" + gis, "-Xptxas", "-v", shim, "-o", tmp],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {shim}:\n{r.stdout}\n{r.stderr}")
+        names = []
+        for line in (r.stdout + r.stderr).splitlines():
+            if "Compiling entry function '" in line:
+                mangled = line.split("'")[1]
+                names.append(f"{_entry_key(mangled)} {mangled}")
+        with open(REF_CUBIN_NAMES + ".tmp", "w") as f:
+            f.write("\n".join(sorted(names)) + "\n")
+        os.replace(REF_CUBIN_NAMES + ".tmp", REF_CUBIN_NAMES)
+        os.replace(tmp, REF_CUBIN)
+    return REF_CUBIN
+
+
+def build_refgpu(force: bool = False) -> str:
+    """The oracle backend that runs the reference's kernels (own source)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    src = os.path.join(HERE, "refgpu", "ref_gpu.c")
+    hdr = os.path.join(HERE, "oracle.h")
+    if force or _stale(REFGPU_SO, [src, hdr]):
+        cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(
+            subprocess.check_output(["which", "nvcc"], text=True).strip()))), "include")
+        tmp = REFGPU_SO + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-Wall",
+                               "-I" + cuda_inc, src, "-o", tmp, "-ldl", "-lm"])
+        os.replace(tmp, REFGPU_SO)
+    return REFGPU_SO
+
+
 def build_all(force: bool = False) -> None:
     build_oracle(force)
     build_ref_ldu2csr(force)
     build_ref_formats(force)
+    build_ref_kernels(force)
+    build_refgpu(force)
 
 
 if __name__ == "__main__":

@@ -118,10 +118,18 @@ static double block_tree(double *t)
     return t[0];
 }
 
+static const orc_backend *g_backend = NULL;
+
+void orc_set_backend(const orc_backend *backend)
+{
+    g_backend = backend;
+}
+
 /* kind: 0 dot (fma(a,b,t)), 1 sum (t + a), 2 distance (fma(d,d,t), d=a-b) */
 static double ref_reduce(int kind, const double *a, const double *b, int32_t n,
                          int32_t grid)
 {
+    if (g_backend) return g_backend->reduce(kind, a, b, n, grid);
     if (grid <= 0) grid = 1;
     /* blocks whose first index is past n hold exact +0 partials */
     const int32_t busy = (int32_t)(((int64_t)n + REF_BLOCK - 1) / REF_BLOCK) < grid
@@ -187,12 +195,14 @@ static inline double ref_row(const orc_csr *A, const double *x, int32_t row)
 
 void orc_ref_spmv(const orc_csr *A, const double *x, double *y)
 {
+    if (g_backend) { g_backend->spmv(A, x, y); return; }
 #pragma omp parallel for schedule(static) if (A->n > 16384)
     for (int32_t i = 0; i < A->n; ++i) y[i] = ref_row(A, x, i);
 }
 
 void orc_ref_residual(const orc_csr *A, const double *b, const double *x, double *r)
 {
+    if (g_backend) { g_backend->residual(A, b, x, r); return; }
 #pragma omp parallel for schedule(static) if (A->n > 16384)
     for (int32_t i = 0; i < A->n; ++i) r[i] = b[i] - ref_row(A, x, i);
 }
@@ -200,24 +210,28 @@ void orc_ref_residual(const orc_csr *A, const double *b, const double *x, double
 /* Element-wise kernels (gis/SparseSystem/kernels.h:318-402). */
 static void v_add(double *res, const double *v1, const double *v2, double alpha, int32_t n)
 {   /* AddKernel1: v1 + alpha*v2, contracted to fma */
+    if (g_backend) { g_backend->add(res, v1, v2, alpha, n); return; }
 #pragma omp parallel for schedule(static) if (n > 65536)
     for (int32_t i = 0; i < n; ++i) res[i] = fma(alpha, v2[i], v1[i]);
 }
 
 static void v_hadamard(double *res, const double *v1, const double *v2, int32_t n)
 {
+    if (g_backend) { g_backend->hadamard(res, v1, v2, n); return; }
 #pragma omp parallel for schedule(static) if (n > 65536)
     for (int32_t i = 0; i < n; ++i) res[i] = v1[i] * v2[i];
 }
 
 static void v_scale(double *res, const double *v, double alpha, int32_t n)
 {
+    if (g_backend) { g_backend->scale(res, v, alpha, n); return; }
 #pragma omp parallel for schedule(static) if (n > 65536)
     for (int32_t i = 0; i < n; ++i) res[i] = alpha * v[i];
 }
 
 static void v_fill(double *res, double val, int32_t n)
 {
+    if (g_backend) { g_backend->fill(res, val, n); return; }
 #pragma omp parallel for schedule(static) if (n > 65536)
     for (int32_t i = 0; i < n; ++i) res[i] = val;
 }
@@ -228,15 +242,18 @@ static void v_copy(double *res, const double *v, int32_t n)
 }
 
 /* diagonal entry of each row (FindDiag, gis/SparseSystem/kernels.h:447-464):
- * the entry with column == row; rows without one read as 0. */
-static void find_diag(const orc_csr *A, double *d)
+ * the entry with column == row; rows without one read as 0 (the reference
+ * leaves them unset).  mode 1 gives 1/a_ii (FindDiagInv, :563-580), mode 2
+ * sqrt(1/a_ii) (FindDiagInvSqrt, :586-603). */
+static void diag_vec(const orc_csr *A, double *d, int mode)
 {
+    if (g_backend) { g_backend->diag(A, d, mode); return; }
 #pragma omp parallel for schedule(static)
     for (int32_t i = 0; i < A->n; ++i) {
         double v = 0.0;
         for (int32_t j = A->row_offsets[i]; j < A->row_offsets[i + 1] && A->cols[j] <= i; ++j)
             if (A->cols[j] == i) v = A->vals[j];
-        d[i] = v;
+        d[i] = mode == 0 ? v : mode == 1 ? 1.0 / v : sqrt(1.0 / v);
     }
 }
 
@@ -385,9 +402,10 @@ static int solve_bicg(const orc_csr *A, const orc_csr *At, const double *b, doub
 /* FindDiagAbsMin, SolverSingleGPU.h:686-720 */
 static double diag_abs_min(const orc_csr *A)
 {
+    if (g_backend) return g_backend->diag_abs_min(A);
     const int32_t N = A->n;
     VEC(d);
-    find_diag(A, d);
+    diag_vec(A, d, 0);
     double m = HUGE_VAL;
     for (int32_t i = 0; i < N; ++i) { double a = fabs(d[i]); if (a < m) m = a; }
     free(d);
@@ -473,8 +491,7 @@ static void solve_jacobi(const orc_csr *A, const double *b, double *x, double er
     VEC(r); VEC(D_1); VEC(D_1r); VEC(AD_1r);
     orc_ref_residual(A, b, x, r);
     double norm_r = sqrt(orc_ref_dot(r, r, N, G));
-    find_diag(A, D_1);
-    for (int32_t i = 0; i < N; ++i) D_1[i] = 1.0 / D_1[i]; /* FindDiagInv */
+    diag_vec(A, D_1, 1); /* FindDiagInv */
     if (max_steps <= 0) max_steps = INT_MAX;
     hist_push(h, norm_r);
     int64_t k = 1;
@@ -497,8 +514,7 @@ static void solve_mrjacobi(const orc_csr *A, const double *b, double *x, double 
     VEC(r); VEC(D_1); VEC(D_1r); VEC(AD_1r);
     orc_ref_residual(A, b, x, r);
     double norm_r = sqrt(orc_ref_dot(r, r, N, G));
-    find_diag(A, D_1);
-    for (int32_t i = 0; i < N; ++i) D_1[i] = 1.0 / D_1[i];
+    diag_vec(A, D_1, 1); /* FindDiagInv */
     if (max_steps <= 0) max_steps = INT_MAX;
     hist_push(h, norm_r);
     int64_t k = 1;
@@ -520,8 +536,7 @@ static void solve_jmr(const orc_csr *A, const double *b, double *x, double error
 {
     const int32_t N = A->n;
     VEC(sD); VEC(r); VEC(sDr); VEC(z);
-    find_diag(A, sD);
-    for (int32_t i = 0; i < N; ++i) sD[i] = sqrt(1.0 / sD[i]); /* FindDiagInvSqrt */
+    diag_vec(A, sD, 2); /* FindDiagInvSqrt */
     orc_ref_residual(A, b, x, r);
     v_hadamard(r, sD, r, N);
     double norm_r = sqrt(orc_ref_dot(r, r, N, G));

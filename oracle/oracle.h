@@ -22,10 +22,13 @@
  *
  * Parity status: ldu2csr is pinned against the reference's own
  * gis/ldu2csr.h compiled from its sources (oracle/refstub).  The solver
- * restatement is parity unpinned: the reference ships no tests or golden
- * vectors and its solvers only run on a GPU through sources that are not
- * available where the GPU is; it is cross-checked instead against dense
- * direct solves and analytic solutions.
+ * restatement's arithmetic is pinned on the GPU: the same drivers run once
+ * on the CPU emulation and once on the reference's own kernels
+ * (gis/SparseSystem/kernels.h, compiled from its sources into a cubin by
+ * oracle/build.py and launched by oracle/refgpu/ref_gpu.c), and the two
+ * must agree bit for bit (tests/test_gpu_refgpu.py).  The host-side
+ * sequencing of each driver is restated from SolverSingleGPU.h line by
+ * line; the reference ships no tests or golden vectors of its own.
  */
 #ifndef CUFOAM_ORACLE_H
 #define CUFOAM_ORACLE_H
@@ -62,6 +65,29 @@ double orc_ref_sum(const double *a, int32_t n, int32_t grid);
 double orc_ref_distance(const double *a, const double *b, int32_t n, int32_t grid);
 void orc_ref_spmv(const orc_csr *A, const double *x, double *y);
 void orc_ref_residual(const orc_csr *A, const double *b, const double *x, double *r);
+
+/* The primitives the drivers below run on.  By default they are the CPU
+ * emulation above; a backend replaces them (all or none), e.g. with the
+ * reference's own kernels launched on a GPU (oracle/refgpu/ref_gpu.c), so
+ * that the same drivers run once through each and their bits compare. */
+typedef struct orc_backend {
+    /* kind 0: sum a*b (DotKernel), 1: sum a (ReductionKernel), 2: sum
+     * (a-b)^2 (DistanceKernel); G blocks, host sum of the partials */
+    double (*reduce)(int kind, const double *a, const double *b, int32_t n, int32_t grid);
+    void (*spmv)(const orc_csr *A, const double *x, double *y);                     /* SpMvKernel */
+    void (*residual)(const orc_csr *A, const double *b, const double *x, double *r); /* ResidualKernel */
+    void (*add)(double *res, const double *v1, const double *v2, double alpha, int32_t n); /* AddKernel1 */
+    void (*hadamard)(double *res, const double *v1, const double *v2, int32_t n);   /* HadamardKernel */
+    void (*scale)(double *res, const double *v, double alpha, int32_t n);           /* ScaleKernel */
+    void (*fill)(double *res, double val, int32_t n);                               /* FillKernel */
+    /* mode 0: a_ii (FindDiag), 1: 1/a_ii (FindDiagInv), 2: sqrt(1/a_ii)
+     * (FindDiagInvSqrt); only rows with a diagonal entry are defined */
+    void (*diag)(const orc_csr *A, double *d, int mode);
+    double (*diag_abs_min)(const orc_csr *A);                                       /* FindDiagAbsMin */
+} orc_backend;
+
+/* NULL restores the CPU emulation.  Not thread-safe: set it between solves. */
+void orc_set_backend(const orc_backend *backend);
 
 /* compensated (double-double) true residual norm ||b - A x||_2 */
 double orc_true_residual_norm(const orc_csr *A, const double *b, const double *x);
