@@ -216,9 +216,35 @@ def run_reference(args):
                                    f"(plain-C restatement of SolverSingleGPU.h CG, OpenMP)"},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "reference_gpu_kernels": reference_gpu_cg(A, b),
     }
     print(json.dumps(line))
     return 0
+
+
+def reference_gpu_cg(A, b):
+    """The whole 128^3 CG solve through the reference's own kernels on this
+    GPU (gis/SparseSystem/kernels.h compiled from the reference sources into
+    oracle/_ref/ref_kernels.cubin) with its host loop (SolverSingleGPU.h
+    CG: two synchronous host-summed dot products and their allocations per
+    step), matrix and vectors already on the device.  Rate in the same
+    algorithmic bytes as the `solve_hbm_gbs` line of this build."""
+    import oracle as O
+    try:
+        import torch
+        if not torch.cuda.is_available() or not O.reference_kernels.available():
+            return {"unavailable": "no GPU or no compiled reference kernels"}
+        x0 = np.zeros(A.n)
+        nf = O.norm_factor(A, b, x0)
+        with O.reference_kernels(0) as rk:
+            rk.cg_device(A, b, x0, 0.0, 3)
+            _, _, k, ms = rk.cg_device(A, b, x0, TOL * nf, MAX_ITER)
+        mat = csr_matrix_bytes(A.n, A.nnz)
+        work = (mat + 24 * A.n) + k * cg_iteration_bytes(mat, A.n)
+        return {"ms_per_solve": round(ms, 2), "iterations": k, "value": round(work / (ms * 1e-3) / 1e9, 2),
+                "unit": "GB/s", "path": "reference kernels + reference host loop, device-resident data"}
+    except Exception as e:  # informative only, never fatal to the line
+        return {"unavailable": repr(e)}
 
 
 def run_ours(args):

@@ -155,7 +155,7 @@ class LduMatrix:
         self._h = h
         self.n = int(n_cells)
         self.n_faces = v.n_faces
-        self._symmetric = _same(lower, upper)
+        self._set_symmetry(lambda: _same(lower, upper))
 
     @classmethod
     def from_ldu(cls, ldu, context: Context | None = None, with_addressing: bool = False):
@@ -183,8 +183,17 @@ class LduMatrix:
     def handle(self):
         return self._h
 
+    def _set_symmetry(self, fn) -> None:
+        # decided on the first symmetric() call: comparing the coefficient
+        # arrays costs more than a solve's upload, and most callers never ask
+        self._symmetric = None
+        self._sym_fn = fn
+
     def symmetric(self) -> bool:
         """lduMatrix::symmetric(): no separate upper coefficients."""
+        if self._symmetric is None:
+            self._symmetric = bool(self._sym_fn())
+            self._sym_fn = None
         return self._symmetric
 
     def shape(self):
@@ -214,7 +223,7 @@ class LduMatrix:
             raise ValueError("coefficients must all be host arrays or all CUDA tensors")
         self.ctx.check(self._lib.cf_matrix_update_values(self._h, pd, pl, pu, m1),
                        "cf_matrix_update_values")
-        self._symmetric = _same(lower, upper)
+        self._set_symmetry(lambda: _same(lower, upper))
 
     def to_csr(self, transpose: bool = False):
         n, _, nnz = self.shape()
@@ -285,7 +294,7 @@ class CsrMatrix(LduMatrix):
         self._h = h
         self.n = int(n)
         self.n_faces = -1
-        self._symmetric = _csr_symmetric(n, row_offsets, cols, vals)
+        self._set_symmetry(lambda: _csr_symmetric(n, row_offsets, cols, vals))
 
     def update_values(self, diag, lower, upper) -> None:
         raise NotImplementedError("a CSR matrix has no LDU coefficients")

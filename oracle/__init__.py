@@ -120,6 +120,24 @@ class reference_kernels:
         lib().orc_set_backend(g.rg_backend())
         return self
 
+    def cg_device(self, A, b, x0, error: float, max_steps: int):
+        """The reference's CG with its own kernels on device-resident data:
+        (x, history, steps, wall ms of the solver call)."""
+        g = self._g
+        g.rg_cg_device.restype = C.c_int
+        g.rg_cg_device.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_double, C.c_int, _dp,
+                                   C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        x = np.array(x0, dtype=np.float64, copy=True)
+        cap = (max_steps if max_steps > 0 else 100_000) + 1
+        hist = np.zeros(cap)
+        nh, ms = C.c_int(0), C.c_double(0.0)
+        k = g.rg_cg_device(A.n, A.nnz, A.row_offsets, A.cols, A.vals, _f64(b), x, error, max_steps, hist,
+                           cap, C.byref(nh), C.byref(ms))
+        self.check()
+        if k < 0:
+            raise RuntimeError("reference CG failed")
+        return x, hist[:nh.value].copy(), int(k), float(ms.value)
+
     def launches(self) -> int:
         """Reference kernels launched since the context opened."""
         return int(self._g.rg_launches())

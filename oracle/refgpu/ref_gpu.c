@@ -17,6 +17,7 @@
  * The CUDA driver is opened with dlopen, so this library builds and loads
  * on a machine without one; rg_open then reports the failure.
  */
+#define _POSIX_C_SOURCE 200809L
 #include "../oracle.h"
 
 #include <cuda.h>
@@ -26,6 +27,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 enum {
     K_FILL, K_REDUCTION, K_DOT, K_SPMV, K_DISTANCE, K_SCALE, K_ADD1, K_HADAMARD, K_RESIDUAL,
@@ -52,6 +54,7 @@ typedef CUresult (*PFN_MemFree)(CUdeviceptr);
 typedef CUresult (*PFN_MemcpyHtoD)(CUdeviceptr, const void *, size_t);
 typedef CUresult (*PFN_MemcpyDtoH)(void *, CUdeviceptr, size_t);
 typedef CUresult (*PFN_MemsetD8)(CUdeviceptr, unsigned char, size_t);
+typedef CUresult (*PFN_MemcpyDtoD)(CUdeviceptr, CUdeviceptr, size_t);
 typedef CUresult (*PFN_LaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned,
                                      unsigned, unsigned, CUstream, void **, void **);
 typedef CUresult (*PFN_CtxSynchronize)(void);
@@ -73,6 +76,7 @@ static struct {
     PFN_MemcpyHtoD MemcpyHtoD;
     PFN_MemcpyDtoH MemcpyDtoH;
     PFN_MemsetD8 MemsetD8;
+    PFN_MemcpyDtoD MemcpyDtoD;
     PFN_LaunchKernel LaunchKernel;
     PFN_CtxSynchronize CtxSynchronize;
 } cu;
@@ -271,6 +275,112 @@ static double be_diag_abs_min(const orc_csr *A)
     return result;
 }
 
+/* ---- the reference's CG on device-resident data, timed ------------------ */
+/* Kernels go to the legacy default stream without a synchronisation after
+ * each one, as the reference's LaunchKernel does; Dot synchronises through
+ * its copy of the block partials. */
+static void launch_async(int k, void **args)
+{
+    if (g.error) return;
+    if (fail(cu.LaunchKernel(g.fn[k], (unsigned)g.grid, 1, 1, 256, 1, 1, 0, NULL, args, NULL), kKernelNames[k]))
+        return;
+    ++g.launches;
+}
+
+/* Dot (SolverSingleGPU.h:101-126): a fresh device partial buffer, the
+ * DotKernel, a synchronous copy of the partials, a host sum in block order,
+ * and the buffers freed again. */
+static double dev_dot(CUdeviceptr a, CUdeviceptr b, int n)
+{
+    CUdeviceptr part = 0;
+    if (fail(cu.MemAlloc(&part, sizeof(double) * (size_t)g.grid), "cuMemAlloc")) return NAN;
+    void *args[] = {&part, &a, &b, &n};
+    launch_async(K_DOT, args);
+    double *h = (double *)malloc(sizeof(double) * (size_t)g.grid);
+    double sum = 0.0;
+    if (h) {
+        get(h, part, sizeof(double) * (size_t)g.grid);
+        for (int i = 0; i < g.grid; ++i) sum += h[i];
+        free(h);
+    }
+    cu.MemFree(part);
+    return sum;
+}
+
+static void dev_add(CUdeviceptr res, CUdeviceptr v1, CUdeviceptr v2, int n, double alpha)
+{
+    void *args[] = {&res, &v1, &v2, &n, &alpha};
+    launch_async(K_ADD1, args);
+}
+
+static double now_ms(void)
+{
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return 1e3 * (double)t.tv_sec + 1e-6 * (double)t.tv_nsec;
+}
+
+/* The reference's CG (SolverSingleGPU.h:366-445) with the matrix, b and x
+ * already on the device: r = b - Ax, p = r, rho = (r, r), then per step
+ * p = r + (rho0/rho1) p, q = A p, xi = rho0 / (p, q), x += xi p,
+ * r -= xi q, rho = (r, r), stopping at ||r|| <= error.  x is updated in
+ * place; history gets ||r|| per step (initial first).  *solve_ms is the wall
+ * time of the solver call, its work vectors' allocation and release
+ * included (the reference allocates them per call).  Returns the number of
+ * steps, or -1 on a driver error. */
+int rg_cg_device(int n, int nnz, const int32_t *ro, const int32_t *col, const double *val,
+                 const double *b, double *x, double error, int max_steps, double *history,
+                 int hist_cap, int *n_hist, double *solve_ms)
+{
+    if (!g.open) return -1;
+    orc_csr A = {n, nnz, ro, col, val};
+    CUdeviceptr dro, dcol, dval;
+    put_matrix(&A, &dro, &dcol, &dval);
+    CUdeviceptr db = put(0, b, sizeof(double) * (size_t)n);
+    CUdeviceptr dx = put(1, x, sizeof(double) * (size_t)n);
+    fail(cu.CtxSynchronize(), "upload");
+    if (g.error) return -1;
+    int len = 0;
+    const double t0 = now_ms();
+    CUdeviceptr r = 0, p = 0, q = 0;
+    const size_t vb = sizeof(double) * (size_t)(n > 0 ? n : 1);
+    fail(cu.MemAlloc(&r, vb), "cuMemAlloc");
+    {
+        void *args[] = {&r, &dval, &dro, &dcol, &n, &db, &dx};
+        launch_async(K_RESIDUAL, args);
+    }
+    fail(cu.MemAlloc(&p, vb), "cuMemAlloc");
+    fail(cu.MemcpyDtoD(p, r, vb), "cuMemcpyDtoD");
+    double rho0 = dev_dot(r, r, n), rho1 = 0.0;
+    double norm_r = sqrt(rho0);
+    fail(cu.MemAlloc(&q, vb), "cuMemAlloc");
+    if (max_steps <= 0) max_steps = 0x7fffffff;
+    if (len < hist_cap) history[len++] = norm_r;
+    int k = 1;
+    for (; k <= max_steps && norm_r > error && !g.error; ++k) {
+        if (k > 1) dev_add(p, r, p, n, rho0 / rho1);
+        {
+            void *args[] = {&q, &dval, &dro, &dcol, &n, &p};
+            launch_async(K_SPMV, args);
+        }
+        const double xi = rho0 / dev_dot(p, q, n);
+        dev_add(dx, dx, p, n, xi);
+        dev_add(r, r, q, n, -xi);
+        rho1 = rho0;
+        rho0 = dev_dot(r, r, n);
+        norm_r = sqrt(rho0);
+        if (len < hist_cap) history[len++] = norm_r;
+    }
+    fail(cu.CtxSynchronize(), "CG");
+    cu.MemFree(r);
+    cu.MemFree(p);
+    cu.MemFree(q);
+    *solve_ms = now_ms() - t0;
+    get(x, dx, sizeof(double) * (size_t)n);
+    *n_hist = len;
+    return g.error ? -1 : k - 1;
+}
+
 static const orc_backend kBackend = {be_reduce, be_spmv,  be_residual, be_add,         be_hadamard,
                                      be_scale,  be_fill,  be_diag,     be_diag_abs_min};
 
@@ -300,6 +410,7 @@ static int load_driver(void)
     SYM(MemcpyHtoD, "cuMemcpyHtoD_v2");
     SYM(MemcpyDtoH, "cuMemcpyDtoH_v2");
     SYM(MemsetD8, "cuMemsetD8_v2");
+    SYM(MemcpyDtoD, "cuMemcpyDtoD_v2");
     SYM(LaunchKernel, "cuLaunchKernel");
     SYM(CtxSynchronize, "cuCtxSynchronize");
 #undef SYM

@@ -152,3 +152,17 @@ def test_plugin_solve_matches_bitwise(refk):
     assert _same([cpu.norm_factor, cpu.initial_residual, cpu.final_residual],
                  [gpu.norm_factor, gpu.initial_residual, gpu.final_residual])
     assert _same(cpu.psi, gpu.psi)
+
+
+def test_device_resident_reference_cg_matches_the_oracle(refk):
+    # the timed device-resident reference CG (the reference's host loop with
+    # data kept on the GPU) computes what the oracle's CG computes
+    L = O.grid_lognormal(20, 20, 20, 9)
+    A = O.ldu2csr(L)
+    b = O.uniform(4, L.n)
+    O.lib().orc_set_backend(None)
+    want = O.solve(O.CG, A, b, np.zeros(L.n), 1e-6, 500, refk.grid)
+    x, hist, k, ms = refk.cg_device(A, b, np.zeros(L.n), 1e-6, 500)
+    assert k == want.n_iterations and ms > 0
+    assert _same(hist, want.history)
+    assert _same(x, want.x)
