@@ -205,6 +205,14 @@ def run_reference(args):
     total = sum(times)
     value = bytes_step * args.steps / total / 1e9
     cores = O.get_threads()
+    # the same sample on one host core
+    O.set_threads(1)
+    try:
+        t0 = time.perf_counter()
+        O.solve(O.CG, A, b, x0, 0.0, sample)
+        one_core = bytes_step / (time.perf_counter() - t0) / 1e9
+    finally:
+        O.set_threads(cores)
     line = {
         "metric": "solve_hbm_gbs", "value": round(value, 3), "unit": "GB/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -216,6 +224,7 @@ def run_reference(args):
                                    f"(plain-C restatement of SolverSingleGPU.h CG, OpenMP)"},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "cpu_one_core": {"value": round(one_core, 3), "unit": "GB/s", "cores": 1},
         "reference_gpu_kernels": reference_gpu_cg(A, b),
     }
     print(json.dumps(line))

@@ -297,6 +297,27 @@ __device__ __forceinline__ V row_product(const Chunk<V> &c, const int32_t *__res
     return tree8(t);
 }
 
+// The same sum for one row of a SELL-32 copy, where slot t of the row holds
+// its t-th CSR entry: lane l of 8 takes slots l, l + 8, ... below the row's
+// CSR length rl (len = the slice's slots per row; cp, vp point at this
+// lane's column and value of slot 0, slots 32 elements apart).
+template <class G>
+__device__ __forceinline__ double sell_ref_row(const int32_t *__restrict__ cp, const double *__restrict__ vp,
+                                               int len, int rl, G g)
+{
+    double t[8];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) t[l] = 0.0;
+    for (int t0 = 0; t0 < len; t0 += 8) {
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+            const int slot = t0 + l;
+            if (slot < rl) t[l] = fma_t(__ldg(vp + 32 * slot), g(__ldg(cp + 32 * slot)), t[l]);
+        }
+    }
+    return tree8(t);
+}
+
 // Two products over the same pattern (A and A^T values share row_offsets
 // and column indices for LDU matrices): the column index is read once.
 template <class V, class G1, class G2>

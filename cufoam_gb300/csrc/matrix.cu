@@ -267,6 +267,26 @@ __global__ void __launch_bounds__(kBlock) k_spmv(int n, int cap, const int32_t *
     }
 }
 
+// y = A x with the reference's row order, read from the SELL-32 copy (one
+// warp per slice; the same bits as k_spmv).
+__global__ void __launch_bounds__(kBlock) k_spmv_sell_ref(int n, int n_slices, const int32_t *__restrict__ off,
+                                                          const int32_t *__restrict__ col,
+                                                          const double *__restrict__ val,
+                                                          const int32_t *__restrict__ ro,
+                                                          const double *__restrict__ x, double *y)
+{
+    const int lane = threadIdx.x & 31;
+    const int nw = gridDim.x * kWarps;
+    for (int s = blockIdx.x * kWarps + (threadIdx.x >> 5); s < n_slices; s += nw) {
+        const int b = __ldg(off + s);
+        const int len = (__ldg(off + s + 1) - b) >> 5;
+        const int row = s * 32 + lane;
+        const int rl = row < n ? __ldg(ro + row + 1) - __ldg(ro + row) : 0;
+        const double v = sell_ref_row(col + b + lane, val + b + lane, len, rl, [&](int c) { return __ldg(x + c); });
+        if (row < n) y[row] = v;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // SELL-32 copy (layout described in device.cuh)
 // ---------------------------------------------------------------------------
@@ -913,12 +933,17 @@ void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order)
     Context *ctx = m->ctx;
     if (transpose) matrix_ensure_transpose(m);
     if (m->n == 0) return;
-    if (!ref_order && matrix_ensure_sell(m, transpose, false)) {
-        const int g = ctx->fast_grid((const void *)k_spmv_sell, 0);
-        k_spmv_sell<<<g, kBlock, 0, ctx->stream>>>(m->n, m->n_slices, m->s_off.as<int32_t>(),
-                                                   m->s_col.as<int32_t>(),
-                                                   transpose ? m->s_valT.as<double>() : m->s_val.as<double>(),
-                                                   x, y);
+    if (matrix_ensure_sell(m, transpose, false)) {
+        const double *sv = transpose ? m->s_valT.as<double>() : m->s_val.as<double>();
+        if (ref_order) {
+            const int g = ctx->fast_grid((const void *)k_spmv_sell_ref, 0);
+            k_spmv_sell_ref<<<g, kBlock, 0, ctx->stream>>>(m->n, m->n_slices, m->s_off.as<int32_t>(),
+                                                           m->s_col.as<int32_t>(), sv, m->ro.as<int32_t>(), x, y);
+        } else {
+            const int g = ctx->fast_grid((const void *)k_spmv_sell, 0);
+            k_spmv_sell<<<g, kBlock, 0, ctx->stream>>>(m->n, m->n_slices, m->s_off.as<int32_t>(),
+                                                       m->s_col.as<int32_t>(), sv, x, y);
+        }
         CF_CHECK_LAUNCH();
         return;
     }

@@ -46,12 +46,12 @@ __global__ void __launch_bounds__(kBlock) k_nf_dist(const SolveArgs *__restrict_
     const double xbar = ld_cg(&a->st->xbar);
     double acc[2] = {0.0, 0.0};
     CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const RefRow R(a, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        const double Y = row_product<double>(ch, col, val, [&](int c) { return x[c]; });
+        const double Y = R.product([&](int c) { return x[c]; });
         double Yb;
-        if (!l1) Yb = row_product<double>(ch, col, val, [&](int) { return xbar; });
-        else Yb = __dmul_rn(row_product<double>(ch, col, val, [&](int) { return 1.0; }), xbar);
+        if (!l1) Yb = R.product([&](int) { return xbar; });
+        else Yb = __dmul_rn(R.product([&](int) { return 1.0; }), xbar);
         if (row < n) {
             const double d1 = Y - Yb, d2 = b[row] - Yb;
             if (!l1) {
@@ -86,9 +86,9 @@ __global__ void __launch_bounds__(kBlock) k_res_init(const SolveArgs *__restrict
     double *r = a->r[0], *rs = a->rs;
     double acc[2] = {0.0, 0.0};
     CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const RefRow R(a, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        const double t = row_product<double>(ch, col, val, [&](int c) { return x[c]; });
+        const double t = R.product([&](int c) { return x[c]; });
         if (row < n) {
             double ri = b[row] - t;
             if (mode == 1) ri = __dmul_rn(sD[row], ri);
@@ -133,9 +133,9 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(const SolveArgs *__restrict_
     auto g = [&](int c) { return first ? r[c] : fma_t(beta, pin[c], r[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const RefRow R(a, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        const double y = row_product<double>(ch, col, val, g);
+        const double y = R.product(g);
         if (row < n) {
             const double pi = g(row);
             pout[row] = pi;
@@ -223,10 +223,10 @@ __global__ void __launch_bounds__(kBlock) k_bicg_spmv(const SolveArgs *__restric
     auto gps = [&](int c) { return first ? rs[c] : fma_t(theta, psin[c], rs[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const RefRow R(a, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
         double y1, y2;
-        row_product2<double>(ch, col, val, valT, gp, gps, y1, y2);
+        R.product2(gp, gps, y1, y2);
         if (row < n) {
             const double pi = gp(row), psi = gps(row);
             pout[row] = pi;
@@ -317,9 +317,9 @@ __global__ void __launch_bounds__(kBlock) k_pow_step(const SolveArgs *__restrict
     auto g = [&](int c) { return s == 0 ? inv_n : __dmul_rn(sc, yprev[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const RefRow R(a, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        const double v = row_product<double>(ch, col, val, g);
+        const double v = R.product(g);
         if (row < n) {
             y[row] = v;
             acc[0] = fma_t(v, v, acc[0]);
@@ -345,9 +345,9 @@ __global__ void __launch_bounds__(kBlock) k_pow_final(const SolveArgs *__restric
     auto g = [&](int c) { return steps == 0 ? inv_n : __dmul_rn(sc, ylast[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const RefRow R(a, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        const double av = row_product<double>(ch, col, val, g);
+        const double av = R.product(g);
         if (row < n) acc[0] = fma_t(g(row), av, acc[0]);
         __syncwarp();
     }
@@ -377,9 +377,9 @@ __global__ void __launch_bounds__(kBlock) k_rich_step(const SolveArgs *__restric
     auto g = [&](int c) { return fma_t(omega, rold[c], xold[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const RefRow R(a, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        const double t = row_product<double>(ch, col, val, g);
+        const double t = R.product(g);
         if (row < n) {
             const double ri = b[row] - t;
             xnew[row] = g(row);
@@ -424,9 +424,9 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_step(const SolveArgs *__restr
     auto g = [&](int c) { return __dmul_rn(dinv[c], rold[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const RefRow R(a, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        const double y = row_product<double>(ch, col, val, g);
+        const double y = R.product(g);
         if (row < n) {
             const double d = g(row);
             x[row] = fma_t(1.0, d, x[row]);
@@ -473,9 +473,9 @@ __global__ void __launch_bounds__(kBlock) k_mr_spmv(const SolveArgs *__restrict_
     auto g = [&](int c) { return mr_apply<KIND>(dinv, sD, r, c); };
     double acc[2] = {0.0, 0.0};
     CF_FOR_CHUNKS(base, n) {
-        const Chunk<double> ch = stage_chunk<double>(ro, col, val, n, base, cap, sv_, sc_);
+        const RefRow R(a, base, cap, sv_, sc_);
         const int row = base + (threadIdx.x & 31);
-        double v = row_product<double>(ch, col, val, g);
+        double v = R.product(g);
         if (row < n) {
             if (KIND == 3) v = __dmul_rn(sD[row], v);
             y[row] = v;
@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(kBlock) k_mr_update(const SolveArgs *__restric
 // ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
-static Kernels body_kernels(int solver)
+static Kernels body_kernels(int solver, bool sell)
 {
     Kernels k;
     switch (solver) {
@@ -530,6 +530,8 @@ static Kernels body_kernels(int solver)
     case CF_JMR: k.k1 = (const void *)k_mr_spmv<3>; k.k1_spmv = true; k.k2 = (const void *)k_mr_update<3>; break;
     default: break;
     }
+    // rows read from the SELL-32 copy stage nothing in shared memory
+    if (sell) k.k1_spmv = false;
     return k;
 }
 
@@ -552,6 +554,13 @@ double norm_factor(Matrix *m, const double *b, const double *x, int norm_type, b
     A.val = m->val.as<double>();
     A.x = const_cast<double *>(x);
     A.b = b;
+    const bool sell = matrix_ensure_sell(m, false, false);
+    if (sell) {
+        A.n_slices = m->n_slices;
+        A.s_off = m->s_off.as<int32_t>();
+        A.s_col = m->s_col.as<int32_t>();
+        A.s_val = m->s_val.as<double>();
+    }
     A.partials = ctx->partials.as<double>();
     A.partial_stride = stride;
     A.ref_order = ref ? 1 : 0;
@@ -566,7 +575,7 @@ double norm_factor(Matrix *m, const double *b, const double *x, int norm_type, b
     launch(ctx, ctx->stream, (const void *)k_nf_sum, launch_cfg(ctx, (const void *)k_nf_sum, false, cap, ref), args1);
     int l1 = norm_type == CF_NORM_OPENFOAM_L1 ? 1 : 0;
     void *a2[] = {&d_args, &l1};
-    launch(ctx, ctx->stream, (const void *)k_nf_dist, launch_cfg(ctx, (const void *)k_nf_dist, true, cap, ref), a2);
+    launch(ctx, ctx->stream, (const void *)k_nf_dist, launch_cfg(ctx, (const void *)k_nf_dist, !sell, cap, ref), a2);
     CF_CUDA(cudaMemcpyAsync(ctx->h_state, A.st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
     CF_CUDA(cudaStreamSynchronize(ctx->stream));
     return ctx->h_state->nf;
@@ -596,9 +605,10 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     const bool tr = c.transpose != 0;
     if (solver == CF_BICG || tr) matrix_ensure_transpose(m);
     if (solver == CF_RICHARDSON) matrix_ensure_dmin(m);
-    // the fast loops read the SELL-32 copy when the pattern suits it (FP32
-    // values too for the mixed inner solve)
-    const bool sell = !ref && matrix_ensure_sell(m, solver == CF_BICG || tr, mixed);
+    // both orders read the SELL-32 copy when the pattern suits it (FP32
+    // values too for the mixed inner solve); the reference order takes its
+    // 8-lane row sums from the SELL slots (RefRow), the same bits as from CSR
+    const bool sell = matrix_ensure_sell(m, solver == CF_BICG || tr, mixed);
 
     // ---- vectors -------------------------------------------------------
     double *x, *b;
@@ -683,7 +693,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     const bool prof = c.profile_kernels != 0;
     bool use_graph = c.use_graph != 0 && ctx->graphs_ok && !prof;
     GraphEntry *ge = nullptr;
-    const Kernels kk = ref ? body_kernels(solver) : fast_body_kernels(solver, sell);
+    const Kernels kk = ref ? body_kernels(solver, sell) : fast_body_kernels(solver, sell);
     SolveArgs *d_args = ctx->args.as<SolveArgs>();
     if (use_graph && !mixed) {
         try {
@@ -708,7 +718,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
         int l1 = (c.norm_type == CF_NORM_OPENFOAM_L1) ? 1 : 0;
         void *a2[] = {&d_args, &l1};
         launch(ctx, ctx->stream, (const void *)k_nf_dist,
-               launch_cfg(ctx, (const void *)k_nf_dist, true, cap, ref), a2);
+               launch_cfg(ctx, (const void *)k_nf_dist, !sell, cap, ref), a2);
     }
     // ---- Richardson relaxation factor -----------------------------------
     if (solver == CF_RICHARDSON && !mixed) {
@@ -718,11 +728,11 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
             for (int s = 0; s < steps; ++s) {
                 void *a2[] = {&d_args, &s};
                 launch(ctx, ctx->stream, (const void *)k_pow_step,
-                       launch_cfg(ctx, (const void *)k_pow_step, true, cap, ref), a2);
+                       launch_cfg(ctx, (const void *)k_pow_step, !sell, cap, ref), a2);
             }
             void *a3[] = {&d_args, &steps};
             launch(ctx, ctx->stream, (const void *)k_pow_final,
-                   launch_cfg(ctx, (const void *)k_pow_final, true, cap, ref), a3);
+                   launch_cfg(ctx, (const void *)k_pow_final, !sell, cap, ref), a3);
         }
     }
     // ---- initial residual ----------------------------------------------
@@ -730,7 +740,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
         int mode = mixed ? 0 : (solver == CF_JMR ? 1 : (solver == CF_BICG ? 2 : (solver == CF_PCG ? 3 : 0)));
         void *a2[] = {&d_args, &mode};
         launch(ctx, ctx->stream, (const void *)k_res_init,
-               launch_cfg(ctx, (const void *)k_res_init, true, cap, ref), a2);
+               launch_cfg(ctx, (const void *)k_res_init, !sell, cap, ref), a2);
     }
     // ---- iterations: device-driven while loop, or host-driven chunks ----
     CF_CUDA(cudaEventRecord(ctx->ev_mid, ctx->stream));

@@ -83,6 +83,75 @@ __device__ __forceinline__ void for_rows2(const SolveArgs *a, const V *val1, con
 }
 
 // ---------------------------------------------------------------------------
+// Reference-order row products.  The reference's SpMV (kernels.h:206-237)
+// lets lane l of 8 accumulate a row's entries l, l + 8, ... with FMA and
+// adds the 8 lane sums in a fixed tree.  A SELL-32 copy keeps a row's t-th
+// CSR entry in slot t, so the same sums read from SELL slots l, l + 8, ...
+// of the row: the bits are the reference's, the loads coalesced and the
+// loop free of per-row trip counts.  RefRow serves one chunk of 32 rows
+// (base + lane) from the SELL copy when the solve has one (a->s_off set),
+// else from the staged CSR chunk.
+// ---------------------------------------------------------------------------
+struct RefRow {
+    const SolveArgs *a;
+    bool sell;
+    int off, len, rl;  // SELL: slice start, slots per row, this row's CSR length
+    Chunk<double> ch;
+
+    __device__ __forceinline__ RefRow(const SolveArgs *a_, int base, int cap, double *sv, int32_t *sc)
+        : a(a_), sell(a_->s_off != nullptr)
+    {
+        const int n = a->n, row = base + (threadIdx.x & 31);
+        if (sell) {
+            const int s = base >> 5;
+            off = __ldg(a->s_off + s);
+            len = (__ldg(a->s_off + s + 1) - off) >> 5;
+            rl = row < n ? __ldg(a->ro + row + 1) - __ldg(a->ro + row) : 0;
+        } else {
+            ch = stage_chunk<double>(a->ro, a->col, a->val, n, base, cap, sv, sc);
+        }
+    }
+
+    template <class G>
+    __device__ __forceinline__ double product(G g) const
+    {
+        if (!sell) return row_product<double>(ch, a->col, a->val, g);
+        const int lane = threadIdx.x & 31;
+        return sell_ref_row(a->s_col + off + lane, a->s_val + off + lane, len, rl, g);
+    }
+
+    // A and A^T values on the same pattern (row_product2)
+    template <class G1, class G2>
+    __device__ __forceinline__ void product2(G1 g1, G2 g2, double &y1, double &y2) const
+    {
+        if (!sell) {
+            row_product2<double>(ch, a->col, a->val, a->valT, g1, g2, y1, y2);
+            return;
+        }
+        const int lane = threadIdx.x & 31;
+        const int32_t *cp = a->s_col + off + lane;
+        const double *vp1 = a->s_val + off + lane;
+        const double *vp2 = a->s_valT + off + lane;
+        double t[8], u[8];
+#pragma unroll
+        for (int l = 0; l < 8; ++l) t[l] = u[l] = 0.0;
+        for (int t0 = 0; t0 < len; t0 += 8) {
+#pragma unroll
+            for (int l = 0; l < 8; ++l) {
+                const int slot = t0 + l;
+                if (slot < rl) {
+                    const int c = __ldg(cp + 32 * slot);
+                    t[l] = fma_t(__ldg(vp1 + 32 * slot), g1(c), t[l]);
+                    u[l] = fma_t(__ldg(vp2 + 32 * slot), g2(c), u[l]);
+                }
+            }
+        }
+        y1 = tree8(t);
+        y2 = tree8(u);
+    }
+};
+
+// ---------------------------------------------------------------------------
 // loop bookkeeping (thread 0 of the last block)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long global_ns()

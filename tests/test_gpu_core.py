@@ -197,13 +197,17 @@ def _problem(case, kind):
     return L, b, tol, maxit
 
 
+@pytest.mark.parametrize("fmt", ["sell", "csr"])
 @pytest.mark.parametrize("case", list(CASES))
 @pytest.mark.parametrize("name", list(O.SOLVER_NAMES))
-def test_solver_reference_order_is_bit_exact(ctx, ref_grid, name, case):
+def test_solver_reference_order_is_bit_exact(ctx, ref_grid, name, case, fmt):
+    """Reference order: the oracle's bits, whether the rows are read from the
+    staged CSR arrays or from the SELL-32 slots."""
     kind = O.SOLVER_NAMES[name]
     L, b, tol, maxit = _problem(case, kind)
     want = O.plugin_solve(kind, L, b, np.zeros(L.n), tol, maxit, grid=ref_grid)
     M = _matrix(ctx, L)
+    M.set_format(fmt)
     psi = np.zeros(L.n)
     s = cf.New("p", M, {"solver": "cuFoam" + name, "tolerance": tol, "maxIter": maxit,
                         "reduction": "reference"})
