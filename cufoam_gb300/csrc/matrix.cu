@@ -326,13 +326,28 @@ __global__ void k_sell_fill(int n, int n_slices, const int32_t *__restrict__ ro,
     }
 }
 
-// y = A x over the SELL-32 copy (the fast order of k_spmv_fast)
-__global__ void __launch_bounds__(kBlock) k_spmv_sell(int n, int n_slices, const int32_t *__restrict__ off,
+// y = A x over the SELL-32 copy (the fast order of k_spmv_fast).  Entries
+// per batch and resident blocks per SM (0: no register constraint) are
+// tuning constants; measured on the 7-point 128^3 product (100 launches
+// back to back): 4 entries at 5 blocks/SM 37.0 us, 2 at 6 37.1, 8 with no
+// constraint 39.1, 4 at 4 39.6, 3 at 5 41.2, 16 70.7.
+#ifndef CF_PLAIN_SPMV_BATCH
+#define CF_PLAIN_SPMV_BATCH 4
+#endif
+#ifndef CF_PLAIN_SPMV_MINB
+#define CF_PLAIN_SPMV_MINB 5
+#endif
+#if CF_PLAIN_SPMV_MINB > 0
+#define CF_PLAIN_SPMV_BOUNDS __launch_bounds__(kBlock, CF_PLAIN_SPMV_MINB)
+#else
+#define CF_PLAIN_SPMV_BOUNDS __launch_bounds__(kBlock)
+#endif
+__global__ void CF_PLAIN_SPMV_BOUNDS k_spmv_sell(int n, int n_slices, const int32_t *__restrict__ off,
                                                       const int32_t *__restrict__ col,
                                                       const double *__restrict__ val,
                                                       const double *__restrict__ x, double *y)
 {
-    sell_rows<double, 8>(n, n_slices, off, col, val, [&](int c) { return __ldg(x + c); },
+    sell_rows<double, CF_PLAIN_SPMV_BATCH>(n, n_slices, off, col, val, [&](int c) { return __ldg(x + c); },
                          [&](int row, double v) { y[row] = v; });
 }
 
