@@ -46,6 +46,12 @@ constexpr int kBatchMaxR = 4;
 #define CF_BATCH_ENTRY_BATCH 1
 #endif
 constexpr int kBatchEntryBatch = CF_BATCH_ENTRY_BATCH;
+// the same for the FP32 inner sweeps (single-width values and gathers leave
+// the registers for a deeper batch)
+#ifndef CF_BATCH_ENTRY_BATCH32
+#define CF_BATCH_ENTRY_BATCH32 4
+#endif
+constexpr int kBatchEntryBatch32 = CF_BATCH_ENTRY_BATCH32;
 // 1: matrix entries loaded with an L2 evict-first hint (they are re-read
 // only in the next step), 0: plain read-only loads
 #ifndef CF_BATCH_STREAM_HINT
@@ -208,7 +214,7 @@ __device__ __forceinline__ void row_product(const BatchSystem &S, const V *__res
     for (int j = 0; j < R; ++j) y[j] = T(0);
     ys = T(0);
     if (S.sell) {
-        constexpr int B = kBatchEntryBatch;
+        constexpr int B = sizeof(V) == 4 ? kBatchEntryBatch32 : kBatchEntryBatch;
 #if CF_BATCH_STREAM_HINT
         const uint64_t pol = l2_evict_first_policy();
 #define CF_BATCH_LD(ptr) ld_stream(ptr, pol)
@@ -472,25 +478,40 @@ __global__ void __launch_bounds__(BT, batch_min_blocks<BT>()) k_batch_cg(const B
                             beta[j] = (k > 1 && ain[j]) ? st.rho32[j] / st.rho32_old[j] : 0.f;
                             pend[j] = (float)st.alpha[j];
                         }
-                        const float *r32 = a.r32 + S.vec_offset * R;
-                        float *p32 = a.p32 + S.vec_offset * pad_r<R>(), *e32 = a.e32 + S.vec_offset * R;
-                        for (int s = s_lo + warp; s < s_hi; s += W) {
-                            const int row = s * 32 + lane;
-                            if (row < n) {
-                                float pv[R];
-                                if (k > 1) ld_row<R>(p32, row, pv);
+                        const float *__restrict__ r32 = a.r32 + S.vec_offset * R;
+                        float *__restrict__ p32 = a.p32 + S.vec_offset * pad_r<R>();
+                        float *__restrict__ e32 = a.e32 + S.vec_offset * R;
+                        // two rows (slices s and s + W) per step, all loads first
+                        for (int s = s_lo + warp; s < s_hi; s += 2 * W) {
+                            const int rows[2] = {s * 32 + lane, (s + W) * 32 + lane};
+                            const bool ok[2] = {rows[0] < n, s + W < s_hi && rows[1] < n};
+                            float pv[2][R], rv[2][R], ev[2][R];
 #pragma unroll
-                                for (int j = 0; j < R; ++j) {
-                                    const int64_t o = (int64_t)row * R + j;
-                                    if (k == 1) {
-                                        pv[j] = ain[j] ? r32[o] : 0.f;
-                                    } else {
-                                        if (pend[j] != 0.f) e32[o] = fma_t(pend[j], pv[j], e32[o]);
-                                        if (ain[j]) pv[j] = fma_t(beta[j], pv[j], r32[o]);
+                            for (int h = 0; h < 2; ++h)
+                                if (ok[h]) {
+                                    if (k > 1) ld_row<R>(p32, rows[h], pv[h]);
+#pragma unroll
+                                    for (int j = 0; j < R; ++j) {
+                                        const int64_t o = (int64_t)rows[h] * R + j;
+                                        rv[h][j] = r32[o];
+                                        ev[h][j] = (k > 1 && pend[j] != 0.f) ? e32[o] : 0.f;
                                     }
                                 }
-                                st_row<R>(p32, row, pv);
-                            }
+#pragma unroll
+                            for (int h = 0; h < 2; ++h)
+                                if (ok[h]) {
+#pragma unroll
+                                    for (int j = 0; j < R; ++j) {
+                                        const int64_t o = (int64_t)rows[h] * R + j;
+                                        if (k == 1) {
+                                            pv[h][j] = ain[j] ? rv[h][j] : 0.f;
+                                        } else {
+                                            if (pend[j] != 0.f) e32[o] = fma_t(pend[j], pv[h][j], ev[h][j]);
+                                            if (ain[j]) pv[h][j] = fma_t(beta[j], pv[h][j], rv[h][j]);
+                                        }
+                                    }
+                                    st_row<R>(p32, rows[h], pv[h]);
+                                }
                         }
                     }
                     if (!any_in) break;
@@ -530,20 +551,32 @@ __global__ void __launch_bounds__(BT, batch_min_blocks<BT>()) k_batch_cg(const B
                         float alpha[R];
 #pragma unroll
                         for (int j = 0; j < R; ++j) alpha[j] = ain[j] ? st.rho32[j] / (float)tot[j] : 0.f;
-                        const float *q32 = a.q32 + S.vec_offset * R;
-                        float *r32 = a.r32 + S.vec_offset * R;
+                        const float *__restrict__ q32 = a.q32 + S.vec_offset * R;
+                        float *__restrict__ r32 = a.r32 + S.vec_offset * R;
                         float accf[R];
 #pragma unroll
                         for (int j = 0; j < R; ++j) accf[j] = 0.f;
-                        for (int s = s_lo + warp; s < s_hi; s += W) {
-                            const int row = s * 32 + lane;
-                            if (row < n)
+                        // two rows per step, all loads first
+                        for (int s = s_lo + warp; s < s_hi; s += 2 * W) {
+                            const int rows[2] = {s * 32 + lane, (s + W) * 32 + lane};
+                            const bool ok[2] = {rows[0] < n, s + W < s_hi && rows[1] < n};
+                            float qv[2][R], rv[2][R];
+#pragma unroll
+                            for (int h = 0; h < 2; ++h)
+#pragma unroll
+                                for (int j = 0; j < R; ++j) {
+                                    const int64_t o = (int64_t)rows[h] * R + j;
+                                    const bool use = ok[h] && ain[j];
+                                    qv[h][j] = use ? q32[o] : 0.f;
+                                    rv[h][j] = use ? r32[o] : 0.f;
+                                }
+#pragma unroll
+                            for (int h = 0; h < 2; ++h)
 #pragma unroll
                                 for (int j = 0; j < R; ++j)
-                                    if (ain[j]) {
-                                        const int64_t o = (int64_t)row * R + j;
-                                        const float ri = fma_t(-alpha[j], q32[o], r32[o]);
-                                        r32[o] = ri;
+                                    if (ok[h] && ain[j]) {
+                                        const float ri = fma_t(-alpha[j], qv[h][j], rv[h][j]);
+                                        r32[(int64_t)rows[h] * R + j] = ri;
                                         accf[j] = fma_t(ri, ri, accf[j]);
                                     }
                         }
