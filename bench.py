@@ -142,19 +142,26 @@ def measured_hbm_peak():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(name: str):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/<name>), or None."""
+def profiled_value(name: str, key: str):
+    """A `key: value` line of a committed ncu summary (profiles/<name>),
+    or None."""
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             try:
-                return int(float(line.split(":", 1)[1].split()[0]))
+                return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def profiled_traffic(name: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary, or None."""
+    v = profiled_value(name, "traffic_bytes_per_launch")
+    return None if v is None else int(v)
 
 
 # ---------------------------------------------------------------------------
@@ -449,7 +456,11 @@ def run_ours(args):
                      "peak_source": peak_kind,
                      "bytes_per_launch": k1_bytes,
                      "us_per_launch": round(k1_ms * 1e3, 2),
-                     "traffic": profiled_traffic("k_f_cg_spmv_sell_poisson128.md")},
+                     "traffic": profiled_traffic("k_f_cg_spmv_sell_poisson128.md"),
+                     # the co-binding unit: 8 FP64 operations per row at the
+                     # measured 1.68 DFMA/clk/SM (ncu, same summary)
+                     "fp64_pipe_active": profiled_value("k_f_cg_spmv_sell_poisson128.md",
+                                                        "fp64_pipe_active_frac")},
         "kernels": {"k_f_cg_update_gbs": round(k2_gbs, 1), "k_f_cg_update_us": round(k2_ms * 1e3, 2),
                     "k_f_cg_prep_gbs": round(k0_gbs, 1), "k_f_cg_prep_us": round(k0_ms * 1e3, 2),
                     "spmv_gbs": round(spmv_gbs, 1), "spmv_us": round(spmv_ms * 1e3, 2),
