@@ -331,6 +331,12 @@ static bool build_loop_graph(Context *ctx, const Kernels &kk, int cap, bool ref,
 // The device-driven loop of one solver configuration, built once per
 // context: with programmatic launches between the body kernels where the
 // driver accepts them in a conditional body, else without.
+// Loop-body kernels launched with programmatic dependent launch inside the
+// loop graphs (1), or as plain serialised launches (0).
+#ifndef CF_LOOP_PDL
+#define CF_LOOP_PDL 1
+#endif
+
 static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int precision, int cap,
                               bool ref, SolveArgs *d_args, int format = 0)
 {
@@ -338,8 +344,8 @@ static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int p
     auto it = ctx->graphs.find(key);
     if (it != ctx->graphs.end()) return &it->second;
     GraphEntry ge;
-    if (!(ctx->pdl_ok && build_loop_graph(ctx, kk, cap, ref, d_args, true, ge))) {
-        ctx->pdl_ok = false;
+    if (!(CF_LOOP_PDL && ctx->pdl_ok && build_loop_graph(ctx, kk, cap, ref, d_args, true, ge))) {
+        if (CF_LOOP_PDL) ctx->pdl_ok = false; // a programmatic launch failed to capture
         if (!build_loop_graph(ctx, kk, cap, ref, d_args, false, ge))
             throw Error{CF_CUDA_ERROR, "cannot build the solver loop graph"};
     }

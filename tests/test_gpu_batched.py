@@ -96,3 +96,29 @@ def test_batched_mixed_precision_reaches_fp64_tolerance(ctx, config):
             assert true_rel <= 1.5 * tol
             err = np.linalg.norm(xs32[s][j] - xs64[s][j]) / np.linalg.norm(xs64[s][j])
             assert err < 1e-6, (s, j, err)
+
+
+@pytest.mark.parametrize("n_rhs", [1, 2, 4])
+@pytest.mark.parametrize("precision", ["FP64", "mixed"])
+def test_batched_other_component_counts(ctx, n_rhs, precision):
+    """1, 2 and 4 right-hand sides per system (each count has its own row
+    layout of the gathered search direction: 8, 16 and 32 bytes per cell):
+    every pair reaches the tolerance on its true residual, and FP64 matches
+    independent solves in iterations."""
+    systems, _ = c4_systems(7, seed=13, lo=6, hi=12)
+    rhs = [np.stack([O.uniform(500 + 10 * s + j, L.n) for j in range(n_rhs)])
+           for s, L in enumerate(systems)]
+    tol, maxit = 1e-9, 20000
+    B = BatchSolver(systems, n_rhs=n_rhs, context=ctx)
+    x, results, _ = B.solve(rhs, tolerance=tol, max_iter=maxit, precision=precision)
+    xs = B.unpack(x)
+    for s, L in enumerate(systems):
+        A = O.ldu2csr(L)
+        for j in range(n_rhs):
+            res = results[s * n_rhs + j]
+            assert res["status"] == 0 and res["final_residual"] <= tol, (s, j, res)
+            true_rel = O.true_residual_norm(A, rhs[s][j], xs[s][j]) / res["norm_factor"]
+            assert true_rel <= 1.5 * tol
+            if precision == "FP64":
+                want = O.plugin_solve(O.CG, L, rhs[s][j], np.zeros(L.n), tol, maxit)
+                assert abs(res["n_iterations"] - want.n_iterations) <= 2, (s, j)
