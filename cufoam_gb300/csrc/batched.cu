@@ -1019,6 +1019,81 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
     CF_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
+// ---------------------------------------------------------------------------
+// One small system: the whole CG solve in one cluster-persistent launch
+// ---------------------------------------------------------------------------
+// Rows per CTA the single-system path aims for when it sizes its cluster
+// (one row per thread: its passes are latency chains, so the most threads
+// win; measured at 64^2: 256 rows 8.7 us per step, 512 10.2, 2048 22.6).
+#ifndef CF_SMALL_CG_ROWS_PER_CTA
+#define CF_SMALL_CG_ROWS_PER_CTA 256
+#endif
+
+// CG (FP64, the fast summation order) on one system with the batched
+// kernel: one cluster of up to 16 CTAs runs normFactor, the initial residual
+// and every step, with hardware cluster barriers where the multi-kernel
+// loop has kernel boundaries.  x, b, r, p, q are device vectors of n rows.
+SmallSolveResult solve_cg_single_cluster(Matrix *m, const cf_controls &c, const double *b, double *x,
+                                         double *r, double *p, double *q)
+{
+    Context *ctx = m->ctx;
+    const int n = m->n;
+    const bool sell = matrix_ensure_sell(m, false, false);
+    struct Block {
+        BatchSystem sys;
+        int32_t order[4];
+        int32_t queue[4];
+        BatchResult out;
+    };
+    DeviceBuffer &blk = ctx->vec[23];
+    blk.ensure(sizeof(Block));
+    Block h{};
+    h.sys.n = n;
+    h.sys.sell = sell ? 1 : 0;
+    h.sys.vec_offset = 0;
+    h.sys.ro = m->ro.as<int32_t>();
+    h.sys.col = m->col.as<int32_t>();
+    h.sys.val = m->val.as<double>();
+    h.sys.val32 = nullptr;
+    h.sys.s_off = sell ? m->s_off.as<int32_t>() : nullptr;
+    h.sys.s_col = sell ? m->s_col.as<int32_t>() : nullptr;
+    h.sys.s_val = sell ? m->s_val.as<double>() : nullptr;
+    h.sys.s_val32 = nullptr;
+    Block *d = blk.as<Block>();
+    CF_CUDA(cudaMemcpyAsync(d, &h, sizeof(Block), cudaMemcpyHostToDevice, ctx->stream));
+    BatchArgs a{};
+    a.sys = &d->sys;
+    a.order = d->order;
+    a.n_systems = 1;
+    a.max_iter = c.max_iter <= 0 ? INT_MAX : c.max_iter;
+    a.tolerance = c.tolerance;
+    a.b = b;
+    a.x = x;
+    a.r = r;
+    a.p = p;
+    a.q = q;
+    a.queue = d->queue;
+    a.out = &d->out;
+    int cs = 1;
+    while (cs < 16 && (int64_t)cs * CF_SMALL_CG_ROWS_PER_CTA < n) cs <<= 1;
+    CF_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
+    launch_batch<1, 256, false>(ctx, a, cs, 1, ctx->stream);
+    CF_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
+    BatchResult res;
+    CF_CUDA(cudaMemcpyAsync(&res, &d->out, sizeof(res), cudaMemcpyDeviceToHost, ctx->stream));
+    CF_CUDA(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    CF_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+    SmallSolveResult o;
+    o.nf = res.nf;
+    o.norm0 = res.norm0;
+    o.norm = res.norm;
+    o.iters = res.iters;
+    o.status = res.status;
+    o.ms = ms;
+    return o;
+}
+
 int64_t batch_rows(const Batch *B) { return B->rows; }
 int batch_systems(const Batch *B) { return (int)B->mats.size(); }
 int64_t batch_offset(const Batch *B, int s) { return B->offsets[s]; }

@@ -59,7 +59,8 @@ int Context::fast_grid(const void *kernel, size_t dyn_smem) const
     }
     int g = per_sm * sm_count;
     const int cap = sm_count * 8;
-    return g > cap ? cap : g;
+    if (g > cap) g = cap;
+    return (grid_cap > 0 && g > grid_cap) ? grid_cap : g;
 }
 
 Context::~Context()

@@ -144,11 +144,11 @@ struct DeviceBuffer {
 };
 
 struct GraphKey {
-    int solver, precision, reduction, stage_cap, phase, format;
+    int solver, precision, reduction, stage_cap, phase, format, grid_cap;
     bool operator<(const GraphKey &o) const
     {
-        return std::tie(solver, precision, reduction, stage_cap, phase, format) <
-               std::tie(o.solver, o.precision, o.reduction, o.stage_cap, o.phase, o.format);
+        return std::tie(solver, precision, reduction, stage_cap, phase, format, grid_cap) <
+               std::tie(o.solver, o.precision, o.reduction, o.stage_cap, o.phase, o.format, o.grid_cap);
     }
 };
 
@@ -183,8 +183,34 @@ struct Context {
     std::vector<cudaEvent_t> prof_events;
     std::map<GraphKey, GraphEntry> graphs;
 
+    // > 0: fast-order launches use at most this many blocks (a small
+    // system, see GridCap); the reference order keeps the reference's grid
+    int grid_cap = 0;
+
     int fast_grid(const void *kernel, size_t dyn_smem) const;
     ~Context();
+};
+
+// A small system's fast-order launches take one row per thread at most,
+// rounded up to a power of two of blocks (so that few loop graphs exist):
+// idle blocks would only add grid-reduction arrivals and last-block work.
+// Set for the duration of one library call.
+struct GridCap {
+    Context *ctx;
+    int old;
+    GridCap(Context *c, int64_t rows) : ctx(c), old(c->grid_cap)
+    {
+        const int64_t need = (rows + kBlock - 1) / kBlock;
+        int cap = 0;
+        if (need < (int64_t)c->sm_count * 4) {
+            cap = 1;
+            while (cap < need) cap <<= 1;
+        }
+        c->grid_cap = cap;
+    }
+    ~GridCap() { ctx->grid_cap = old; }
+    GridCap(const GridCap &) = delete;
+    GridCap &operator=(const GridCap &) = delete;
 };
 
 struct Matrix {
@@ -240,6 +266,15 @@ void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order)
 double norm_factor(Matrix *m, const double *b, const double *x, int norm_type, bool ref_order);
 void solve(Matrix *m, int solver, const cf_controls &c, const double *b, double *x,
            cf_perf *perf);
+
+// CG on one small system in a single cluster-persistent launch (batched.cu)
+struct SmallSolveResult {
+    double nf, norm0, norm;
+    int32_t iters, status;
+    float ms;
+};
+SmallSolveResult solve_cg_single_cluster(Matrix *m, const cf_controls &c, const double *b, double *x,
+                                         double *r, double *p, double *q);
 
 struct Batch;
 Batch *batch_create(Context *ctx, int n_systems, const cf_ldu_view *views);

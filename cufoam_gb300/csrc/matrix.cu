@@ -946,6 +946,7 @@ int stage_cap_for(const Matrix *m)
 void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order)
 {
     Context *ctx = m->ctx;
+    const GridCap small(ctx, m->n);
     if (transpose) matrix_ensure_transpose(m);
     if (m->n == 0) return;
     if (matrix_ensure_sell(m, transpose, false)) {

@@ -537,11 +537,22 @@ static Kernels body_kernels(int solver, bool sell)
 
 static size_t vec_bytes(int n) { return sizeof(double) * ((size_t)n + 8); }
 
+// Systems up to this many rows solve CG (fast order, FP64, no history) in one
+// cluster-persistent launch instead of the multi-kernel loop: at 64^2 8.7 us
+// per step against 16.7; from ~14k rows on (24^3: 17.4 against 17-20 us)
+// the loop's full-GPU passes are as fast, and at 40^3 the single cluster is
+// 2.5x slower.
+#ifndef CF_SMALL_CG_ROWS
+#define CF_SMALL_CG_ROWS 8192
+#endif
+constexpr int kSmallCgRows = CF_SMALL_CG_ROWS;
+
 // normFactor alone (cf_norm_factor): b, x are device pointers.
 double norm_factor(Matrix *m, const double *b, const double *x, int norm_type, bool ref)
 {
     Context *ctx = m->ctx;
     require(m->n > 0, CF_BAD_INPUT, "empty matrix");
+    const GridCap small(ctx, m->n);
     const int cap = stage_cap_for(m);
     const int stride = std::max(ctx->ref_grid, ctx->sm_count * 8);
     ctx->partials.ensure(sizeof(double) * kMaxNV * (size_t)stride);
@@ -592,6 +603,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
             "bad reduction");
     const int n = m->n;
     require(n > 0, CF_BAD_INPUT, "empty matrix");
+    const GridCap small(ctx, n);
     const bool mixed = c.precision == CF_PREC_MIXED;
     require(c.precision == CF_PREC_FP64 || mixed, CF_BAD_INPUT, "bad precision");
     require(!mixed || mixed_supported(solver), CF_UNSUPPORTED,
@@ -631,6 +643,31 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     if (want_hist) ctx->hist.ensure(sizeof(double) * (size_t)hist_cap);
     const bool hist_time = want_hist && c.history_time != 0;
     if (hist_time) ctx->hist_t.ensure(sizeof(unsigned long long) * (size_t)hist_cap);
+
+    // ---- a small system's CG: one cluster-persistent launch -------------
+    // (kernel boundaries, not bytes, set a small system's step time; the
+    // batched kernel runs the whole solve behind hardware cluster barriers)
+    if (solver == CF_CG && !ref && !mixed && !tr && n <= kSmallCgRows && !want_hist &&
+        c.time_limit_s <= 0 && c.profile_kernels == 0 && c.rel_tol == 0 && c.min_iter <= 0 &&
+        c.norm_type == CF_NORM_REFERENCE_L2 && !c.absolute_tolerance) {
+        const SmallSolveResult R = solve_cg_single_cluster(m, c, b, x, ctx->vec[2].as<double>(),
+                                                           ctx->vec[4].as<double>(), ctx->vec[6].as<double>());
+        if (c.memory == CF_MEM_HOST) download(ctx, x_io, x, sizeof(double) * n, CF_MEM_HOST);
+        CF_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (perf) {
+            *perf = cf_perf{};
+            perf->norm_factor = R.nf;
+            perf->initial_residual_abs = R.norm0;
+            perf->final_residual_abs = R.norm;
+            perf->initial_residual = R.norm0 / R.nf;
+            perf->final_residual = R.norm / R.nf;
+            perf->n_iterations = R.iters;
+            perf->status = R.status;
+            perf->solve_ms = R.ms;
+            perf->true_residual = -1.0;
+        }
+        return;
+    }
 
     SolveArgs &A = *ctx->h_args;
     A = SolveArgs{};

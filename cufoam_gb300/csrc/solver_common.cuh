@@ -286,6 +286,15 @@ static void launch_body(Context *ctx, cudaStream_t s, const Kernels &kk, int cap
     if (kk.k2) launch(ctx, s, kk.k2, launch_cfg(ctx, kk.k2, kk.k2_spmv, cap, ref, kk.value_bytes), args, pdl);
 }
 
+// Solver steps captured per pass of the device-driven loop (fewer
+// evaluations of the conditional node; measured on GB300, 8 against 1: CG
+// 19.2 -> 16.7 us per step at 64^2, 84.5 -> 81.6 at 128^3; Jacobi 65.4 ->
+// 62.2 at 128^3).  A solve that converges mid-pass launches at most 7 steps
+// of kernels that return at once.
+#ifndef CF_LOOP_UNROLL
+#define CF_LOOP_UNROLL 8
+#endif
+
 static bool build_loop_graph(Context *ctx, const Kernels &kk, int cap, bool ref, SolveArgs *d_args,
                              bool pdl, GraphEntry &ge)
 {
@@ -306,7 +315,9 @@ static bool build_loop_graph(Context *ctx, const Kernels &kk, int cap, bool ref,
         CF_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         CF_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal));
-        launch_body(ctx, cs, kk, cap, ref, d_args, pdl);
+        // CF_LOOP_UNROLL steps per evaluation of the loop condition: the
+        // kernels of steps past convergence return at once (CF_EXIT_IF_DONE)
+        for (int u = 0; u < CF_LOOP_UNROLL; ++u) launch_body(ctx, cs, kk, cap, ref, d_args, pdl);
         cudaGraph_t out = nullptr;
         CF_CUDA(cudaStreamEndCapture(cs, &out));
         CF_CUDA(cudaStreamDestroy(cs));
@@ -340,7 +351,7 @@ static bool build_loop_graph(Context *ctx, const Kernels &kk, int cap, bool ref,
 static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int precision, int cap,
                               bool ref, SolveArgs *d_args, int format = 0)
 {
-    GraphKey key{solver, precision, ref ? 1 : 0, cap, 0, format};
+    GraphKey key{solver, precision, ref ? 1 : 0, cap, 0, format, ref ? 0 : ctx->grid_cap};
     auto it = ctx->graphs.find(key);
     if (it != ctx->graphs.end()) return &it->second;
     GraphEntry ge;

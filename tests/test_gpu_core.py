@@ -345,3 +345,31 @@ def test_spmv_async_into_device_buffer(ctx):
     with pytest.raises(ValueError):
         M.spmv(x, out=yd)
 
+
+
+@pytest.mark.parametrize("fmt", ["sell", "csr"])
+@pytest.mark.parametrize("case", ["c1", "lognormal3d", "lognormal_nonzero_x0"])
+def test_small_system_cg_single_launch(ctx, case, fmt):
+    """CG on a small system without a residual history runs as one
+    cluster-persistent launch (a different summation order again): same
+    normFactor and initial residual to rounding, iterations within the fast
+    order's slack, the answer's true residual at the tolerance."""
+    import torch
+    L = O.grid_const(64, 64, 1) if case == "c1" else O.grid_lognormal(18, 16, 14, 5)
+    tol, maxit = (1e-6, 40000) if case == "c1" else (1e-9, 40000)
+    b = O.uniform(3, L.n)
+    x0 = np.zeros(L.n) if case != "lognormal_nonzero_x0" else O.uniform(9, L.n)
+    want = O.plugin_solve(O.CG, L, b, x0, tol, maxit)
+    M = _matrix(ctx, L)
+    M.set_format(fmt)
+    for where in ("host", "device"):
+        psi = x0.copy() if where == "host" else torch.from_numpy(x0.copy()).cuda()
+        src = b if where == "host" else torch.from_numpy(b).cuda()
+        perf = cf.cuFoamCG("p", M, {"tolerance": tol, "maxIter": maxit}).solve(psi, src)
+        out = psi if where == "host" else psi.cpu().numpy()
+        assert abs(perf.n_iterations - want.n_iterations) <= fast_order_iteration_slack(want.n_iterations)
+        assert abs(perf.norm_factor - want.norm_factor) <= 1e-13 * want.norm_factor
+        assert abs(perf.initial_residual - want.initial_residual) <= 1e-13 * want.initial_residual
+        assert perf.converged and perf.final_residual <= tol
+        true_rel = O.true_residual_norm(O.ldu2csr(L), b, out) / perf.norm_factor
+        assert true_rel <= 1.5 * tol
