@@ -326,7 +326,10 @@ def run_ours(args):
     bytes_total = sum(solve_bytes(mat_it, mat_csr, n, k) for k in its) * world
     csr_equiv = sum(solve_bytes(mat_csr, mat_csr, n, k) for k in its) * world
     value = bytes_total / (ms * 1e-3) / 1e9
-    launches = sum(5 + 3 * k for k in its)  # nf_sum, nf_dist, res_init, 3/iter, flush, clear
+    # nf_sum, nf_dist, res_init, flush, clear, and 3 kernels per step in
+    # passes of 8 steps (the steps of the last pass past convergence return
+    # at once)
+    launches = sum(5 + 3 * 8 * ((k + 7) // 8) for k in its)
 
     # ---- e2e through the public API with pinned host buffers -------------
     # What the plugin does per cuFoamCG::solve in a running case (its device

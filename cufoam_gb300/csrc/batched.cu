@@ -1029,6 +1029,33 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
 #define CF_SMALL_CG_ROWS_PER_CTA 256
 #endif
 
+// Whether a 16-CTA cluster of the single-system kernel fits on this device
+// (asked once per context; the solve takes the multi-kernel loop otherwise).
+bool small_cg_ok(Context *ctx)
+{
+    if (ctx->small_cg_ok < 0) {
+        const auto kernel = k_batch_cg<1, 256, false>;
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 16;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.blockDim = dim3(256);
+        cfg.gridDim = dim3(16);
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        const bool ok = cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                             1) == cudaSuccess &&
+                        cudaOccupancyMaxActiveClusters(&nclusters, (void *)kernel, &cfg) == cudaSuccess &&
+                        nclusters >= 1;
+        cudaGetLastError();
+        ctx->small_cg_ok = ok ? 1 : 0;
+    }
+    return ctx->small_cg_ok == 1;
+}
+
 // CG (FP64, the fast summation order) on one system with the batched
 // kernel: one cluster of up to 16 CTAs runs normFactor, the initial residual
 // and every step, with hardware cluster barriers where the multi-kernel

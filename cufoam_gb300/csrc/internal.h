@@ -186,6 +186,7 @@ struct Context {
     // > 0: fast-order launches use at most this many blocks (a small
     // system, see GridCap); the reference order keeps the reference's grid
     int grid_cap = 0;
+    int small_cg_ok = -1;      // 16-CTA clusters schedulable (-1: not asked yet)
 
     int fast_grid(const void *kernel, size_t dyn_smem) const;
     ~Context();
@@ -275,6 +276,7 @@ struct SmallSolveResult {
 };
 SmallSolveResult solve_cg_single_cluster(Matrix *m, const cf_controls &c, const double *b, double *x,
                                          double *r, double *p, double *q);
+bool small_cg_ok(Context *ctx);
 
 struct Batch;
 Batch *batch_create(Context *ctx, int n_systems, const cf_ldu_view *views);

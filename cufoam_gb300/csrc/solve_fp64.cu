@@ -649,7 +649,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     // batched kernel runs the whole solve behind hardware cluster barriers)
     if (solver == CF_CG && !ref && !mixed && !tr && n <= kSmallCgRows && !want_hist &&
         c.time_limit_s <= 0 && c.profile_kernels == 0 && c.rel_tol == 0 && c.min_iter <= 0 &&
-        c.norm_type == CF_NORM_REFERENCE_L2 && !c.absolute_tolerance) {
+        c.norm_type == CF_NORM_REFERENCE_L2 && !c.absolute_tolerance && small_cg_ok(ctx)) {
         const SmallSolveResult R = solve_cg_single_cluster(m, c, b, x, ctx->vec[2].as<double>(),
                                                            ctx->vec[4].as<double>(), ctx->vec[6].as<double>());
         if (c.memory == CF_MEM_HOST) download(ctx, x_io, x, sizeof(double) * n, CF_MEM_HOST);
