@@ -25,8 +25,12 @@
 // Mixed precision (k_batch_cg<R, BT, true>): after the FP64 normFactor and
 // residual, each refinement sweep solves A e = r / ||r|| by CG with FP32
 // values, FP32 vectors and FP32 per-thread sums (combined across threads
-// and CTAs in FP64) to a relative inner tolerance, then adds ||r|| e to x and forms the
-// FP64 residual b - A x again; the FP64 tolerance decides convergence.
+// and CTAs in FP64) to a relative inner tolerance, then adds ||r|| e to x
+// and forms the FP64 residual b - A x again; the FP64 tolerance decides
+// convergence.
+//
+// The same kernel with one system and one component is the single-launch
+// CG of small systems (solve_cg_single_cluster, at the end of this file).
 #include <cooperative_groups.h>
 
 #include "device.cuh"
