@@ -263,6 +263,27 @@ def reference_gpu_cg(A, b):
         return {"unavailable": repr(e)}
 
 
+def max_over_ranks(value: float, dist, device: str) -> float:
+    """The largest of every rank's `value` (the job's time is its slowest
+    rank's); the value itself without a process group."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(value: float, dist, device: str) -> float:
+    """The sum of every rank's `value` (work done by the whole job)."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def run_ours(args):
     import torch
 
@@ -318,13 +339,11 @@ def run_ours(args):
     if dist:
         dist.barrier()
     clock_info = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    bytes_total = sum(solve_bytes(mat_it, mat_csr, n, k) for k in its) * world
-    csr_equiv = sum(solve_bytes(mat_csr, mat_csr, n, k) for k in its) * world
+    dev = f"cuda:{device}"
+    ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
+    # replicas: every rank solves its own copy; the job's work is the sum
+    bytes_total = sum_over_ranks(sum(solve_bytes(mat_it, mat_csr, n, k) for k in its), dist, dev)
+    csr_equiv = sum_over_ranks(sum(solve_bytes(mat_csr, mat_csr, n, k) for k in its), dist, dev)
     value = bytes_total / (ms * 1e-3) / 1e9
     # nf_sum, nf_dist, res_init, flush, clear, and 3 kernels per step in
     # passes of 8 steps (the steps of the last pass past convergence return
@@ -369,12 +388,9 @@ def run_ours(args):
         dist.barrier()
     t0 = time.perf_counter()
     e_its = [e2e_step().n_iterations for _ in range(max(1, args.steps))]
-    e_dt = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e_dt], device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e_dt = float(t.item())
-    e2e_value = sum(solve_bytes(mat_it, mat_csr, n, k) for k in e_its) * world / e_dt / 1e9
+    e_dt = max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{device}")
+    e2e_value = sum_over_ranks(sum(solve_bytes(mat_it, mat_csr, n, k) for k in e_its), dist,
+                               f"cuda:{device}") / e_dt / 1e9
     first_call()
     t0 = time.perf_counter()
     f_its = first_call().n_iterations
