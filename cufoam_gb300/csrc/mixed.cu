@@ -4,8 +4,8 @@
 // normFactor and the stopping test.
 //
 // Outer step j:  r = b - A x (FP64);  solve A d = r / ||r|| in FP32 to a
-// relative tolerance eta (CG, BiCG or MR, same fused kernels as FP64 with
-// float data);  x += ||r|| d (FP64).  The loop stops when the FP64 residual
+// relative tolerance eta (CG and MR: the same fused passes as FP64 with
+// float data; BiCG: BiCGStab, see below);  x += ||r|| d (FP64).  The loop stops when the FP64 residual
 // reaches tolerance * normFactor, so the answer carries the FP64 tolerance.
 // FP32 halves the bytes of every vector stream and cuts the matrix from 12
 // to 8 bytes per entry.
@@ -175,65 +175,107 @@ __global__ void __launch_bounds__(kBlock) k_mx_flush(const SolveArgs *__restrict
     CF_FOR_ELEMS(i, n) d[i] = fma_t(xi, p[i], d[i]);
 }
 
-// BiCG: q = A32 p and q* = A32^T p* over the shared pattern
-template <int FMT>
-__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS - 1) k_mx_bicg_spmv(const SolveArgs *__restrict__ a)
+// BiCG's FP32 inner solver is BiCGStab (van der Vorst): FP32 BiCG loses
+// the bi-orthogonality of its two sequences and diverges on the
+// convection-diffusion systems where FP64 BiCG converges, BiCGStab in FP32
+// reaches the inner tolerance.  The outer FP64 loop is BiCG's own stopping
+// test on the true residual.  One step is four passes:
+//   K0  p = r + beta (p - omega v)                       (first step: p = r)
+//   K1  v = A p, alpha = rho / (r^, v)
+//   K2  s = r - alpha v (formed for every gathered column), t = A s,
+//       omega = (t, s) / (t, t)
+//   K3  d += alpha p + omega s, r = s - omega t, rho' = (r^, r), ||r||
+// with r^ the fixed shadow residual (the scaled r of the sweep's start).
+__global__ void __launch_bounds__(kBlock) k_mx_bcs_prep(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     CF_EXIT_IF_DONE(a, st, false);
+    const int n = a->n;
     const int k = ld_cg(&st->k) + 1;
-    const bool first = (k == 1);
-    const float theta = (float)ld_cg(&st->theta);
-    const float xi_prev = (float)ld_cg(&st->xi);
-    const bool xpend = ld_cg(&st->x_pending) != 0;
-    const float *pin = a->fp[(k + 1) & 1], *psin = a->fps[(k + 1) & 1];
-    float *pout = a->fp[k & 1], *psout = a->fps[k & 1];
-    const float *r = a->fr, *rs = a->frs;
-    float *d = a->fx, *q = a->fq, *qs = a->fqs;
-    auto gp = [&](int c) { return first ? r[c] : fma_t(theta, pin[c], r[c]); };
-    auto gps = [&](int c) { return first ? rs[c] : fma_t(theta, psin[c], rs[c]); };
+    const float *__restrict__ r = a->fr;
+    float *__restrict__ p = a->fp[0];
+    if (k == 1) {
+        CF_FOR_ELEMS(i, n) p[i] = r[i];
+        return;
+    }
+    const float beta = (float)ld_cg(&st->theta);
+    const float w = (float)ld_cg(&st->omega);
+    const float *__restrict__ v = a->fq;
+    CF_FOR_ELEMS(i, n) p[i] = fma_t(beta, fma_t(-w, v[i], p[i]), r[i]);
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_bcs_spmv1(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st_in;
+    CF_EXIT_IF_DONE(a, st, false);
+    const float *__restrict__ p = a->fp[0];
+    const float *__restrict__ rh = a->frs;
+    float *__restrict__ v = a->fq;
     float acc[1] = {0.f};
-    for_rows2<FMT, float>(a, a->val32, a->valT32, a->s_val32, a->s_valT32, gp, gps,
-                          [&](int row, float y1, float y2) {
-                              const float pi = gp(row), psi = gps(row);
-                              pout[row] = pi;
-                              psout[row] = psi;
-                              q[row] = y1;
-                              qs[row] = y2;
-                              if (xpend) d[row] = fma_t(xi_prev, pin[row], d[row]);
-                              acc[0] = fma_t(psi, y1, acc[0]);
-                          });
+    for_rows<FMT, float>(a, a->val32, a->s_val32, [&](int c) { return p[c]; }, [&](int row, float y) {
+        v[row] = y;
+        acc[0] = fma_t(rh[row], y, acc[0]);
+    });
     float tot[1];
     if (grid_reduce<1, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_A], false,
                               tot) && threadIdx.x == 0) {
-        const float xi = (float)st->rho0 / tot[0];
-        st->x_pending = 0;
-        const double bound = st->int_bound;
-        if (!(xi > -bound && xi < bound) && isfinite(xi)) {
-            st->xi = xi;
+        const float alpha = (float)st->rho0 / tot[0];
+        if (isfinite(alpha) && tot[0] != 0.f) {
+            st->xi = alpha;
         } else {
             st->done = 1;
-            st->status = isfinite(xi) ? CF_BREAKDOWN : CF_NONFINITE;
+            st->status = tot[0] == 0.f ? CF_BREAKDOWN : CF_NONFINITE;
         }
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_mx_bicg_update(const SolveArgs *__restrict__ a)
+template <int FMT>
+__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_bcs_spmv2(const SolveArgs *__restrict__ a)
+{
+    DevState *st = a->st_in;
+    CF_EXIT_IF_DONE(a, st, false);
+    const float alpha = (float)ld_cg(&st->xi);
+    const float *__restrict__ r = a->fr;
+    const float *__restrict__ v = a->fq;
+    float *__restrict__ sv = a->fp[1];
+    float *__restrict__ t = a->fqs;
+    auto g = [&](int c) { return fma_t(-alpha, v[c], r[c]); };
+    float acc[2] = {0.f, 0.f};
+    for_rows<FMT, float>(a, a->val32, a->s_val32, g, [&](int row, float y) {
+        const float si = g(row);
+        sv[row] = si;
+        t[row] = y;
+        acc[0] = fma_t(y, si, acc[0]);
+        acc[1] = fma_t(y, y, acc[1]);
+    });
+    float tot[2];
+    if (grid_reduce<2, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_C], false,
+                              tot) && threadIdx.x == 0)
+        st->omega = tot[1] > 0.f ? tot[0] / tot[1] : 0.f;
+}
+
+__global__ void __launch_bounds__(kBlock) k_mx_bcs_update(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     CF_EXIT_IF_DONE(a, st, true);
     const int n = a->n;
-    const float xi = (float)ld_cg(&st->xi);
-    float *r = a->fr, *rs = a->frs;
-    const float *q = a->fq, *qs = a->fqs;
+    const float alpha = (float)ld_cg(&st->xi);
+    const float w = (float)ld_cg(&st->omega);
+    const float *__restrict__ p = a->fp[0];
+    const float *__restrict__ sv = a->fp[1];
+    const float *__restrict__ t = a->fqs;
+    const float *__restrict__ rh = a->frs;
+    float *__restrict__ r = a->fr;
+    float *__restrict__ d = a->fx;
     float acc[2] = {0.f, 0.f};
     CF_FOR_ELEMS(i, n) {
-        const float ri = fma_t(-xi, q[i], r[i]);
-        const float rsi = fma_t(-xi, qs[i], rs[i]);
+        const float si = sv[i];
+        d[i] = fma_t(w, si, fma_t(alpha, p[i], d[i]));
+        const float ri = fma_t(-w, t[i], si);
         r[i] = ri;
-        rs[i] = rsi;
         acc[0] = fma_t(ri, ri, acc[0]);
-        acc[1] = fma_t(ri, rsi, acc[1]);
+        acc[1] = fma_t(rh[i], ri, acc[1]);
     }
     float tot[2];
     if (grid_reduce<2, float>(acc, a->partials32, a->partial_stride, &st->counters[SLOT_B], false,
@@ -242,18 +284,18 @@ __global__ void __launch_bounds__(kBlock) k_mx_bicg_update(const SolveArgs *__re
         const int k = st->k + 1;
         st->k = k;
         st->norm = norm;
-        st->x_pending = 1;
         bool cont = true;
         int status = CF_NOT_CONVERGED;
         if (norm < st->tol) { cont = false; status = CF_OK; }
         else if (k >= st->max_steps) { cont = false; }
         else if (!isfinite(norm)) { cont = false; status = CF_NONFINITE; }
+        else if (tot[1] == 0.f || w == 0.f) { cont = false; status = CF_BREAKDOWN; }
         st->body_count += 1;
         if (st->body_count > k + 2 || (a->abort_flag && *a->abort_flag)) { cont = false; status = CF_TIMEOUT; }
         if (cont) {
             st->rho1 = st->rho0;
             st->rho0 = tot[1];
-            st->theta = (float)st->rho0 / (float)st->rho1;
+            st->theta = ((float)st->rho0 / (float)st->rho1) * (alpha / w);
         } else {
             st->done = 1;
             st->status = status;
@@ -337,7 +379,13 @@ static Kernels inner_kernels_t(int solver)
     k.value_bytes = sizeof(float);
     switch (solver) {
     case CF_CG: k.k1 = (const void *)k_mx_cg_spmv<FMT>; k.k2 = (const void *)k_mx_cg_update; break;
-    case CF_BICG: k.k1 = (const void *)k_mx_bicg_spmv<FMT>; k.k2 = (const void *)k_mx_bicg_update; break;
+    case CF_BICG:
+        k.k0 = (const void *)k_mx_bcs_prep;
+        k.k1 = (const void *)k_mx_bcs_spmv1<FMT>;
+        k.k2 = (const void *)k_mx_bcs_spmv2<FMT>;
+        k.k3 = (const void *)k_mx_bcs_update;
+        k.k2_spmv = FMT == kCsr;
+        break;
     case CF_MR: k.k1 = (const void *)k_mx_mr_spmv<FMT>; k.k2 = (const void *)k_mx_mr_update; break;
     default: break;
     }
@@ -421,9 +469,8 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
     const int64_t max_total = c.max_iter <= 0 ? INT_MAX : c.max_iter;
     const int max_outer = c.mixed_max_outer > 0 ? c.mixed_max_outer : 50;
     const double eta = (c.mixed_inner_rtol > 0 && c.mixed_inner_rtol < 1) ? c.mixed_inner_rtol : 1e-4;
-    // BiCG's residual is not monotone, so its FP32 sweeps are kept short;
-    // CG and MR sweeps run to the inner tolerance
-    int inner_cap = c.mixed_inner_max > 0 ? c.mixed_inner_max : (solver == CF_BICG ? 400 : INT_MAX);
+    // every inner sweep runs to the inner tolerance unless capped
+    int inner_cap = c.mixed_inner_max > 0 ? c.mixed_inner_max : INT_MAX;
     // x and r before each correction, to undo a sweep that made things worse
     // (workspace vectors 12 and 13: unused by the mixed path otherwise)
     const size_t vb = sizeof(double) * (size_t)m->n;

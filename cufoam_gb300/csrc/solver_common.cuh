@@ -234,6 +234,7 @@ struct Kernels {
     const void *k0 = nullptr;    // element-wise prep kernel (may be null)
     const void *k1 = nullptr;    // SpMV body kernel
     const void *k2 = nullptr;    // update body kernel (may be null)
+    const void *k3 = nullptr;    // a fourth element-wise kernel (may be null)
     bool k1_spmv = false, k2_spmv = false;
     size_t value_bytes = sizeof(double);
 };
@@ -284,6 +285,7 @@ static void launch_body(Context *ctx, cudaStream_t s, const Kernels &kk, int cap
     if (kk.k0) launch(ctx, s, kk.k0, launch_cfg(ctx, kk.k0, false, cap, ref, kk.value_bytes), args, pdl);
     launch(ctx, s, kk.k1, launch_cfg(ctx, kk.k1, kk.k1_spmv, cap, ref, kk.value_bytes), args, pdl);
     if (kk.k2) launch(ctx, s, kk.k2, launch_cfg(ctx, kk.k2, kk.k2_spmv, cap, ref, kk.value_bytes), args, pdl);
+    if (kk.k3) launch(ctx, s, kk.k3, launch_cfg(ctx, kk.k3, false, cap, ref, kk.value_bytes), args, pdl);
 }
 
 // Solver steps captured per pass of the device-driven loop (fewer

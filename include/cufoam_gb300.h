@@ -128,10 +128,11 @@ typedef struct cf_controls {
     int32_t history_time;    /* 1: history holds seconds since the initial residual
                                 at the end of each step (device clock), the
                                 reference's DetailType::Time, instead of ||r||_2 */
-    int32_t mixed_inner_max; /* mixed: FP32 steps per refinement sweep; 0 = 400
-                                for BiCG, no limit for CG and MR.  A sweep that
+    int32_t mixed_inner_max; /* mixed: FP32 steps per refinement sweep; 0 = no
+                                limit (to the inner tolerance).  A sweep that
                                 raises the FP64 residual is undone and retried
-                                with half as many steps. */
+                                with half as many steps.  Mixed BiCG's FP32
+                                inner solver is BiCGStab. */
     int32_t reserved[3];
 } cf_controls;
 

@@ -248,11 +248,11 @@ def test_max_iter_cap_and_loop_semantics():
 
 
 def test_fp32_bicg_diverges_on_upwind_convection_diffusion():
-    """Why the mixed-precision BiCG cannot meet the FP64 tolerance on the
-    convection-diffusion workload: BiCG's residual grows transiently on this
-    non-normal system before it converges; in FP64 it recovers, with FP32
-    vectors and accumulation it stalls far above the FP64 level (numpy,
-    48^3, cell Peclet 10; at 64^3 and above FP32 BiCG diverges outright)."""
+    """Why mixed-precision BiCG does not use FP32 BiCG sweeps: BiCG's
+    residual grows transiently on this non-normal system before it
+    converges; in FP64 it recovers, with FP32 vectors and accumulation it
+    stalls far above the FP64 level (numpy, 48^3, cell Peclet 10; at 64^3
+    and above FP32 BiCG diverges outright)."""
     import scipy.sparse as sp
     L, _ = O.grid_convdiff(48, 48, 48, 7, 10.0)
     A = O.ldu2csr(L)
@@ -278,3 +278,40 @@ def test_fp32_bicg_diverges_on_upwind_convection_diffusion():
 
     assert bicg(np.float64, 800) < 1e-8
     assert bicg(np.float32, 800) > 1e-5
+
+
+def test_fp32_bicgstab_reaches_inner_tolerance_where_fp32_bicg_fails():
+    """The FP32 inner solver of mixed BiCG is BiCGStab: on the same system
+    (48^3, cell Peclet 10) FP32 BiCGStab reaches a 1e-4 relative residual,
+    which one FP64 refinement sweep then needs, while FP32 BiCG (previous
+    test) stalls above 1e-5."""
+    import scipy.sparse as sp
+    L, _ = O.grid_convdiff(48, 48, 48, 7, 10.0)
+    A = O.ldu2csr(L)
+    M = sp.csr_matrix((A.vals, A.cols, A.row_offsets), shape=(L.n, L.n))
+    b = O.uniform(8, L.n)
+    Ms = M.astype(np.float32)
+    r = b.astype(np.float32) / np.float32(np.linalg.norm(b))
+    rh = r.copy()
+    x = np.zeros(L.n, np.float32)
+    p = r.copy()
+    v = np.zeros(L.n, np.float32)
+    rho, alpha, w = np.dot(rh, r), np.float32(1), np.float32(1)
+    steps = 0
+    for k in range(1, 2000):
+        if k > 1:
+            p = r + (rho / rho_old) * (alpha / w) * (p - w * v)
+        v = Ms @ p
+        alpha = rho / np.dot(rh, v)
+        s = r - alpha * v
+        t = Ms @ s
+        w = np.dot(t, s) / np.dot(t, t)
+        x += alpha * p + w * s
+        r = s - w * t
+        rho_old, rho = rho, np.dot(rh, r)
+        steps = k
+        if np.linalg.norm(r) < 1e-4:
+            break
+    bn = b / np.linalg.norm(b)
+    true_rel = np.linalg.norm(bn - M @ x.astype(np.float64))
+    assert steps < 2000 and true_rel < 2e-4
