@@ -440,7 +440,7 @@ class LduSolver:
         c.richardson_omega = float(d.get("omega", 0.0))
         c.power_max_steps = int(d.get("powerMaxSteps", 30))
         c.mixed_max_outer = int(d.get("maxRefinements", 50))
-        c.mixed_inner_rtol = float(d.get("innerRelTol", 1e-4))
+        c.mixed_inner_rtol = float(d.get("innerRelTol", 0.0))   # 0: the solver's default
         c.mixed_inner_max = int(d.get("innerMaxIter", 0))
         c.use_graph = int(d.get("useGraph", 1))
         c.time_limit_s = float(d.get("timeLimit", 0.0))

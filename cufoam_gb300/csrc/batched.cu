@@ -949,7 +949,7 @@ void batch_solve(Batch *B, const cf_controls &c, int nrhs, const double *b_in, d
     a.p32 = mixed ? B->d_p32.as<float>() : nullptr;
     a.q32 = mixed ? B->d_q32.as<float>() : nullptr;
     a.e32 = mixed ? B->d_e32.as<float>() : nullptr;
-    a.inner_rtol = (c.mixed_inner_rtol > 0 && c.mixed_inner_rtol < 1) ? c.mixed_inner_rtol : 1e-4;
+    a.inner_rtol = (c.mixed_inner_rtol > 0 && c.mixed_inner_rtol < 1) ? c.mixed_inner_rtol : 1e-6;
     a.max_outer = c.mixed_max_outer > 0 ? c.mixed_max_outer : 50;
     const int cs = cfg && cfg->cluster_size > 0 ? cfg->cluster_size : 0;   // 0: 16, else 8
     const int bt = cfg && cfg->threads > 0 ? cfg->threads : 256;

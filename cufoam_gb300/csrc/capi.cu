@@ -309,7 +309,7 @@ void cf_controls_init(cf_controls *c)
     c->richardson_omega = 0.0;   // cuFoamRichardson/cuFoamRichardson.C:66
     c->power_max_steps = 30;
     c->mixed_max_outer = 50;
-    c->mixed_inner_rtol = 1e-4;
+    c->mixed_inner_rtol = 0.0; // the solver's default
     c->history = nullptr;
     c->history_capacity = 0;
     c->use_graph = 1;
