@@ -115,7 +115,8 @@ struct SolveArgs {
     double *qs;
     double *w[2];
     // vectors (FP32, mixed precision inner solve)
-    float *fx, *fr, *fp[2], *fq, *frs, *fps[2], *fqs, *fb;
+    float *fx, *fr, *fp[2], *fq, *frs, *fps[2], *fqs;
+    const double *corr_scale;  // mixed MR family: x += s * corr_scale * d (1 / a_ii or sqrt(1 / a_ii))
     // reductions / state
     double *partials;          // [kMaxNV][partial_stride]
     float *partials32;
@@ -174,6 +175,7 @@ struct Context {
     // workspace (grow-only, reused by every solve)
     DeviceBuffer vec[24];
     DeviceBuffer partials, partials32, hist, hist_t, state, state_in, args;
+    DeviceBuffer scaled32;     // FP32 diagonally scaled matrix of a mixed MR-family solve
     SolveArgs *h_args = nullptr;   // pinned
     DevState *h_state = nullptr;   // pinned
     DevState *h_state_in = nullptr; // pinned

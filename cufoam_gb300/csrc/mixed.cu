@@ -5,8 +5,10 @@
 //
 // Outer step j:  r = b - A x (FP64);  solve A d = r / ||r|| in FP32 to a
 // relative tolerance eta (CG and MR: the same fused passes as FP64 with
-// float data; BiCG: BiCGStab, see below);  x += ||r|| d (FP64).  The loop stops when the FP64 residual
-// reaches tolerance * normFactor, so the answer carries the FP64 tolerance.
+// float data; MRJacobi, MRS, JMR: MR on a diagonally scaled matrix; BiCG:
+// BiCGStab, see below);  x += ||r|| d (FP64).  The loop stops when the FP64
+// residual reaches tolerance * normFactor, so the answer carries the FP64
+// tolerance.
 // FP32 halves the bytes of every vector stream and cuts the matrix from 12
 // to 8 bytes per entry.
 #include "solver_common.cuh"
@@ -27,25 +29,66 @@ namespace cf {
 // ---------------------------------------------------------------------------
 // FP64 pieces of the outer loop
 // ---------------------------------------------------------------------------
-// x += s * d with s = ||r|| of the residual the inner system was scaled by.
+// x += s * d with s = ||r|| of the residual the inner system was scaled by
+// (MR family: x += s * R d, R the column scaling of the inner matrix).
 __global__ void __launch_bounds__(kBlock) k_mx_correct(const SolveArgs *__restrict__ a)
 {
     const int n = a->n;
     const double s = ld_cg(&a->st->norm);
     const float *d = a->fx;
+    const double *R = a->corr_scale;
     double *x = a->x;
-    CF_FOR_ELEMS(i, n) x[i] = fma_t(s, (double)d[i], x[i]);
+    CF_FOR_ELEMS(i, n) {
+        double di = (double)d[i];
+        if (R) di *= R[i];
+        x[i] = fma_t(s, di, x[i]);
+    }
 }
 
-// r = b - A x, ||r|| (FP64); records the outer step.
-template <int FMT>
+// FP32 values of L A R (L, R diagonal, L = null: the identity) on A's
+// pattern, over the SELL-32 slots (padding stays 0) ...
+__global__ void __launch_bounds__(kBlock) k_mx_scaled_sell(int n, int n_slices, const int32_t *__restrict__ soff,
+                                                           const int32_t *__restrict__ scol,
+                                                           const double *__restrict__ sval,
+                                                           const double *__restrict__ L,
+                                                           const double *__restrict__ R, float *__restrict__ out)
+{
+    CF_FOR_ELEMS(i, 32 * n_slices) {
+        const int sl = i >> 5, lane = i & 31;
+        const int b = soff[sl], len = (soff[sl + 1] - b) >> 5;
+        const double li = (L && i < n) ? L[i] : 1.0;
+        for (int t = 0; t < len; ++t) {
+            const int o = b + 32 * t + lane;
+            const double v = sval[o];
+            out[o] = v == 0.0 ? 0.f : (float)(li * v * R[scol[o]]);
+        }
+    }
+}
+
+// ... or over the CSR entries
+__global__ void __launch_bounds__(kBlock) k_mx_scaled_csr(int n, const int32_t *__restrict__ ro,
+                                                          const int32_t *__restrict__ col,
+                                                          const double *__restrict__ val,
+                                                          const double *__restrict__ L,
+                                                          const double *__restrict__ R, float *__restrict__ out)
+{
+    CF_FOR_ELEMS(i, n) {
+        const double li = L ? L[i] : 1.0;
+        for (int j = ro[i]; j < ro[i + 1]; ++j) out[j] = (float)(li * val[j] * R[col[j]]);
+    }
+}
+
+// r = b - A x, ||r|| (FP64); records the outer step.  SCALED (JMR, whose
+// residual is the symmetrically scaled one): r = D^-1/2 (b - A x).
+template <int FMT, bool SCALED>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_mx_residual(const SolveArgs *__restrict__ a)
 {
-    const double *x = a->x, *b = a->b;
+    const double *x = a->x, *b = a->b, *sD = a->dinv_sqrt;
     double *r = a->r[0];
     double acc[1] = {0.0};
     for_rows<FMT, double>(a, a->val, a->s_val, [&](int c) { return x[c]; }, [&](int row, double t) {
-        const double ri = b[row] - t;
+        double ri = b[row] - t;
+        if (SCALED) ri = __dmul_rn(sD[row], ri);
         r[row] = ri;
         acc[0] = fma_t(ri, ri, acc[0]);
     });
@@ -386,7 +429,10 @@ static Kernels inner_kernels_t(int solver)
         k.k3 = (const void *)k_mx_bcs_update;
         k.k2_spmv = FMT == kCsr;
         break;
-    case CF_MR: k.k1 = (const void *)k_mx_mr_spmv<FMT>; k.k2 = (const void *)k_mx_mr_update; break;
+    case CF_MR:
+    case CF_MRJACOBI: // the preconditioned MR solvers run MR on a scaled matrix
+    case CF_MRS:
+    case CF_JMR: k.k1 = (const void *)k_mx_mr_spmv<FMT>; k.k2 = (const void *)k_mx_mr_update; break;
     default: break;
     }
     k.k1_spmv = FMT == kCsr;   // the SELL passes stage nothing
@@ -398,27 +444,70 @@ static Kernels inner_kernels(int solver, bool sell)
     return sell ? inner_kernels_t<kSell>(solver) : inner_kernels_t<kCsr>(solver);
 }
 
-bool mixed_supported(int solver) { return solver == CF_CG || solver == CF_BICG || solver == CF_MR; }
+// The diagonally preconditioned MR solvers.  Their FP32 sweep is MR on a
+// scaled matrix: MRJacobi's and MRS's step y = A D^-1 r, x += w D^-1 r is
+// MR on A D^-1 with x = D^-1 x'; JMR's y = D^-1/2 A D^-1/2 r on the scaled
+// residual r = D^-1/2 (b - A x), x += w D^-1/2 r is MR on D^-1/2 A D^-1/2
+// with x = D^-1/2 x'.  The same iterates in exact arithmetic, two passes a
+// step and no preconditioned vector: the scaling is paid once per solve
+// (a matrix-sized pass) and once per sweep (in the correction of x).
+static bool mr_precond(int solver) { return solver == CF_MRJACOBI || solver == CF_MRS || solver == CF_JMR; }
+
+bool mixed_supported(int solver)
+{
+    return solver == CF_CG || solver == CF_BICG || solver == CF_MR || mr_precond(solver);
+}
 
 void mixed_prepare(Context *ctx, Matrix *m, int solver, SolveArgs &A)
 {
     require(mixed_supported(solver), CF_UNSUPPORTED,
-            "mixed precision is implemented for CG, BiCG and MR");
+            "mixed precision is implemented for CG, BiCG, MR, MRJacobi, MRS and JMR");
     const bool tr = A.val != m->val.as<double>(); // transposed solve
-    matrix_ensure_fp32(m, false);
-    if (solver == CF_BICG || tr) matrix_ensure_fp32(m, true);
+    const bool scaled = mr_precond(solver);
+    if (!scaled) {
+        matrix_ensure_fp32(m, false);
+        if (solver == CF_BICG || tr) matrix_ensure_fp32(m, true);
+    }
     const size_t fb = sizeof(float) * ((size_t)m->n + 16);
     for (int i = 14; i < 24; ++i) ctx->vec[i].ensure(fb);
     const int stride = std::max(ctx->ref_grid, ctx->sm_count * 8);
     ctx->partials32.ensure(sizeof(float) * kMaxNV * (size_t)stride);
     ctx->state_in.ensure(sizeof(DevState));
-    A.val32 = m->val32.as<float>();
-    A.valT32 = m->have_T32 ? m->valT32.as<float>() : nullptr;
-    if (tr) std::swap(A.val32, A.valT32);
-    if (A.n_slices > 0) { // SELL-32 copies (FP32 values filled by the caller's matrix_ensure_sell)
-        A.s_val32 = m->s_val32.as<float>();
-        A.s_valT32 = m->have_svalT32 ? m->s_valT32.as<float>() : nullptr;
-        if (tr) std::swap(A.s_val32, A.s_valT32);
+    A.corr_scale = nullptr;
+    if (scaled) {
+        // FP32 L A R of the solved matrix (A^T for a transposed solve: A.val
+        // and A.s_val point at its values), refreshed every solve since the
+        // values change between solves
+        const double *L = solver == CF_JMR ? A.dinv_sqrt : nullptr;
+        const double *R = solver == CF_JMR ? A.dinv_sqrt : A.dinv;
+        const int n = m->n;
+        DeviceBuffer &buf = ctx->scaled32;
+        if (A.n_slices > 0) {
+            buf.ensure(sizeof(float) * ((size_t)m->sell_nnz + 32));
+            k_mx_scaled_sell<<<launch_cfg(ctx, (const void *)k_mx_scaled_sell, false, 0, false).grid, kBlock, 0,
+                               ctx->stream>>>(n, A.n_slices, A.s_off, A.s_col, A.s_val, L, R, buf.as<float>());
+            A.s_val32 = buf.as<float>();
+            A.val32 = nullptr;
+        } else {
+            buf.ensure(sizeof(float) * ((size_t)m->nnz + 4));
+            CF_CUDA(cudaMemsetAsync(buf.as<float>() + m->nnz, 0, sizeof(float) * 4, ctx->stream));
+            k_mx_scaled_csr<<<launch_cfg(ctx, (const void *)k_mx_scaled_csr, false, 0, false).grid, kBlock, 0,
+                              ctx->stream>>>(n, A.ro, A.col, A.val, L, R, buf.as<float>());
+            A.val32 = buf.as<float>();
+            A.s_val32 = nullptr;
+        }
+        CF_CUDA(cudaGetLastError());
+        A.valT32 = A.s_valT32 = nullptr;
+        A.corr_scale = R;
+    } else {
+        A.val32 = m->val32.as<float>();
+        A.valT32 = m->have_T32 ? m->valT32.as<float>() : nullptr;
+        if (tr) std::swap(A.val32, A.valT32);
+        if (A.n_slices > 0) { // SELL-32 copies (FP32 values filled by the caller's matrix_ensure_sell)
+            A.s_val32 = m->s_val32.as<float>();
+            A.s_valT32 = m->have_svalT32 ? m->s_valT32.as<float>() : nullptr;
+            if (tr) std::swap(A.s_val32, A.s_valT32);
+        }
     }
     A.fx = ctx->vec[14].as<float>();
     A.fr = ctx->vec[15].as<float>();
@@ -447,7 +536,11 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
     void *args1[] = {&d_args};
     const bool sell = A.n_slices > 0;
     const Kernels kk = inner_kernels(solver, sell);
-    const void *k_residual = sell ? (const void *)k_mx_residual<kSell> : (const void *)k_mx_residual<kCsr>;
+    const bool scaled = solver == CF_JMR;
+    const void *k_residual = sell ? (scaled ? (const void *)k_mx_residual<kSell, true>
+                                            : (const void *)k_mx_residual<kSell, false>)
+                                  : (scaled ? (const void *)k_mx_residual<kCsr, true>
+                                            : (const void *)k_mx_residual<kCsr, false>);
     bool use_graph = use_graph_in;
     GraphEntry *ge = nullptr;
     if (use_graph) {
@@ -509,7 +602,7 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
                 if (SI.done) break;
             }
         }
-        if (solver != CF_MR)
+        if (solver == CF_CG || solver == CF_BICG)
             launch(ctx, ctx->stream, (const void *)k_mx_flush,
                    launch_cfg(ctx, (const void *)k_mx_flush, false, cap, false), args1);
         CF_CUDA(cudaMemcpyAsync(x_keep, A.x, vb, cudaMemcpyDeviceToDevice, ctx->stream));

@@ -607,7 +607,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     const bool mixed = c.precision == CF_PREC_MIXED;
     require(c.precision == CF_PREC_FP64 || mixed, CF_BAD_INPUT, "bad precision");
     require(!mixed || mixed_supported(solver), CF_UNSUPPORTED,
-            "mixed precision is implemented for CG, BiCG and MR");
+            "mixed precision is implemented for CG, BiCG, MR, MRJacobi, MRS and JMR");
     require(solver != CF_PCG || (!mixed && c.transpose == 0), CF_UNSUPPORTED,
             "the preconditioned CG is FP64 only");
     require(solver != CF_PCG || c.reduction == CF_REDUCE_FAST, CF_UNSUPPORTED,
@@ -620,7 +620,9 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     // both orders read the SELL-32 copy when the pattern suits it (FP32
     // values too for the mixed inner solve); the reference order takes its
     // 8-lane row sums from the SELL slots (RefRow), the same bits as from CSR
-    const bool sell = matrix_ensure_sell(m, solver == CF_BICG || tr, mixed);
+    // (the mixed MR family's FP32 values are a scaled matrix, made per solve)
+    const bool fp32_copy = mixed && (solver == CF_CG || solver == CF_BICG || solver == CF_MR);
+    const bool sell = matrix_ensure_sell(m, solver == CF_BICG || tr, fp32_copy);
 
     // ---- vectors -------------------------------------------------------
     double *x, *b;
@@ -774,7 +776,8 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     }
     // ---- initial residual ----------------------------------------------
     {
-        int mode = mixed ? 0 : (solver == CF_JMR ? 1 : (solver == CF_BICG ? 2 : (solver == CF_PCG ? 3 : 0)));
+        // (the mixed JMR loop keeps the scaled residual as well)
+        int mode = solver == CF_JMR ? 1 : mixed ? 0 : (solver == CF_BICG ? 2 : (solver == CF_PCG ? 3 : 0));
         void *a2[] = {&d_args, &mode};
         launch(ctx, ctx->stream, (const void *)k_res_init,
                launch_cfg(ctx, (const void *)k_res_init, !sell, cap, ref), a2);

@@ -62,7 +62,8 @@ enum { CF_MEM_HOST = 0, CF_MEM_DEVICE = 1 };
 enum {
     CF_PREC_FP64 = 0,  /* FP64 values, vectors and reductions (the reference's) */
     CF_PREC_MIXED = 1  /* FP32 matrix/vectors/accumulation inside an FP64
-                          iterative-refinement loop (CG, BiCG, MR only) */
+                          iterative-refinement loop (CG, BiCG, MR, MRJacobi,
+                          MRS and JMR) */
 };
 
 /* Reduction order of dot products in FP64 solves. */
@@ -117,7 +118,7 @@ typedef struct cf_controls {
     int32_t mixed_max_outer; /* mixed: refinement sweeps limit, default 50 */
     double mixed_inner_rtol; /* mixed: inner FP32 relative tolerance; 0 (the
                                 default) = 1e-6 for CG (batched too), 1e-4 for
-                                BiCG and MR, the fastest measured */
+                                BiCG and the MR family, the fastest measured */
     double *history;         /* optional HOST buffer: absolute ||r||_2 per step */
     int32_t history_capacity;
     int32_t use_graph;       /* 1 (default): device-driven loop in a CUDA graph */

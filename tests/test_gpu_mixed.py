@@ -10,13 +10,21 @@ import oracle as O
 pytestmark = pytest.mark.gpu
 
 
-def _true_rel(L, b, x, nf):
-    return O.true_residual_norm(O.ldu2csr(L), b, x) / nf
+def _true_rel(L, b, x, nf, scaled=False):
+    A = O.ldu2csr(L)
+    if not scaled:
+        return O.true_residual_norm(A, b, x) / nf
+    # JMR's residual: D^-1/2 (b - A x)
+    r = b - O.ref_spmv(A, x)
+    return np.linalg.norm(r / np.sqrt(np.asarray(L.diag, np.float64))) / nf
 
 
 @pytest.mark.parametrize("name,make", [
     ("BiCG", lambda: O.grid_convdiff(32, 30, 28, 4, 10.0)[0]),
     ("MR", lambda: O.grid_convdiff(20, 18, 16, 5, 10.0)[0]),
+    ("MRJacobi", lambda: O.grid_convdiff(20, 18, 16, 5, 10.0)[0]),
+    ("MRS", lambda: O.grid_convdiff(20, 18, 16, 5, 10.0)[0]),
+    ("JMR", lambda: O.grid_convdiff(20, 18, 16, 5, 10.0)[0]),
     ("CG", lambda: O.grid_lognormal(32, 30, 28, 6)),
 ])
 def test_mixed_reaches_fp64_tolerance(ctx, name, make):
@@ -30,7 +38,7 @@ def test_mixed_reaches_fp64_tolerance(ctx, name, make):
     assert perf.status == 0, perf.status_name
     assert perf.n_outer >= 2
     assert perf.final_residual <= tol
-    true_rel = _true_rel(L, b, psi, perf.norm_factor)
+    true_rel = _true_rel(L, b, psi, perf.norm_factor, scaled=name == "JMR")
     assert true_rel <= tol
     # error against the FP64 oracle solution at the same tolerance
     want = O.plugin_solve(O.SOLVER_NAMES[name], L, b, np.zeros(L.n), tol, 200000)
@@ -58,3 +66,25 @@ def test_mixed_respects_max_iter(ctx):
                                 "precision": "mixed"}).solve(np.zeros(L.n), b)
     assert perf.n_iterations <= 30
     assert perf.status == 1
+
+
+@pytest.mark.parametrize("fmt", ["sell", "csr"])
+@pytest.mark.parametrize("name", ["MRJacobi", "JMR"])
+@pytest.mark.parametrize("transpose", [False, True])
+def test_mixed_mr_family_formats_and_transpose(ctx, fmt, name, transpose):
+    # the FP32 sweep of the preconditioned MR solvers runs MR on a scaled
+    # copy of the solved matrix (A or A^T), built from SELL-32 or CSR values
+    L, _ = O.grid_convdiff(14, 12, 10, 9, 4.0)
+    b = O.uniform(5, L.n)
+    tol = 1e-10
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    M.set_format(fmt)
+    psi = np.zeros(L.n)
+    perf = cf._TABLE["cuFoam" + name]("p", M, {"tolerance": tol, "maxIter": 200000,
+                                              "precision": "mixed"}).solve(psi, b, transpose=transpose)
+    assert M.format()[0] == fmt
+    assert perf.status == 0, perf.status_name
+    Ls = L.transposed() if transpose else L
+    assert _true_rel(Ls, b, psi, perf.norm_factor, scaled=name == "JMR") <= tol
+    want = O.plugin_solve(O.SOLVER_NAMES[name], Ls, b, np.zeros(L.n), tol, 200000)
+    assert np.linalg.norm(psi - want.psi) / np.linalg.norm(want.psi) < 1e-6
