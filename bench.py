@@ -435,10 +435,12 @@ def run_ours(args):
 
     extras = {}
     if world == 1 and not args.no_extras:
-        # C3 (cell Peclet 10): MR converges in both precisions; FP64 BiCG
-        # breaks down while mixed BiCG (FP32 BiCGStab sweeps) converges; at
-        # cell Peclet 1 both BiCG variants converge and the times compare
+        # C3 (cell Peclet 10): MR and MRJacobi converge in both precisions;
+        # FP64 BiCG breaks down while mixed BiCG (FP32 BiCGStab sweeps)
+        # converges; at cell Peclet 1 both BiCG variants converge and the
+        # times compare
         for key, solver, mx, pe in (("mixed_vs_fp64", "cuFoamMR", 100000, 10.0),
+                                    ("mixed_vs_fp64_mrjacobi", "cuFoamMRJacobi", 100000, 10.0),
                                     ("mixed_vs_fp64_bicg", "cuFoamBiCG", 20000, 10.0),
                                     ("mixed_vs_fp64_bicg_pe1", "cuFoamBiCG", 20000, 1.0)):
             try:
