@@ -457,6 +457,7 @@ cf_status cf_matrix_set_format(cf_matrix *m, int32_t format)
             mi->format_request = format;
             mi->sell = -1;
             mi->have_sval = mi->have_svalT = mi->have_sval32 = mi->have_svalT32 = false;
+            ++mi->gen;
         }
     });
 }

@@ -116,7 +116,8 @@ struct SolveArgs {
     double *w[2];
     // vectors (FP32, mixed precision inner solve)
     float *fx, *fr, *fp[2], *fq, *frs, *fps[2], *fqs;
-    const double *corr_scale;  // mixed MR family: x += s * corr_scale * d (1 / a_ii or sqrt(1 / a_ii))
+    const double *corr_scale;  // MR family on L A R: x += s * corr_scale * d (1 / a_ii or sqrt(1 / a_ii))
+    const double *sc_val;      // FP64 fast-order MR family: values of L A R (the format in use)
     // reductions / state
     double *partials;          // [kMaxNV][partial_stride]
     float *partials32;
@@ -175,7 +176,6 @@ struct Context {
     // workspace (grow-only, reused by every solve)
     DeviceBuffer vec[24];
     DeviceBuffer partials, partials32, hist, hist_t, state, state_in, args;
-    DeviceBuffer scaled32;     // FP32 diagonally scaled matrix of a mixed MR-family solve
     SolveArgs *h_args = nullptr;   // pinned
     DevState *h_state = nullptr;   // pinned
     DevState *h_state_in = nullptr; // pinned
@@ -216,6 +216,12 @@ struct GridCap {
     GridCap &operator=(const GridCap &) = delete;
 };
 
+struct ScaledCopy {
+    DeviceBuffer buf;
+    uint64_t gen = 0;          // Matrix::gen it was made at (0: none)
+    int scale = 0, transpose = 0, sell = 0;
+};
+
 struct Matrix {
     Context *ctx = nullptr;
     int32_t n = 0, nf = 0;
@@ -238,6 +244,11 @@ struct Matrix {
     int64_t sell_nnz = 0;      // stored entries including padding
     DeviceBuffer s_off, s_col, s_val, s_valT, s_val32, s_valT32;
     bool have_sval = false, have_svalT = false, have_sval32 = false, have_svalT32 = false;
+    // bumped by every change of the values, of 1/a_ii or of the format
+    uint64_t gen = 1;
+    // diagonally scaled values L A R of the MR family's loop (FP64 fast
+    // order, FP32 mixed sweeps), kept until `gen` or the request changes
+    ScaledCopy sc64, sc32;
 };
 
 // ---------------------------------------------------------------------------

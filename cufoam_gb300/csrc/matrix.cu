@@ -602,6 +602,7 @@ static void build_from_ldu(Context *ctx, Matrix *m, const cf_ldu_view &v)
         CF_CHECK_LAUNCH();
     }
     m->have_valT = m->have_32 = m->have_T32 = m->have_dmin = false;
+    ++m->gen;
 }
 
 Matrix *matrix_create(Context *ctx, const cf_ldu_view &v)
@@ -640,6 +641,7 @@ void matrix_update_values(Matrix *m, const double *diag, const double *lower, co
     }
     m->have_valT = m->have_32 = m->have_T32 = m->have_dmin = false;
     m->have_sval = m->have_svalT = m->have_sval32 = m->have_svalT32 = false;
+    ++m->gen;
 }
 
 // A^T values on A's pattern: the same fill with lower and upper swapped.
@@ -824,6 +826,7 @@ void matrix_set_transpose_csr(Matrix *m, const int32_t *roT, const int32_t *colT
     m->have_valT = true;
     m->have_T32 = false;
     m->have_svalT = m->have_svalT32 = false;
+    ++m->gen;
 }
 
 static void matrix_transpose_from_csr(Matrix *m)
@@ -847,6 +850,7 @@ static void matrix_transpose_from_csr(Matrix *m)
     m->have_valT = true;
     m->have_T32 = false;
     m->have_svalT = m->have_svalT32 = false;
+    ++m->gen;
 }
 
 // Decide the fast kernels' format (once per pattern) and bring the SELL-32
@@ -888,6 +892,7 @@ bool matrix_ensure_sell(Matrix *m, bool transpose, bool fp32)
             }
         }
         m->have_sval = m->have_svalT = m->have_sval32 = m->have_svalT32 = false;
+        ++m->gen;
     }
     if (m->sell != 1) return false;
     if (transpose) matrix_ensure_transpose(m);
@@ -933,6 +938,7 @@ void matrix_set_inverse_diagonal(Matrix *m, const double *dinv)
 {
     Context *ctx = m->ctx;
     CF_CUDA(cudaMemcpyAsync(m->dinv.ptr, dinv, sizeof(double) * m->n, cudaMemcpyDeviceToDevice, ctx->stream));
+    ++m->gen;
 }
 
 int stage_cap_for(const Matrix *m)

@@ -45,39 +45,6 @@ __global__ void __launch_bounds__(kBlock) k_mx_correct(const SolveArgs *__restri
     }
 }
 
-// FP32 values of L A R (L, R diagonal, L = null: the identity) on A's
-// pattern, over the SELL-32 slots (padding stays 0) ...
-__global__ void __launch_bounds__(kBlock) k_mx_scaled_sell(int n, int n_slices, const int32_t *__restrict__ soff,
-                                                           const int32_t *__restrict__ scol,
-                                                           const double *__restrict__ sval,
-                                                           const double *__restrict__ L,
-                                                           const double *__restrict__ R, float *__restrict__ out)
-{
-    CF_FOR_ELEMS(i, 32 * n_slices) {
-        const int sl = i >> 5, lane = i & 31;
-        const int b = soff[sl], len = (soff[sl + 1] - b) >> 5;
-        const double li = (L && i < n) ? L[i] : 1.0;
-        for (int t = 0; t < len; ++t) {
-            const int o = b + 32 * t + lane;
-            const double v = sval[o];
-            out[o] = v == 0.0 ? 0.f : (float)(li * v * R[scol[o]]);
-        }
-    }
-}
-
-// ... or over the CSR entries
-__global__ void __launch_bounds__(kBlock) k_mx_scaled_csr(int n, const int32_t *__restrict__ ro,
-                                                          const int32_t *__restrict__ col,
-                                                          const double *__restrict__ val,
-                                                          const double *__restrict__ L,
-                                                          const double *__restrict__ R, float *__restrict__ out)
-{
-    CF_FOR_ELEMS(i, n) {
-        const double li = L ? L[i] : 1.0;
-        for (int j = ro[i]; j < ro[i + 1]; ++j) out[j] = (float)(li * val[j] * R[col[j]]);
-    }
-}
-
 // r = b - A x, ||r|| (FP64); records the outer step.  SCALED (JMR, whose
 // residual is the symmetrically scaled one): r = D^-1/2 (b - A x).
 template <int FMT, bool SCALED>
@@ -444,18 +411,9 @@ static Kernels inner_kernels(int solver, bool sell)
     return sell ? inner_kernels_t<kSell>(solver) : inner_kernels_t<kCsr>(solver);
 }
 
-// The diagonally preconditioned MR solvers.  Their FP32 sweep is MR on a
-// scaled matrix: MRJacobi's and MRS's step y = A D^-1 r, x += w D^-1 r is
-// MR on A D^-1 with x = D^-1 x'; JMR's y = D^-1/2 A D^-1/2 r on the scaled
-// residual r = D^-1/2 (b - A x), x += w D^-1/2 r is MR on D^-1/2 A D^-1/2
-// with x = D^-1/2 x'.  The same iterates in exact arithmetic, two passes a
-// step and no preconditioned vector: the scaling is paid once per solve
-// (a matrix-sized pass) and once per sweep (in the correction of x).
-static bool mr_precond(int solver) { return solver == CF_MRJACOBI || solver == CF_MRS || solver == CF_JMR; }
-
 bool mixed_supported(int solver)
 {
-    return solver == CF_CG || solver == CF_BICG || solver == CF_MR || mr_precond(solver);
+    return solver == CF_CG || solver == CF_BICG || solver == CF_MR || mr_scaled_solver(solver);
 }
 
 void mixed_prepare(Context *ctx, Matrix *m, int solver, SolveArgs &A)
@@ -463,7 +421,7 @@ void mixed_prepare(Context *ctx, Matrix *m, int solver, SolveArgs &A)
     require(mixed_supported(solver), CF_UNSUPPORTED,
             "mixed precision is implemented for CG, BiCG, MR, MRJacobi, MRS and JMR");
     const bool tr = A.val != m->val.as<double>(); // transposed solve
-    const bool scaled = mr_precond(solver);
+    const bool scaled = mr_scaled_solver(solver);
     if (!scaled) {
         matrix_ensure_fp32(m, false);
         if (solver == CF_BICG || tr) matrix_ensure_fp32(m, true);
@@ -475,30 +433,11 @@ void mixed_prepare(Context *ctx, Matrix *m, int solver, SolveArgs &A)
     ctx->state_in.ensure(sizeof(DevState));
     A.corr_scale = nullptr;
     if (scaled) {
-        // FP32 L A R of the solved matrix (A^T for a transposed solve: A.val
-        // and A.s_val point at its values), refreshed every solve since the
-        // values change between solves
-        const double *L = solver == CF_JMR ? A.dinv_sqrt : nullptr;
-        const double *R = solver == CF_JMR ? A.dinv_sqrt : A.dinv;
-        const int n = m->n;
-        DeviceBuffer &buf = ctx->scaled32;
-        if (A.n_slices > 0) {
-            buf.ensure(sizeof(float) * ((size_t)m->sell_nnz + 32));
-            k_mx_scaled_sell<<<launch_cfg(ctx, (const void *)k_mx_scaled_sell, false, 0, false).grid, kBlock, 0,
-                               ctx->stream>>>(n, A.n_slices, A.s_off, A.s_col, A.s_val, L, R, buf.as<float>());
-            A.s_val32 = buf.as<float>();
-            A.val32 = nullptr;
-        } else {
-            buf.ensure(sizeof(float) * ((size_t)m->nnz + 4));
-            CF_CUDA(cudaMemsetAsync(buf.as<float>() + m->nnz, 0, sizeof(float) * 4, ctx->stream));
-            k_mx_scaled_csr<<<launch_cfg(ctx, (const void *)k_mx_scaled_csr, false, 0, false).grid, kBlock, 0,
-                              ctx->stream>>>(n, A.ro, A.col, A.val, L, R, buf.as<float>());
-            A.val32 = buf.as<float>();
-            A.s_val32 = nullptr;
-        }
-        CF_CUDA(cudaGetLastError());
+        // FP32 L A R of the solved matrix in the layout in use
+        const float *v = mr_scaled_values<float>(ctx, m, A, solver, tr, m->sc32, &A.corr_scale);
+        A.val32 = A.n_slices > 0 ? nullptr : v;
+        A.s_val32 = A.n_slices > 0 ? v : nullptr;
         A.valT32 = A.s_valT32 = nullptr;
-        A.corr_scale = R;
     } else {
         A.val32 = m->val32.as<float>();
         A.valT32 = m->have_T32 ? m->valT32.as<float>() : nullptr;

@@ -415,40 +415,23 @@ __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_rich_spmv(cons
 }
 
 // ---------------------------------------------------------------------------
-// MR family: prep d = M r (kinds 1-3); spmv y = A d (JMR: z = D^-1/2 y),
-// (r, y), (y, y) -> step; update as in solve_fp64.cu (k_mr_update).
+// MR family.  SCALED = false: MR; true: MRJacobi, MRS and JMR as MR on
+// L A R (a->sc_val, see mr_scaled_values), which needs no prep pass.
+//   spmv:   y = A r (or L A R r), (r, y), (y, y) -> step
+//   update: x += alpha d, r -= alpha y, ||r|| with d = r (MR) or d = R r
+//           (R = a->corr_scale: MRJacobi's D^-1 r, JMR's D^-1/2 r)
 // ---------------------------------------------------------------------------
-template <int KIND>
-__global__ void __launch_bounds__(kBlock) k_f_mr_prep(const SolveArgs *__restrict__ a)
-{
-    DevState *st = a->st;
-    CF_EXIT_IF_DONE(a, st, false);
-    const int n = a->n;
-    const double *__restrict__ r = a->r[0];
-    const double *__restrict__ dinv = a->dinv;
-    const double *__restrict__ sD = a->dinv_sqrt;
-    double *__restrict__ d = a->w[1];
-    CF_FOR_ELEMS(i, n) {
-        double v;
-        if (KIND == 1) v = __dmul_rn(dinv[i], r[i]);
-        else if (KIND == 2) v = __dadd_rn(__dmul_rn(dinv[i], r[i]), 0.0);
-        else v = __dmul_rn(sD[i], r[i]);
-        d[i] = v;
-    }
-}
-
-template <int KIND, int FMT>
+template <bool SCALED, int FMT>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_mr_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, false);
     const double *__restrict__ r = a->r[0];
-    const double *__restrict__ d = (KIND == 0) ? a->r[0] : a->w[1];
-    const double *__restrict__ sD = a->dinv_sqrt;
+    const double *val = SCALED ? a->sc_val : a->val;
+    const double *sval = SCALED ? a->sc_val : a->s_val;
     double *__restrict__ y = a->w[0];
     double acc[2] = {0.0, 0.0};
-    for_rows<FMT, double>(a, a->val, a->s_val, [&](int c) { return d[c]; }, [&](int row, double v) {
-        if (KIND == 3) v = __dmul_rn(sD[row], v);
+    for_rows<FMT, double>(a, val, sval, [&](int c) { return r[c]; }, [&](int row, double v) {
         y[row] = v;
         acc[0] = fma_t(r[row], v, acc[0]);
         acc[1] = fma_t(v, v, acc[1]);
@@ -528,9 +511,7 @@ __global__ void __launch_bounds__(kBlock) k_f_bicg_update(const SolveArgs *__res
     }
 }
 
-// MR family update: x += alpha d, r -= alpha y, ||r|| (d = r for MR, the
-// prep vector otherwise).
-template <int KIND>
+template <bool SCALED>
 __global__ void __launch_bounds__(kBlock) k_f_mr_update(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
@@ -540,7 +521,7 @@ __global__ void __launch_bounds__(kBlock) k_f_mr_update(const SolveArgs *__restr
     double *__restrict__ r = a->r[0];
     double *__restrict__ x = a->x;
     const double *__restrict__ y = a->w[0];
-    const double *__restrict__ d = (KIND == 0) ? a->r[0] : a->w[1];
+    const double *__restrict__ R = a->corr_scale;
     double part[4] = {0.0, 0.0, 0.0, 0.0};
     CF_X4_LOOP(i, n) {
         double rv[4], xv[4], yv[4], dv[4];
@@ -549,7 +530,7 @@ __global__ void __launch_bounds__(kBlock) k_f_mr_update(const SolveArgs *__restr
             rv[u] = r[CF_X4_IDX(i, u)];
             xv[u] = x[CF_X4_IDX(i, u)];
             yv[u] = y[CF_X4_IDX(i, u)];
-            dv[u] = (KIND == 0) ? rv[u] : d[CF_X4_IDX(i, u)];
+            dv[u] = SCALED ? __dmul_rn(R[CF_X4_IDX(i, u)], rv[u]) : rv[u];
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -561,7 +542,7 @@ __global__ void __launch_bounds__(kBlock) k_f_mr_update(const SolveArgs *__restr
     }
     CF_X4_TAIL(i, n) {
         const double ri0 = r[i];
-        const double di = (KIND == 0) ? ri0 : d[i];
+        const double di = SCALED ? __dmul_rn(R[i], ri0) : ri0;
         x[i] = fma_t(alpha, di, x[i]);
         const double ri = fma_t(-alpha, y[i], ri0);
         r[i] = ri;
@@ -604,23 +585,14 @@ static Kernels fast_kernels(int solver)
         k.k1 = (const void *)k_f_rich_spmv<FMT>;
         break;
     case CF_MR:
-        k.k1 = (const void *)k_f_mr_spmv<0, FMT>;
-        k.k2 = (const void *)k_f_mr_update<0>;
+        k.k1 = (const void *)k_f_mr_spmv<false, FMT>;
+        k.k2 = (const void *)k_f_mr_update<false>;
         break;
     case CF_MRJACOBI:
-        k.k0 = (const void *)k_f_mr_prep<1>;
-        k.k1 = (const void *)k_f_mr_spmv<1, FMT>;
-        k.k2 = (const void *)k_f_mr_update<1>;
-        break;
     case CF_MRS:
-        k.k0 = (const void *)k_f_mr_prep<2>;
-        k.k1 = (const void *)k_f_mr_spmv<2, FMT>;
-        k.k2 = (const void *)k_f_mr_update<2>;
-        break;
-    case CF_JMR:
-        k.k0 = (const void *)k_f_mr_prep<3>;
-        k.k1 = (const void *)k_f_mr_spmv<3, FMT>;
-        k.k2 = (const void *)k_f_mr_update<3>;
+    case CF_JMR: // MR on L A R (mr_scaled_values), set up by the caller
+        k.k1 = (const void *)k_f_mr_spmv<true, FMT>;
+        k.k2 = (const void *)k_f_mr_update<true>;
         break;
     default: break;
     }

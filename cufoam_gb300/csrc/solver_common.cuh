@@ -368,4 +368,84 @@ static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int p
 Kernels fast_body_kernels(int solver, bool sell);
 const void *fast_flush_kernel();
 
+// ---------------------------------------------------------------------------
+// The diagonally preconditioned MR solvers as MR on a scaled matrix.
+// MRJacobi's and MRS's step (y = A D^-1 r, alpha = (r, y)/(y, y),
+// x += alpha D^-1 r, r -= alpha y) is MR on A D^-1; JMR's (y = D^-1/2 A
+// D^-1/2 r on the scaled residual r = D^-1/2 (b - A x), x += alpha D^-1/2
+// r) is MR on D^-1/2 A D^-1/2.  The scaled values take the place of the
+// preconditioned vector: a step is MR's two passes, with R r formed in the
+// x update.
+// ---------------------------------------------------------------------------
+// values of L A R (L, R diagonal, L = null: the identity) on A's pattern,
+// over the SELL-32 slots (padding stays 0) ...
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_scaled_sell(int n, int n_slices, const int32_t *__restrict__ soff,
+                                                        const int32_t *__restrict__ scol,
+                                                        const double *__restrict__ sval,
+                                                        const double *__restrict__ L,
+                                                        const double *__restrict__ R, T *__restrict__ out)
+{
+    CF_FOR_ELEMS(i, 32 * n_slices) {
+        const int sl = i >> 5, lane = i & 31;
+        const int b = soff[sl], len = (soff[sl + 1] - b) >> 5;
+        const double li = (L && i < n) ? L[i] : 1.0;
+        for (int t = 0; t < len; ++t) {
+            const int o = b + 32 * t + lane;
+            const double v = sval[o];
+            out[o] = v == 0.0 ? T(0) : (T)(li * v * R[scol[o]]);
+        }
+    }
+}
+
+// ... or over the CSR entries
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_scaled_csr(int n, const int32_t *__restrict__ ro,
+                                                       const int32_t *__restrict__ col,
+                                                       const double *__restrict__ val,
+                                                       const double *__restrict__ L,
+                                                       const double *__restrict__ R, T *__restrict__ out)
+{
+    CF_FOR_ELEMS(i, n) {
+        const double li = L ? L[i] : 1.0;
+        for (int j = ro[i]; j < ro[i + 1]; ++j) out[j] = (T)(li * val[j] * R[col[j]]);
+    }
+}
+
+inline bool mr_scaled_solver(int solver) { return solver == CF_MRJACOBI || solver == CF_MRS || solver == CF_JMR; }
+
+// L A R of the solved matrix for an MR-family solve in the layout in use
+// (A.val / A.s_val point at A^T's values for a transposed solve); R is
+// returned in *R_out.  Kept on the matrix until its values change.
+template <class T>
+static const T *mr_scaled_values(Context *ctx, Matrix *m, const SolveArgs &A, int solver, bool transpose,
+                                 ScaledCopy &sc, const double **R_out)
+{
+    const double *L = solver == CF_JMR ? A.dinv_sqrt : nullptr;
+    const double *R = solver == CF_JMR ? A.dinv_sqrt : A.dinv;
+    *R_out = R;
+    const int scale = solver == CF_JMR ? 2 : 1;
+    const int sell = A.n_slices > 0 ? 1 : 0;
+    const int tr = transpose ? 1 : 0;
+    if (sc.gen == m->gen && sc.scale == scale && sc.transpose == tr && sc.sell == sell) return sc.buf.as<T>();
+    sc.gen = 0;
+    const Launch l = launch_cfg(ctx, sell ? (const void *)k_scaled_sell<T> : (const void *)k_scaled_csr<T>,
+                                false, 0, false);
+    if (sell) {
+        sc.buf.ensure(sizeof(T) * ((size_t)m->sell_nnz + 32));
+        k_scaled_sell<T><<<l.grid, kBlock, 0, ctx->stream>>>(m->n, A.n_slices, A.s_off, A.s_col, A.s_val, L, R,
+                                                             sc.buf.as<T>());
+    } else {
+        sc.buf.ensure(sizeof(T) * ((size_t)m->nnz + 4));
+        CF_CUDA(cudaMemsetAsync(sc.buf.as<T>() + m->nnz, 0, sizeof(T) * 4, ctx->stream));
+        k_scaled_csr<T><<<l.grid, kBlock, 0, ctx->stream>>>(m->n, A.ro, A.col, A.val, L, R, sc.buf.as<T>());
+    }
+    CF_CUDA(cudaGetLastError());
+    sc.gen = m->gen;
+    sc.scale = scale;
+    sc.transpose = tr;
+    sc.sell = sell;
+    return sc.buf.as<T>();
+}
+
 } // namespace cf
