@@ -117,7 +117,7 @@ struct SolveArgs {
     // vectors (FP32, mixed precision inner solve)
     float *fx, *fr, *fp[2], *fq, *frs, *fps[2], *fqs;
     const double *corr_scale;  // MR family on L A R: x += s * corr_scale * d (1 / a_ii or sqrt(1 / a_ii))
-    const double *sc_val;      // FP64 fast-order MR family: values of L A R (the format in use)
+    const double *sc_val;      // FP64 fast order (MR family, Jacobi): values of L A R (the format in use)
     // reductions / state
     double *partials;          // [kMaxNV][partial_stride]
     float *partials32;

@@ -434,7 +434,7 @@ void mixed_prepare(Context *ctx, Matrix *m, int solver, SolveArgs &A)
     A.corr_scale = nullptr;
     if (scaled) {
         // FP32 L A R of the solved matrix in the layout in use
-        const float *v = mr_scaled_values<float>(ctx, m, A, solver, tr, m->sc32, &A.corr_scale);
+        const float *v = scaled_values<float>(ctx, m, A, solver, tr, m->sc32, &A.corr_scale);
         A.val32 = A.n_slices > 0 ? nullptr : v;
         A.s_val32 = A.n_slices > 0 ? v : nullptr;
         A.valT32 = A.s_valT32 = nullptr;

@@ -317,51 +317,28 @@ __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS - 1) k_f_bicg_spmv(
 }
 
 // ---------------------------------------------------------------------------
-// Jacobi (SolverSingleGPU.h:924-994):
-//   prep: d = D^-1 r, x += d     spmv: r -= A d, ||r||
+// Jacobi (SolverSingleGPU.h:924-994): x += D^-1 r, r -= A D^-1 r, ||r||.
+// One pass per step over the scaled matrix A D^-1 (a->sc_val, cached on the
+// matrix): the residual alternates between r[0] and r[1] (step k reads
+// r[(k + 1) & 1], writes r[k & 1]), so every row gathers the old residual
+// while its own row writes the new one; x += D^-1 r is row-local.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_f_jac_prep(const SolveArgs *__restrict__ a)
-{
-    DevState *st = a->st;
-    CF_EXIT_IF_DONE(a, st, false);
-    const int n = a->n;
-    const double *__restrict__ r = a->r[0];
-    const double *__restrict__ dinv = a->dinv;
-    double *__restrict__ d = a->w[1];
-    double *__restrict__ x = a->x;
-    CF_X4_LOOP(i, n) {
-        double dv[4], rv[4], xv[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            dv[u] = dinv[CF_X4_IDX(i, u)];
-            rv[u] = r[CF_X4_IDX(i, u)];
-            xv[u] = x[CF_X4_IDX(i, u)];
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const double di = __dmul_rn(dv[u], rv[u]);
-            d[CF_X4_IDX(i, u)] = di;
-            x[CF_X4_IDX(i, u)] = fma_t(1.0, di, xv[u]);
-        }
-    }
-    CF_X4_TAIL(i, n) {
-        const double di = __dmul_rn(dinv[i], r[i]);
-        d[i] = di;
-        x[i] = fma_t(1.0, di, x[i]);
-    }
-}
-
 template <int FMT>
-__global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_jac_spmv(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_jac_step(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, true);
-    const double *__restrict__ d = a->w[1];
-    double *__restrict__ r = a->r[0];
+    const int k = ld_cg(&st->k) + 1;
+    const double *__restrict__ rin = a->r[(k + 1) & 1];
+    double *__restrict__ rout = a->r[k & 1];
+    const double *__restrict__ dinv = a->dinv;
+    double *__restrict__ x = a->x;
     double acc[1] = {0.0};
-    for_rows<FMT, double>(a, a->val, a->s_val, [&](int c) { return d[c]; }, [&](int row, double y) {
-        const double ri = fma_t(-1.0, y, r[row]);
-        r[row] = ri;
+    for_rows<FMT, double>(a, a->sc_val, a->sc_val, [&](int c) { return rin[c]; }, [&](int row, double y) {
+        const double r0 = rin[row];
+        x[row] = fma_t(1.0, __dmul_rn(dinv[row], r0), x[row]);
+        const double ri = fma_t(-1.0, y, r0);
+        rout[row] = ri;
         acc[0] = fma_t(ri, ri, acc[0]);
     });
     double tot[1];
@@ -416,7 +393,7 @@ __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_rich_spmv(cons
 
 // ---------------------------------------------------------------------------
 // MR family.  SCALED = false: MR; true: MRJacobi, MRS and JMR as MR on
-// L A R (a->sc_val, see mr_scaled_values), which needs no prep pass.
+// L A R (a->sc_val, see scaled_values), which needs no prep pass.
 //   spmv:   y = A r (or L A R r), (r, y), (y, y) -> step
 //   update: x += alpha d, r -= alpha y, ||r|| with d = r (MR) or d = R r
 //           (R = a->corr_scale: MRJacobi's D^-1 r, JMR's D^-1/2 r)
@@ -571,9 +548,8 @@ static Kernels fast_kernels(int solver)
         k.k1 = (const void *)k_f_bicg_spmv<FMT>;
         k.k2 = (const void *)k_f_bicg_update;
         break;
-    case CF_JACOBI:
-        k.k0 = (const void *)k_f_jac_prep;
-        k.k1 = (const void *)k_f_jac_spmv<FMT>;
+    case CF_JACOBI: // on A D^-1 (scaled_values), set up by the caller
+        k.k1 = (const void *)k_f_jac_step<FMT>;
         break;
     case CF_PCG:
         k.k0 = (const void *)k_f_pcg_prep;
@@ -590,7 +566,7 @@ static Kernels fast_kernels(int solver)
         break;
     case CF_MRJACOBI:
     case CF_MRS:
-    case CF_JMR: // MR on L A R (mr_scaled_values), set up by the caller
+    case CF_JMR: // MR on L A R (scaled_values), set up by the caller
         k.k1 = (const void *)k_f_mr_spmv<true, FMT>;
         k.k2 = (const void *)k_f_mr_update<true>;
         break;

@@ -716,9 +716,10 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     A.abort_flag = (c.time_limit_s > 0) ? ctx->d_abort : nullptr;
 
     if (mixed) mixed_prepare(ctx, m, solver, A);
-    // fast order: MRJacobi, MRS and JMR run as MR on the scaled matrix
-    if (!ref && !mixed && mr_scaled_solver(solver))
-        A.sc_val = mr_scaled_values<double>(ctx, m, A, solver, tr, m->sc64, &A.corr_scale);
+    // fast order: MRJacobi, MRS and JMR run as MR on the scaled matrix,
+    // Jacobi as one pass over A D^-1
+    if (!ref && !mixed && (mr_scaled_solver(solver) || solver == CF_JACOBI))
+        A.sc_val = scaled_values<double>(ctx, m, A, solver, tr, m->sc64, &A.corr_scale);
 
     DevState &S = *ctx->h_state;
     S = DevState{};

@@ -414,12 +414,13 @@ __global__ void __launch_bounds__(kBlock) k_scaled_csr(int n, const int32_t *__r
 
 inline bool mr_scaled_solver(int solver) { return solver == CF_MRJACOBI || solver == CF_MRS || solver == CF_JMR; }
 
-// L A R of the solved matrix for an MR-family solve in the layout in use
-// (A.val / A.s_val point at A^T's values for a transposed solve); R is
+// L A R of the solved matrix in the layout in use (A.val / A.s_val point at
+// A^T's values for a transposed solve): D^-1/2 A D^-1/2 for JMR, A D^-1 for
+// the others (MRJacobi, MRS; the FP64 fast-order Jacobi step too); R is
 // returned in *R_out.  Kept on the matrix until its values change.
 template <class T>
-static const T *mr_scaled_values(Context *ctx, Matrix *m, const SolveArgs &A, int solver, bool transpose,
-                                 ScaledCopy &sc, const double **R_out)
+static const T *scaled_values(Context *ctx, Matrix *m, const SolveArgs &A, int solver, bool transpose,
+                              ScaledCopy &sc, const double **R_out)
 {
     const double *L = solver == CF_JMR ? A.dinv_sqrt : nullptr;
     const double *R = solver == CF_JMR ? A.dinv_sqrt : A.dinv;
