@@ -690,7 +690,8 @@ def run_profile_batch(args):
 def run_profile_all(args):
     """A short run for an ncu launch list of every kernel family: on 128^3
     systems, 20 host-driven steps of each solver in both summation orders
-    (and in mixed precision where it exists), the plain SpMVs, normFactor,
+    (and in mixed precision for CG, MR, MRJacobi, JMR and BiCG), the plain
+    SpMVs, normFactor,
     the device ldu2csr, one adjoint gradient pass and a small batched solve
     (64 systems x 3 right-hand sides, FP64 and mixed)."""
     import torch
@@ -715,7 +716,7 @@ def run_profile_all(args):
             psi = torch.zeros(sym.n, dtype=torch.float64, device=dev)
             cf._TABLE[name]("p", M, {"tolerance": 1e-30, "maxIter": steps, "useGraph": 0,
                                      "reduction": red}).solve(psi, b)
-        if name in ("cuFoamCG", "cuFoamMR", "cuFoamBiCG"):
+        if name in ("cuFoamCG", "cuFoamMR", "cuFoamMRJacobi", "cuFoamJMR", "cuFoamBiCG"):
             psi = torch.zeros(sym.n, dtype=torch.float64, device=dev)
             cf._TABLE[name]("p", M, {"tolerance": 1e-30, "maxIter": steps, "useGraph": 0,
                                      "precision": "mixed", "innerMaxIter": steps,
