@@ -232,6 +232,39 @@ def test_mrs_equals_mrjacobi_in_exact_arithmetic():
     assert np.array_equal(a.history, c.history)
 
 
+def _scaled_csr(A, left, right):
+    rows = np.repeat(np.arange(A.n), np.diff(A.row_offsets))
+    return O.CSR(A.row_offsets.copy(), A.cols.copy(), left[rows] * A.vals * right[A.cols])
+
+
+def test_mr_on_the_scaled_matrix_is_mrjacobi_and_jmr():
+    # The GPU runs MRJacobi (and MRS) as MR on A D^-1 and JMR as MR on
+    # D^-1/2 A D^-1/2: the same iterates as the reference's preconditioned
+    # loops up to rounding (x = D^-1 x' and x = D^-1/2 x').
+    L, _ = O.grid_convdiff(9, 8, 7, 3, 4.0)
+    A = O.ldu2csr(L)
+    b = O.uniform(6, L.n)
+    d = np.asarray(L.diag, np.float64)
+    one, dinv, sd = np.ones(L.n), 1.0 / d, np.sqrt(1.0 / d)
+    steps = 40
+    want = O.solve(O.MRJACOBI, A, b, np.zeros(L.n), 1e-300, steps)
+    got = O.solve(O.MR, _scaled_csr(A, one, dinv), b, np.zeros(L.n), 1e-300, steps)
+    assert np.allclose(got.history, want.history, rtol=1e-12, atol=0)
+    assert np.allclose(dinv * got.x, want.x, rtol=1e-11, atol=1e-14)
+    want = O.solve(O.JMR, A, b, np.zeros(L.n), 1e-300, steps)
+    got = O.solve(O.MR, _scaled_csr(A, sd, sd), sd * b, np.zeros(L.n), 1e-300, steps)
+    assert np.allclose(got.history, want.history, rtol=1e-12, atol=0)
+    assert np.allclose(sd * got.x, want.x, rtol=1e-11, atol=1e-14)
+    # and Jacobi's step x += D^-1 r, r -= A D^-1 r is one product with A D^-1
+    want = O.solve(O.JACOBI, A, b, np.zeros(L.n), 1e-300, steps)
+    AD = _scaled_csr(A, one, dinv).dense()
+    x, r = np.zeros(L.n), b.copy()
+    for _ in range(steps):
+        x, r = x + dinv * r, r - AD @ r
+    assert np.allclose(x, want.x, rtol=1e-11, atol=1e-14)
+    assert np.isclose(np.linalg.norm(r), want.history[-1], rtol=1e-10)
+
+
 def test_max_iter_cap_and_loop_semantics():
     L = O.grid_const(16, 16, 1)
     b = O.uniform(1, L.n)
