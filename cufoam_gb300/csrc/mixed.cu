@@ -23,6 +23,13 @@
 #ifndef CF_MX_MIN_BLOCKS
 #define CF_MX_MIN_BLOCKS 5
 #endif
+// SELL entries per thread and batch in the two BiCGStab SpMV passes: with
+// 8 the 256^3 convection-diffusion BiCGStab step took 735 us against 989 us
+// with the default 4 and 1,039 us with 2 (MR's SpMV: 273, 269 and 412 us,
+// so the others keep 4).
+#ifndef CF_BCS_SELL_BATCH
+#define CF_BCS_SELL_BATCH 8
+#endif
 
 namespace cf {
 
@@ -223,7 +230,7 @@ __global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_bcs_spmv1(const
     const float *__restrict__ rh = a->frs;
     float *__restrict__ v = a->fq;
     float acc[1] = {0.f};
-    for_rows<FMT, float>(a, a->val32, a->s_val32, [&](int c) { return p[c]; }, [&](int row, float y) {
+    for_rows<FMT, float, CF_BCS_SELL_BATCH>(a, a->val32, a->s_val32, [&](int c) { return p[c]; }, [&](int row, float y) {
         v[row] = y;
         acc[0] = fma_t(rh[row], y, acc[0]);
     });
@@ -252,7 +259,7 @@ __global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_bcs_spmv2(const
     float *__restrict__ t = a->fqs;
     auto g = [&](int c) { return fma_t(-alpha, v[c], r[c]); };
     float acc[2] = {0.f, 0.f};
-    for_rows<FMT, float>(a, a->val32, a->s_val32, g, [&](int row, float y) {
+    for_rows<FMT, float, CF_BCS_SELL_BATCH>(a, a->val32, a->s_val32, g, [&](int row, float y) {
         const float si = g(row);
         sv[row] = si;
         t[row] = y;

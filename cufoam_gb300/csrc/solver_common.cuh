@@ -43,11 +43,14 @@ constexpr int kSellBatch = CF_SELL_BATCH;
 #endif
 constexpr int kSellBatch32 = CF_SELL_BATCH32;
 
-template <int FMT, class V, class G, class F>
+// (BATCH > 0 overrides the SELL batch of the value type for one kernel; the
+// sums do not depend on it: every row is one FMA chain in entry order)
+template <int FMT, class V, int BATCH = 0, class G, class F>
 __device__ __forceinline__ void for_rows(const SolveArgs *a, const V *val, const V *sval, G g, F f)
 {
     if constexpr (FMT == kSell) {
-        sell_rows<V, sizeof(V) == 4 ? kSellBatch32 : kSellBatch>(a->n, a->n_slices, a->s_off, a->s_col, sval, g, f);
+        constexpr int B = BATCH > 0 ? BATCH : (sizeof(V) == 4 ? kSellBatch32 : kSellBatch);
+        sell_rows<V, B>(a->n, a->n_slices, a->s_off, a->s_col, sval, g, f);
     } else {
         const int n = a->n, cap = a->stage_cap;
         CF_STAGE(V, cap);
