@@ -687,6 +687,31 @@ def run_profile_batch(args):
     return 0
 
 
+def run_profile_scaled(args):
+    """A short host-driven run on the 128^3 lognormal Poisson system for an
+    ncu capture of the scaled-matrix kernels: 6 FP64 Jacobi steps (one pass
+    over A D^-1 each) and 6 FP32 MRJacobi steps (MR on A D^-1) of one
+    mixed-precision sweep."""
+    import torch
+
+    import cufoam_gb300 as cf
+    from cufoam_gb300 import workloads as W
+    torch.cuda.set_device(0)
+    ctx = cf.Context(0)
+    ctx.set_stream(torch.cuda.current_stream(0))
+    L = W.grid_lognormal(128, 128, 128, 2)
+    b = torch.from_numpy(W.uniform(3, L.n)).cuda()
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    for solver, prec in (("cuFoamJacobi", "FP64"), ("cuFoamMRJacobi", "mixed")):
+        psi = torch.zeros(L.n, dtype=torch.float64, device="cuda")
+        perf = cf._TABLE[solver]("p", M, {"tolerance": 1e-30, "maxIter": 6, "useGraph": 0,
+                                          "precision": prec, "innerMaxIter": 6,
+                                          "maxRefinements": 1}).solve(psi, b)
+        torch.cuda.synchronize()
+        print(solver, prec, perf.n_iterations, perf.status_name, flush=True)
+    return 0
+
+
 def run_profile_all(args):
     """A short run for an ncu launch list of every kernel family: on 128^3
     systems, 20 host-driven steps of each solver in both summation orders
@@ -763,7 +788,11 @@ def main():
                     help="short run launching every kernel family once, for an ncu launch list")
     ap.add_argument("--profile-mr", action="store_true",
                     help="short host-driven MR run (FP64 and mixed, 256^3) for an ncu capture")
+    ap.add_argument("--profile-scaled", action="store_true",
+                    help="6 Jacobi (FP64) and 6 mixed MRJacobi steps at 128^3, for an ncu capture")
     args = ap.parse_args()
+    if args.profile_scaled:
+        return run_profile_scaled(args)
     if args.profile_mr:
         return run_profile_mr(args)
     if args.profile_all:
