@@ -41,8 +41,7 @@ __global__ void __launch_bounds__(kBlock) k_nf_dist(const SolveArgs *__restrict_
 {
     const int n = a->n, cap = a->stage_cap;
     CF_STAGE(double, cap);
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val, *x = a->x, *b = a->b;
+    const double *x = a->x, *b = a->b;
     const double xbar = ld_cg(&a->st->xbar);
     double acc[2] = {0.0, 0.0};
     CF_FOR_CHUNKS(base, n) {
@@ -81,8 +80,7 @@ __global__ void __launch_bounds__(kBlock) k_res_init(const SolveArgs *__restrict
 {
     const int n = a->n, cap = a->stage_cap;
     CF_STAGE(double, cap);
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val, *x = a->x, *b = a->b, *sD = a->dinv_sqrt, *dinv = a->dinv;
+    const double *x = a->x, *b = a->b, *sD = a->dinv_sqrt, *dinv = a->dinv;
     double *r = a->r[0], *rs = a->rs;
     double acc[2] = {0.0, 0.0};
     CF_FOR_CHUNKS(base, n) {
@@ -128,8 +126,6 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(const SolveArgs *__restrict_
     double *pout = a->p[k & 1];
     const double *r = a->r[0];
     double *x = a->x, *q = a->q;
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val;
     auto g = [&](int c) { return first ? r[c] : fma_t(beta, pin[c], r[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
@@ -217,8 +213,6 @@ __global__ void __launch_bounds__(kBlock) k_bicg_spmv(const SolveArgs *__restric
     double *pout = a->p[k & 1], *psout = a->ps[k & 1];
     const double *r = a->r[0], *rs = a->rs;
     double *x = a->x, *q = a->q, *qs = a->qs;
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val, *valT = a->valT;
     auto gp = [&](int c) { return first ? r[c] : fma_t(theta, pin[c], r[c]); };
     auto gps = [&](int c) { return first ? rs[c] : fma_t(theta, psin[c], rs[c]); };
     double acc[1] = {0.0};
@@ -312,8 +306,6 @@ __global__ void __launch_bounds__(kBlock) k_pow_step(const SolveArgs *__restrict
     const double sc = ld_cg(&st->pow_inv);
     const double *yprev = a->w[(s + 1) & 1];
     double *y = a->w[s & 1];
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val;
     auto g = [&](int c) { return s == 0 ? inv_n : __dmul_rn(sc, yprev[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
@@ -340,8 +332,6 @@ __global__ void __launch_bounds__(kBlock) k_pow_final(const SolveArgs *__restric
     const double inv_n = 1.0 / n;
     const double sc = ld_cg(&st->pow_inv);
     const double *ylast = a->w[(steps + 1) & 1];
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val;
     auto g = [&](int c) { return steps == 0 ? inv_n : __dmul_rn(sc, ylast[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
@@ -372,8 +362,6 @@ __global__ void __launch_bounds__(kBlock) k_rich_step(const SolveArgs *__restric
     const double *rold = a->r[(k + 1) & 1];
     double *rnew = a->r[k & 1];
     const double *b = a->b;
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val;
     auto g = [&](int c) { return fma_t(omega, rold[c], xold[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
@@ -419,8 +407,6 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_step(const SolveArgs *__restr
     double *rnew = a->r[k & 1];
     const double *dinv = a->dinv;
     double *x = a->x;
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val;
     auto g = [&](int c) { return __dmul_rn(dinv[c], rold[c]); };
     double acc[1] = {0.0};
     CF_FOR_CHUNKS(base, n) {
@@ -468,8 +454,6 @@ __global__ void __launch_bounds__(kBlock) k_mr_spmv(const SolveArgs *__restrict_
     CF_STAGE(double, cap);
     const double *r = a->r[0], *dinv = a->dinv, *sD = a->dinv_sqrt;
     double *y = a->w[0];
-    const int32_t *ro = a->ro, *col = a->col;
-    const double *val = a->val;
     auto g = [&](int c) { return mr_apply<KIND>(dinv, sD, r, c); };
     double acc[2] = {0.0, 0.0};
     CF_FOR_CHUNKS(base, n) {
