@@ -566,9 +566,17 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
             status = CF_OK;
             break;
         }
+        if (SI.status == CF_BREAKDOWN && SI.k == 0) {
+            // the inner solver broke down before its first step: x is
+            // unchanged, so a retry would repeat the same breakdown
+            status = CF_BREAKDOWN;
+            break;
+        }
         if (!(nrm < prev_norm)) {
             // The FP32 sweep raised the FP64 residual (a non-finite inner
-            // solve included): undo it and retry with a shorter sweep.
+            // solve included): undo it and retry with a sweep half as long
+            // as the one just undone (the sweep is deterministic, so a
+            // retry of the same length would repeat it).
             CF_CUDA(cudaMemcpyAsync(A.x, x_keep, vb, cudaMemcpyDeviceToDevice, ctx->stream));
             CF_CUDA(cudaMemcpyAsync(A.r[0], r_keep, vb, cudaMemcpyDeviceToDevice, ctx->stream));
             DevState &S = *ctx->h_state;
@@ -577,7 +585,7 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
             S.status = CF_NOT_CONVERGED;
             CF_CUDA(cudaMemcpyAsync(A.st, &S, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
             CF_CUDA(cudaStreamSynchronize(ctx->stream));
-            inner_cap /= 2;
+            inner_cap = SI.k / 2;
             if (inner_cap < 8) {
                 status = CF_NOT_CONVERGED;
                 break;
@@ -586,10 +594,6 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
         }
         if (ctx->h_state->done) {
             status = ctx->h_state->status;
-            break;
-        }
-        if (SI.status == CF_BREAKDOWN && SI.k == 0) {
-            status = CF_BREAKDOWN;
             break;
         }
         prev_norm = nrm;

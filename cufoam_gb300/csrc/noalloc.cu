@@ -125,11 +125,19 @@ static cf_status norm_factor_noalloc(int32_t n, const int32_t *ro, const int32_t
     // cannot hold that many block partials
     int grid = ref ? tpsm / kBlock * sms : std::min(sms * 4, kNoAllocMaxBlocks);
     if (grid < 1 || grid > kNoAllocMaxBlocks) return CF_UNSUPPORTED;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    // the scratch address is the current device's: a stream of another
+    // device would run the kernels there against this device's address
+    int stream_device = -1;
+    if (cudaStreamGetDevice(cs, &stream_device) != cudaSuccess) {
+        cudaGetLastError();
+        return CF_BAD_INPUT;
+    }
+    if (stream_device != device) return CF_BAD_INPUT;
     void *p = nullptr;
     cf_status st = noalloc_scratch(device, &p);
     if (st != CF_OK) return st;
     NoAllocScratch *s = static_cast<NoAllocScratch *>(p);
-    cudaStream_t cs = static_cast<cudaStream_t>(stream);
     // the array keeps the last call's contents: restart the arrival counters
     if (cudaMemsetAsync(s->counters, 0, sizeof(s->counters), cs) != cudaSuccess) {
         cudaGetLastError();

@@ -134,8 +134,11 @@ typedef struct cf_controls {
     int32_t mixed_inner_max; /* mixed: FP32 steps per refinement sweep; 0 = no
                                 limit (to the inner tolerance).  A sweep that
                                 raises the FP64 residual is undone and retried
-                                with half as many steps.  Mixed BiCG's FP32
-                                inner solver is BiCGStab. */
+                                with half as many steps as it took (the solve
+                                stops as not converged below 8); an inner
+                                breakdown before the first step ends it with
+                                CF_BREAKDOWN.  Mixed BiCG's FP32 inner solver
+                                is BiCGStab. */
     int32_t reserved[3];
 } cf_controls;
 
@@ -269,8 +272,10 @@ cf_status cf_adjoint_gradients(cf_matrix *m, const double *lambda, const double 
  * start-up, or a latency-critical loop where a cudaMalloc/cudaFree (which
  * can synchronise the whole device) is not acceptable.  It allocates nothing.
  *
- * All pointers are device pointers; the result is written to *norm_factor
- * (device memory) by work enqueued on `cuda_stream`; the call does not wait
+ * All pointers are device pointers on the current device (cudaSetDevice);
+ * the result is written to *norm_factor (device memory) by work enqueued on
+ * `cuda_stream`, which must belong to the current device (CF_BAD_INPUT
+ * otherwise; NULL is the legacy default stream); the call does not wait
  * for it.  The matrix arrays are read only inside [0, nnz).
  * Scratch: one fixed array of about 33 KB inside the library, which every
  * GPU that loads the library keeps until the process exits.  All calls

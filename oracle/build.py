@@ -30,7 +30,17 @@ REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "liboracle.so")
 REF_LDU2CSR_SO = os.path.join(REF_DIR, "libref_ldu2csr.so")
 REF_FORMATS_SO = os.path.join(REF_DIR, "libref_formats.so")
-REFERENCE_ROOT = os.environ.get("CUFOAM_REFERENCE_ROOT", "/root/reference")
+# Where this recipe reads the reference's sources: CUFOAM_REFERENCE_ROOT, or
+# the read-only mount of the build machine.  Only the recipe names that
+# mount; tests and tools ask reference_root(), which is None where neither
+# exists (the GPU machine, which uses the outputs built here).
+_DEFAULT_REFERENCE_MOUNT = "/root/reference"
+REFERENCE_ROOT = os.environ.get("CUFOAM_REFERENCE_ROOT") or _DEFAULT_REFERENCE_MOUNT
+
+
+def reference_root() -> str | None:
+    """The reference source tree this recipe builds from, or None."""
+    return REFERENCE_ROOT if os.path.isdir(REFERENCE_ROOT) else None
 
 
 def _stale(target: str, sources: list[str]) -> bool:

@@ -11,8 +11,11 @@ import pytest
 
 from cufoam_gb300 import build as B
 from cufoam_gb300.compat import GisHarness
+from oracle.build import reference_root
 
-REF_GIS = "/root/reference/gis"
+# the reference's gis/ directory, where its sources are mounted (the oracle
+# build recipe's location); the test skips elsewhere
+REF_GIS = os.path.join(reference_root() or "", "gis")
 
 EXPORTS = ["Transpose", "CG", "BiCG", "Richardson", "MR", "Jacobi", "MRJacobi", "JMR", "MRS",
            "NormFactor"]
@@ -36,7 +39,7 @@ def test_libgis_exports(built):
         assert out.count(" BiCG(SingleGPU::") == 2
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(REF_GIS, "gis.h")),
+@pytest.mark.skipif(not reference_root() or not os.path.exists(os.path.join(REF_GIS, "gis.h")),
                     reason="reference sources not present")
 def test_reference_header_links_to_libgis(built, tmp_path):
     out = tmp_path / "ref_harness.so"

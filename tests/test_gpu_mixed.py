@@ -88,3 +88,37 @@ def test_mixed_mr_family_formats_and_transpose(ctx, fmt, name, transpose):
     assert _true_rel(Ls, b, psi, perf.norm_factor, scaled=name == "JMR") <= tol
     want = O.plugin_solve(O.SOLVER_NAMES[name], Ls, b, np.zeros(L.n), tol, 200000)
     assert np.linalg.norm(psi - want.psi) / np.linalg.norm(want.psi) < 1e-6
+
+
+def test_mixed_rollback_shortens_the_retry(ctx):
+    """A refinement sweep that raises the FP64 residual is undone and retried
+    with half as many FP32 steps as the sweep just undone, so a mixed solve
+    that cannot make progress stops after a few short retries instead of
+    repeating the same deterministic sweep.  Here the FP32 copy of the
+    matrix overflows (a diagonal of 1e39 is inf in FP32): the first sweep
+    ends non-finite after one step and its retry would have zero steps."""
+    L = O.grid_const(16, 16, 1)
+    L = O.LDU(L.n, np.full(L.n, 1e39), L.lower, L.upper, L.lower_addr, L.upper_addr)
+    b = O.uniform(3, L.n)
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    psi = np.zeros(L.n)
+    perf = cf.cuFoamMR("p", M, {"tolerance": 1e-10, "maxIter": 10000,
+                                "precision": "mixed"}).solve(psi, b)
+    assert perf.status == 1, perf.status_name          # not converged
+    assert perf.n_outer == 1 and perf.n_iterations == 1
+    assert np.all(psi == 0.0)                           # the sweep was undone
+
+
+def test_mixed_bicg_inner_breakdown_is_reported(ctx):
+    """The FP32 inner solver of mixed BiCG breaks down before its first step
+    when (r^, A r^) = 0, as for a skew-symmetric matrix: the solve stops
+    with CF_BREAKDOWN (a retry would repeat the same breakdown)."""
+    L = O.LDU(2, np.zeros(2), np.array([-1.0]), np.array([1.0]),
+              np.array([0], np.int32), np.array([1], np.int32))
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    psi = np.zeros(2)
+    perf = cf.cuFoamBiCG("p", M, {"tolerance": 1e-12, "maxIter": 100,
+                                  "precision": "mixed"}).solve(psi, np.array([1.0, 2.0]))
+    assert perf.status == 2, perf.status_name
+    assert perf.n_iterations == 0 and perf.n_outer == 1
+    assert np.all(psi == 0.0)
