@@ -377,7 +377,9 @@ def _same(a, b) -> bool:
 
 _NORM = {"reference": _capi.CF_NORM_REFERENCE_L2, "L2": _capi.CF_NORM_REFERENCE_L2,
          "openfoam": _capi.CF_NORM_OPENFOAM_L1, "L1": _capi.CF_NORM_OPENFOAM_L1}
-_REDUCE = {"fast": _capi.CF_REDUCE_FAST, "reference": _capi.CF_REDUCE_REFERENCE}
+# "auto" (the default): the reference order for BiCG, the fast one for the others
+_REDUCE = {"fast": _capi.CF_REDUCE_FAST, "reference": _capi.CF_REDUCE_REFERENCE,
+           "auto": _capi.CF_REDUCE_AUTO}
 _PREC = {"FP64": _capi.CF_PREC_FP64, "fp64": _capi.CF_PREC_FP64,
          "mixed": _capi.CF_PREC_MIXED}
 
@@ -433,7 +435,7 @@ class LduSolver:
         c.max_iter = int(d.get("maxIter", 1000))
         c.min_iter = int(d.get("minIter", 0))
         c.precision = _PREC[d.get("precision", "FP64")]
-        c.reduction = _REDUCE[d.get("reduction", "fast")]
+        c.reduction = _REDUCE[d.get("reduction", "auto")]
         c.norm_type = _NORM[d.get("normType", "reference")]
         c.memory = memory
         c.bicg_int_bound = float(d.get("intBound", 1e-10))

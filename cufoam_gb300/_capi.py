@@ -16,7 +16,7 @@ CF_OK, CF_NOT_CONVERGED, CF_BREAKDOWN, CF_NONFINITE, CF_BAD_INPUT, CF_CUDA_ERROR
 CF_CG, CF_BICG, CF_JACOBI, CF_MR, CF_MRJACOBI, CF_MRS, CF_JMR, CF_RICHARDSON, CF_PCG = range(9)
 CF_MEM_HOST, CF_MEM_DEVICE = 0, 1
 CF_PREC_FP64, CF_PREC_MIXED = 0, 1
-CF_REDUCE_FAST, CF_REDUCE_REFERENCE = 0, 1
+CF_REDUCE_FAST, CF_REDUCE_REFERENCE, CF_REDUCE_AUTO = 0, 1, 2
 CF_NORM_REFERENCE_L2, CF_NORM_OPENFOAM_L1 = 0, 1
 CF_FORMAT_AUTO, CF_FORMAT_CSR, CF_FORMAT_SELL = 0, 1, 2
 

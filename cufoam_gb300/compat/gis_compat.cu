@@ -68,7 +68,9 @@ cf::Context *shim_context()
 int reduction_order()
 {
     const char *e = std::getenv("CUFOAM_GIS_REDUCTION");
-    return (e && std::strcmp(e, "reference") == 0) ? CF_REDUCE_REFERENCE : CF_REDUCE_FAST;
+    if (e && std::strcmp(e, "reference") == 0) return CF_REDUCE_REFERENCE;
+    if (e && std::strcmp(e, "fast") == 0) return CF_REDUCE_FAST;
+    return CF_REDUCE_AUTO;
 }
 
 [[noreturn]] void rethrow(const cf::Error &e)

@@ -302,7 +302,7 @@ void cf_controls_init(cf_controls *c)
     c->max_iter = 1000;       // OpenFOAM default maxIter
     c->min_iter = 0;
     c->precision = CF_PREC_FP64;
-    c->reduction = CF_REDUCE_FAST;
+    c->reduction = CF_REDUCE_AUTO;
     c->memory = CF_MEM_HOST;
     c->norm_type = CF_NORM_REFERENCE_L2;
     c->bicg_int_bound = 1e-10;   // cuFoamBiCG/cuFoamBiCG.C:68

@@ -72,26 +72,29 @@ __device__ __forceinline__ void block_tree(T (&v)[NV], T *sm)
 #define CF_FAST_BLOCK_SUM 1
 #endif
 
-// Fast-order block sum (result valid in thread 0): an xor-shuffle tree in
-// every warp, the eight warp sums through shared memory, and a shuffle tree
-// over them in warp 0 -- one block barrier instead of three.
+// Fast-order block sum (result valid in thread 0): the 256 values through
+// shared memory, lane l of warp 0 adds values l, l + 32, ..., l + 224 in a
+// three-level tree, then a shuffle tree over the 32 lane sums.  A warp-wide
+// FP64 instruction occupies a GB300 sub-partition's FP64 unit for the same
+// time whatever its active lanes (measured: 19.6 G warp instructions/s with
+// 32 or with 1 active lane), so the block spends 12 FP64 instructions per
+// value here against 43 for a shuffle tree in every warp.
 template <int NV, class T>
 __device__ __forceinline__ void block_sum_fast(T (&v)[NV], T *sm)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int i = 0; i < NV; ++i) {
-#pragma unroll
-        for (int o = 16; o; o >>= 1) v[i] = v[i] + __shfl_xor_sync(kFull, v[i], o);
-        if (lane == 0) sm[i * kWarps + warp] = v[i];
-    }
+    for (int i = 0; i < NV; ++i) sm[i * kBlock + threadIdx.x] = v[i];
     __syncthreads();
     if (warp == 0) {
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            T x = lane < kWarps ? sm[i * kWarps + lane] : T(0);
+            const T *s = sm + i * kBlock + lane;
+            const T a = (s[0] + s[32]) + (s[64] + s[96]);
+            const T b = (s[128] + s[160]) + (s[192] + s[224]);
+            T x = a + b;
 #pragma unroll
-            for (int o = kWarps / 2; o; o >>= 1) x = x + __shfl_xor_sync(kFull, x, o);
+            for (int o = 16; o; o >>= 1) x = x + __shfl_xor_sync(kFull, x, o);
             v[i] = x;
         }
     }

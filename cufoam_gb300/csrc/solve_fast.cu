@@ -392,23 +392,35 @@ __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_rich_spmv(cons
 }
 
 // ---------------------------------------------------------------------------
-// MR family.  SCALED = false: MR; true: MRJacobi, MRS and JMR as MR on
-// L A R (a->sc_val, see scaled_values), which needs no prep pass.
-//   spmv:   y = A r (or L A R r), (r, y), (y, y) -> step
-//   update: x += alpha d, r -= alpha y, ||r|| with d = r (MR) or d = R r
-//           (R = a->corr_scale: MRJacobi's D^-1 r, JMR's D^-1/2 r)
+// MR family.  FORM kMrPlain: MR; kMrScaled: JMR as MR on D^-1/2 A D^-1/2
+// (a->sc_val, see scaled_values), which needs no prep pass; kMrZ: MRJacobi
+// and MRS in the reference's arithmetic (SolverSingleGPU.h:1000-1073), the
+// SpMV gathering z = D^-1 r, which the previous update wrote.
+//   spmv:   y = A r (A z, or L A R r), (r, y), (y, y) -> step
+//   update: x += alpha d, r -= alpha y, ||r|| with d = r (MR), R r (JMR:
+//           R = a->corr_scale = D^-1/2) or z (MRJacobi, MRS, which also
+//           write the next z = D^-1 r)
+// MRJacobi on a scaled A D^-1 -- one rounding of a_ij / a_jj in the
+// matrix instead of one of r_j / a_jj in the vector -- converged in 282-330
+// steps instead of the reference's 277 on a 32^3 lognormal system, outside
+// the 254-277 the reference itself takes when one source entry moves by
+// one ulp, while every unscaled summation order stayed inside; JMR's
+// scaled form stayed at the reference's count.
 // ---------------------------------------------------------------------------
-template <bool SCALED, int FMT>
+enum { kMrPlain = 0, kMrScaled = 1, kMrZ = 2 };
+
+template <int FORM, int FMT>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_mr_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
     CF_EXIT_IF_DONE(a, st, false);
     const double *__restrict__ r = a->r[0];
-    const double *val = SCALED ? a->sc_val : a->val;
-    const double *sval = SCALED ? a->sc_val : a->s_val;
+    const double *__restrict__ gv = FORM == kMrZ ? a->w[1] : a->r[0];
+    const double *val = FORM == kMrScaled ? a->sc_val : a->val;
+    const double *sval = FORM == kMrScaled ? a->sc_val : a->s_val;
     double *__restrict__ y = a->w[0];
     double acc[2] = {0.0, 0.0};
-    for_rows<FMT, double>(a, val, sval, [&](int c) { return r[c]; }, [&](int row, double v) {
+    for_rows<FMT, double>(a, val, sval, [&](int c) { return gv[c]; }, [&](int row, double v) {
         y[row] = v;
         acc[0] = fma_t(r[row], v, acc[0]);
         acc[1] = fma_t(v, v, acc[1]);
@@ -488,7 +500,7 @@ __global__ void __launch_bounds__(kBlock) k_f_bicg_update(const SolveArgs *__res
     }
 }
 
-template <bool SCALED>
+template <int FORM>
 __global__ void __launch_bounds__(kBlock) k_f_mr_update(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
@@ -498,31 +510,39 @@ __global__ void __launch_bounds__(kBlock) k_f_mr_update(const SolveArgs *__restr
     double *__restrict__ r = a->r[0];
     double *__restrict__ x = a->x;
     const double *__restrict__ y = a->w[0];
-    const double *__restrict__ R = a->corr_scale;
+    const double *__restrict__ R = FORM == kMrZ ? a->dinv : a->corr_scale;
+    double *__restrict__ z = a->w[1];
     double part[4] = {0.0, 0.0, 0.0, 0.0};
     CF_X4_LOOP(i, n) {
-        double rv[4], xv[4], yv[4], dv[4];
+        double rv[4], xv[4], yv[4], dv[4], sv[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             rv[u] = r[CF_X4_IDX(i, u)];
             xv[u] = x[CF_X4_IDX(i, u)];
             yv[u] = y[CF_X4_IDX(i, u)];
-            dv[u] = SCALED ? __dmul_rn(R[CF_X4_IDX(i, u)], rv[u]) : rv[u];
+            if (FORM == kMrZ) {
+                dv[u] = z[CF_X4_IDX(i, u)];
+                sv[u] = R[CF_X4_IDX(i, u)];
+            } else {
+                dv[u] = FORM == kMrScaled ? __dmul_rn(R[CF_X4_IDX(i, u)], rv[u]) : rv[u];
+            }
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             x[CF_X4_IDX(i, u)] = fma_t(alpha, dv[u], xv[u]);
             const double ri = fma_t(-alpha, yv[u], rv[u]);
             r[CF_X4_IDX(i, u)] = ri;
+            if (FORM == kMrZ) z[CF_X4_IDX(i, u)] = __dmul_rn(sv[u], ri);
             part[u] = fma_t(ri, ri, part[u]);
         }
     }
     CF_X4_TAIL(i, n) {
         const double ri0 = r[i];
-        const double di = SCALED ? __dmul_rn(R[i], ri0) : ri0;
+        const double di = FORM == kMrZ ? z[i] : FORM == kMrScaled ? __dmul_rn(R[i], ri0) : ri0;
         x[i] = fma_t(alpha, di, x[i]);
         const double ri = fma_t(-alpha, y[i], ri0);
         r[i] = ri;
+        if (FORM == kMrZ) z[i] = __dmul_rn(R[i], ri);
         part[0] = fma_t(ri, ri, part[0]);
     }
     double acc[1] = {(part[0] + part[1]) + (part[2] + part[3])};
@@ -561,14 +581,17 @@ static Kernels fast_kernels(int solver)
         k.k1 = (const void *)k_f_rich_spmv<FMT>;
         break;
     case CF_MR:
-        k.k1 = (const void *)k_f_mr_spmv<false, FMT>;
-        k.k2 = (const void *)k_f_mr_update<false>;
+        k.k1 = (const void *)k_f_mr_spmv<kMrPlain, FMT>;
+        k.k2 = (const void *)k_f_mr_update<kMrPlain>;
         break;
     case CF_MRJACOBI:
-    case CF_MRS:
-    case CF_JMR: // MR on L A R (scaled_values), set up by the caller
-        k.k1 = (const void *)k_f_mr_spmv<true, FMT>;
-        k.k2 = (const void *)k_f_mr_update<true>;
+    case CF_MRS: // z = D^-1 r of the initial residual written by k_res_init
+        k.k1 = (const void *)k_f_mr_spmv<kMrZ, FMT>;
+        k.k2 = (const void *)k_f_mr_update<kMrZ>;
+        break;
+    case CF_JMR: // MR on D^-1/2 A D^-1/2 (scaled_values), set up by the caller
+        k.k1 = (const void *)k_f_mr_spmv<kMrScaled, FMT>;
+        k.k2 = (const void *)k_f_mr_update<kMrScaled>;
         break;
     default: break;
     }

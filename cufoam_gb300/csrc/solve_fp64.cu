@@ -92,6 +92,7 @@ __global__ void __launch_bounds__(kBlock) k_res_init(const SolveArgs *__restrict
             if (mode == 1) ri = __dmul_rn(sD[row], ri);
             r[row] = ri;
             if (mode == 2) rs[row] = ri;
+            if (mode == 4) a->w[1][row] = __dmul_rn(dinv[row], ri); // z = D^-1 r
             acc[0] = fma_t(ri, ri, acc[0]);
             if (mode == 3) acc[1] = fma_t(ri, __dmul_rn(dinv[row], ri), acc[1]);
         }
@@ -583,8 +584,12 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     require(solver >= CF_CG && solver <= CF_PCG, CF_BAD_INPUT, "unknown solver");
     require(b_in && x_io, CF_BAD_INPUT, "source and psi must not be null");
     require(c.memory == CF_MEM_HOST || c.memory == CF_MEM_DEVICE, CF_BAD_INPUT, "bad memory kind");
-    require(c.reduction == CF_REDUCE_FAST || c.reduction == CF_REDUCE_REFERENCE, CF_BAD_INPUT,
-            "bad reduction");
+    require(c.reduction == CF_REDUCE_FAST || c.reduction == CF_REDUCE_REFERENCE ||
+                c.reduction == CF_REDUCE_AUTO, CF_BAD_INPUT, "bad reduction");
+    // AUTO: the reference order for BiCG, whose iterates follow the
+    // summation order chaotically (see CF_REDUCE_AUTO), the fast one else
+    const int reduction = c.reduction != CF_REDUCE_AUTO ? c.reduction
+                          : (solver == CF_BICG ? CF_REDUCE_REFERENCE : CF_REDUCE_FAST);
     const int n = m->n;
     require(n > 0, CF_BAD_INPUT, "empty matrix");
     const GridCap small(ctx, n);
@@ -594,9 +599,9 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
             "mixed precision is implemented for CG, BiCG, MR, MRJacobi, MRS and JMR");
     require(solver != CF_PCG || (!mixed && c.transpose == 0), CF_UNSUPPORTED,
             "the preconditioned CG is FP64 only");
-    require(solver != CF_PCG || c.reduction == CF_REDUCE_FAST, CF_UNSUPPORTED,
+    require(solver != CF_PCG || reduction == CF_REDUCE_FAST, CF_UNSUPPORTED,
             "the preconditioned CG has no reference summation order (no reference counterpart)");
-    const bool ref = c.reduction == CF_REDUCE_REFERENCE && !mixed;
+    const bool ref = reduction == CF_REDUCE_REFERENCE && !mixed;
     const int cap = stage_cap_for(m);
     const bool tr = c.transpose != 0;
     if (solver == CF_BICG || tr) matrix_ensure_transpose(m);
@@ -700,9 +705,9 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     A.abort_flag = (c.time_limit_s > 0) ? ctx->d_abort : nullptr;
 
     if (mixed) mixed_prepare(ctx, m, solver, A);
-    // fast order: MRJacobi, MRS and JMR run as MR on the scaled matrix,
-    // Jacobi as one pass over A D^-1
-    if (!ref && !mixed && (mr_scaled_solver(solver) || solver == CF_JACOBI))
+    // fast order: JMR runs as MR on the scaled matrix D^-1/2 A D^-1/2,
+    // Jacobi as one pass over A D^-1 (MRJacobi and MRS gather z = D^-1 r)
+    if (!ref && !mixed && (solver == CF_JMR || solver == CF_JACOBI))
         A.sc_val = scaled_values<double>(ctx, m, A, solver, tr, m->sc64, &A.corr_scale);
 
     DevState &S = *ctx->h_state;
@@ -766,6 +771,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     {
         // (the mixed JMR loop keeps the scaled residual as well)
         int mode = solver == CF_JMR ? 1 : mixed ? 0 : (solver == CF_BICG ? 2 : (solver == CF_PCG ? 3 : 0));
+        if (!ref && !mixed && (solver == CF_MRJACOBI || solver == CF_MRS)) mode = 4;
         void *a2[] = {&d_args, &mode};
         launch(ctx, ctx->stream, (const void *)k_res_init,
                launch_cfg(ctx, (const void *)k_res_init, !sell, cap, ref), a2);

@@ -126,8 +126,12 @@ cf_controls cuFoamGB300Solver::gb300Controls() const
     }
     const word precision = d.lookupOrDefault<word>("precision", word("FP64"));
     c.precision = (precision == "mixed") ? CF_PREC_MIXED : CF_PREC_FP64;
-    const word reduction = d.lookupOrDefault<word>("reduction", word("fast"));
-    c.reduction = (reduction == "reference") ? CF_REDUCE_REFERENCE : CF_REDUCE_FAST;
+    // "auto" (default): the reference's summation order for BiCG, the fast
+    // one for the others
+    const word reduction = d.lookupOrDefault<word>("reduction", word("auto"));
+    c.reduction = (reduction == "reference") ? CF_REDUCE_REFERENCE
+                  : (reduction == "fast")    ? CF_REDUCE_FAST
+                                             : CF_REDUCE_AUTO;
     const word normType = d.lookupOrDefault<word>("normType", word("reference"));
     c.norm_type = (normType == "openfoam") ? CF_NORM_OPENFOAM_L1 : CF_NORM_REFERENCE_L2;
     c.memory = CF_MEM_HOST;

@@ -12,7 +12,8 @@
  *
  * Optional controls (all default to the reference's behaviour):
  *     precision   FP64 | mixed        (mixed: FP32 inner solve, FP64 refinement)
- *     reduction   fast | reference    (reference: the reference's exact sums)
+ *     reduction   auto | fast | reference
+ *                 (auto: the reference's exact sums for BiCG, fast for the rest)
  *     normType    reference | openfoam
  *     useRelTol   false               (true: honour relTol_/minIter_ like OpenFOAM)
  *

@@ -66,13 +66,25 @@ enum {
                           MRS and JMR) */
 };
 
-/* Reduction order of dot products in FP64 solves. */
+/* Summation order of FP64 solves (row sums and dot products). */
 enum {
-    CF_REDUCE_FAST = 0,      /* deterministic tree over an occupancy-sized grid */
-    CF_REDUCE_REFERENCE = 1  /* the reference's order on this GPU: grid =
-                                maxThreadsPerSM/256 * SMs blocks of 256,
-                                sequential sum of block partials; gives the
-                                reference algorithm's exact bits */
+    CF_REDUCE_FAST = 0,      /* each row one FMA chain, dot products in a
+                                deterministic tree over an occupancy-sized grid */
+    CF_REDUCE_REFERENCE = 1, /* the reference's order on this GPU: rows in
+                                its 8-lane tree, grid = maxThreadsPerSM/256 *
+                                SMs blocks of 256, sequential sum of block
+                                partials; gives the reference algorithm's
+                                exact bits */
+    CF_REDUCE_AUTO = 2       /* the default (cf_controls_init): REFERENCE for
+                                BiCG, FAST for the other solvers.  BiCG's
+                                iterates follow the summation order
+                                chaotically on non-symmetric systems (on a
+                                48^3 convection-diffusion system at cell
+                                Peclet 3 two correct summation orders take
+                                350 and 377 steps; at 256^3 the fast order
+                                broke down where the reference order
+                                converges), so its default is the
+                                reference's bits */
 };
 
 /* normFactor flavour reported in cf_perf and used for the tolerance. */
@@ -109,7 +121,7 @@ typedef struct cf_controls {
     int32_t max_iter;        /* maxIter_; <= 0 means unlimited, as the reference */
     int32_t min_iter;        /* minIter_; 0 = none (the reference ignores it) */
     int32_t precision;       /* CF_PREC_* */
-    int32_t reduction;       /* CF_REDUCE_* (FP64 only) */
+    int32_t reduction;       /* CF_REDUCE_* (FP64 only; default AUTO) */
     int32_t memory;          /* where source and psi live: CF_MEM_* */
     int32_t norm_type;       /* CF_NORM_* */
     double bicg_int_bound;   /* BiCG breakdown bound, default 1e-10 */

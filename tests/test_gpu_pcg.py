@@ -1,15 +1,15 @@
 """Jacobi-preconditioned CG (cuFoamPCG; no reference counterpart -- the
 reference's roadmap announces preconditioners): checked against a textbook
 PCG with z = D^-1 r in numpy FP64 on the same system and stopping rule
-(||r||_2 <= tolerance * normFactor): iteration count within the fast-order
-slack, true residual at the tolerance; on high-contrast coefficients it
-needs fewer steps than CG."""
+(||r||_2 <= tolerance * normFactor): iteration count within the band of
+counts textbook PCG takes when one source entry moves by one ulp (widened
+by one step plus its width), true residual at the tolerance; on
+high-contrast coefficients it needs fewer steps than CG."""
 import numpy as np
 import pytest
 
 import cufoam_gb300 as cf
 import oracle as O
-from conftest import fast_order_iteration_slack
 
 pytestmark = pytest.mark.gpu
 
@@ -44,12 +44,19 @@ def test_pcg_matches_textbook_pcg(ctx, case):
     tol, maxit = 1e-9, 5000
     M = cf.LduMatrix.from_ldu(L, ctx)
     nf = O.norm_factor(A, b, np.zeros(L.n))
-    _, k_np = numpy_pcg(A, b, tol * nf, maxit)
+    ks = [numpy_pcg(A, b, tol * nf, maxit)[1]]
+    rng = np.random.default_rng(11)
+    for t in range(8):   # the textbook PCG's own one-ulp band
+        bb = b.copy()
+        i = int(rng.integers(L.n))
+        bb[i] = np.nextafter(bb[i], np.inf if t % 2 == 0 else -np.inf)
+        ks.append(numpy_pcg(A, bb, tol * nf, maxit)[1])
     for use_graph in (1, 0):
         psi = np.zeros(L.n)
         perf = cf.cuFoamPCG("p", M, {"tolerance": tol, "maxIter": maxit, "useGraph": use_graph}).solve(psi, b)
         assert perf.converged and perf.final_residual <= tol
-        assert abs(perf.n_iterations - k_np) <= fast_order_iteration_slack(k_np)
+        w = max(ks) - min(ks)
+        assert min(ks) - 1 - w <= perf.n_iterations <= max(ks) + 1 + w, (perf.n_iterations, ks)
         assert O.true_residual_norm(A, b, psi) / perf.norm_factor <= 1.5 * tol
     if case == "lognormal":
         cg = cf.cuFoamCG("p", M, {"tolerance": tol, "maxIter": maxit}).solve(np.zeros(L.n), b)

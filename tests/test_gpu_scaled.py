@@ -1,14 +1,15 @@
-"""Fast-order Jacobi, MRJacobi, MRS and JMR run on a cached diagonally
-scaled copy of the solved matrix (A D^-1, or D^-1/2 A D^-1/2 for JMR).
-These tests cover the copy's life cycle.  A transposed solve scales A^T,
-and a solve without transpose afterwards scales A again.  New coefficient
-values replace the copy."""
+"""Fast-order Jacobi and JMR run on a cached diagonally scaled copy of the
+solved matrix (A D^-1, or D^-1/2 A D^-1/2 for JMR); MRJacobi and MRS
+gather z = D^-1 r like the reference.  These tests cover the scaled copy's
+life cycle, and the same transposed solves and value updates for all four
+solvers.  A transposed solve scales A^T, and a solve without transpose
+afterwards scales A again.  New coefficient values replace the copy."""
 import numpy as np
 import pytest
 
 import cufoam_gb300 as cf
 import oracle as O
-from conftest import fast_order_iteration_slack
+from conftest import assert_fast_order_parity, reference_band
 
 pytestmark = pytest.mark.gpu
 
@@ -27,9 +28,8 @@ def _scaled_true_rel(L, b, psi, nf, jmr):
 @pytest.mark.parametrize("fmt", ["sell", "csr"])
 @pytest.mark.parametrize("name", ["Jacobi", "MRJacobi", "MRS", "JMR"])
 def test_scaled_matrix_solvers_transpose_and_value_update(ctx, name, fmt):
-    """The fast-order Jacobi and MR family run on a cached scaled copy of
-    the solved matrix (A D^-1 or D^-1/2 A D^-1/2): a transposed solve scales
-    A^T, and new coefficient values replace the cached copy."""
+    """Transposed solves and new coefficient values in the fast order:
+    iteration counts within the reference's one-ulp band."""
     kind = O.SOLVER_NAMES[name]
     L, _ = O.grid_convdiff(14, 12, 10, 9, 4.0)
     b = O.uniform(5, L.n)
@@ -45,7 +45,7 @@ def test_scaled_matrix_solvers_transpose_and_value_update(ctx, name, fmt):
             psi, b, transpose=transpose)
         assert M.format()[0] == fmt
         assert perf.converged, (transpose, perf.status_name)
-        assert abs(perf.n_iterations - want.n_iterations) <= fast_order_iteration_slack(want.n_iterations)
+        assert_fast_order_parity(perf, want, reference_band(kind, Ls, b, np.zeros(L.n), tol, maxit), tol)
         assert _scaled_true_rel(Ls, b, psi, perf.norm_factor, jmr) <= 1.5 * tol
         assert np.linalg.norm(psi - want.psi) <= 1e-6 * np.linalg.norm(want.psi)
     # new values (a stronger diagonal): the next solve must use them
@@ -55,6 +55,6 @@ def test_scaled_matrix_solvers_transpose_and_value_update(ctx, name, fmt):
     psi = np.zeros(L.n)
     perf = cf._TABLE["cuFoam" + name]("p", M, {"tolerance": tol, "maxIter": maxit}).solve(psi, b)
     assert perf.converged
-    assert abs(perf.n_iterations - want.n_iterations) <= fast_order_iteration_slack(want.n_iterations)
+    assert_fast_order_parity(perf, want, reference_band(kind, L2, b, np.zeros(L.n), tol, maxit), tol)
     assert _scaled_true_rel(L2, b, psi, perf.norm_factor, jmr) <= 1.5 * tol
     assert np.linalg.norm(psi - want.psi) <= 1e-6 * np.linalg.norm(want.psi)

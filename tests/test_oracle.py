@@ -348,3 +348,28 @@ def test_fp32_bicgstab_reaches_inner_tolerance_where_fp32_bicg_fails():
     bn = b / np.linalg.norm(b)
     true_rel = np.linalg.norm(bn - M @ x.astype(np.float64))
     assert steps < 2000 and true_rel < 2e-4
+
+
+def test_reference_iteration_count_moves_under_one_ulp_source_changes():
+    """The reference algorithm's own iteration count on an ill-conditioned
+    system moves by more than one step when a single source entry changes by
+    one ulp, so no summation order other than the reference's can promise
+    +-1 there (the GPU tests hold the fast order to this band).  On the
+    constant-coefficient 2-D Poisson system (C1) the count does not move."""
+    def counts(kind, L, tol, trials=6):
+        b = O.uniform(3, L.n)
+        ks = [O.plugin_solve(kind, L, b, np.zeros(L.n), tol, 100000).n_iterations]
+        rng = np.random.default_rng(0)
+        for _ in range(trials):
+            bb = b.copy()
+            i = int(rng.integers(L.n))
+            bb[i] = np.nextafter(bb[i], np.inf)
+            ks.append(O.plugin_solve(kind, L, bb, np.zeros(L.n), tol, 100000).n_iterations)
+        return ks
+    L = O.grid_lognormal(32, 32, 32, 2)
+    cg = counts(O.CG, L, 1e-8)
+    mrj = counts(O.MRJACOBI, L, 1e-8)
+    assert cg[0] == 356 and max(cg) - min(cg) >= 2, cg
+    assert mrj[0] == 277 and max(mrj) - min(mrj) >= 10, mrj
+    c1 = counts(O.CG, O.grid_const(64, 64, 1), 1e-6, trials=3)
+    assert len(set(c1)) == 1, c1
