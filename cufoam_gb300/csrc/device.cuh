@@ -195,10 +195,20 @@ __host__ __device__ __forceinline__ size_t stage_bytes_per_warp(int cap)
     return (size_t)(cap + 8) * sizeof(V) + (size_t)(cap + 8) * sizeof(int32_t);
 }
 
+// Rows longer than this are summed by the whole warp (fast order): lane j
+// takes the row's entries j, j + 32, ... as one FMA chain, then a fixed
+// xor-shuffle tree adds the 32 lane sums.  One lane per row stays the rule
+// below it: every warp-wide FP64 instruction costs a GB300 sub-partition
+// the same whatever its active lanes, so splitting short rows over lanes
+// would multiply the FP64 instructions per row, while a long row summed by
+// one lane serialises the warp (a 3,000-entry row: 3,000 dependent FMAs).
+constexpr int kLongRow = 32;
+
 template <class V>
 struct Chunk {
     int rs, re;        // this lane's row [rs, re)
     int ov, oc;        // staging origins (element index of slot 0); -1 = not staged
+    unsigned lng;      // lanes whose row is longer than kLongRow
     const V *sv;
     const int32_t *sc;
 };
@@ -224,7 +234,8 @@ __device__ __forceinline__ Chunk<V> stage_chunk(const int32_t *__restrict__ ro,
     const int ee = last;
     c.sv = sv;
     c.sc = sc;
-    if (cap <= 0 || ee - eb > cap) {
+    c.lng = __ballot_sync(kFull, c.re - c.rs > kLongRow);
+    if (c.lng || cap <= 0 || ee - eb > cap) {
         c.ov = -1;
         c.oc = -1;
         return c;
@@ -345,8 +356,31 @@ __device__ __forceinline__ void row_product2(const Chunk<V> &c, const int32_t *_
     y2 = tree8(u);
 }
 
+// The fixed xor-shuffle tree of a long row's 32 lane sums: every lane ends
+// with the same bits (a + b == b + a in IEEE arithmetic).
+template <class V>
+__device__ __forceinline__ V warp_sum(V v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = add_t(v, __shfl_xor_sync(kFull, v, o));
+    return v;
+}
+
+// One long row summed by the whole warp: entries at cp[stride * t],
+// vp[stride * t] for t < len (CSR: stride 1; SELL slots: stride 32), lane j
+// taking t = j, j + 32, ...
+template <class V, class G>
+__device__ __forceinline__ V warp_row(const int32_t *cp, const V *vp, int len, int stride, G g)
+{
+    V acc = V(0);
+    for (int t = threadIdx.x & 31; t < len; t += 32)
+        acc = fma_t(vp[(size_t)stride * t], g(cp[(size_t)stride * t]), acc);
+    return warp_sum(acc);
+}
+
 // sum_j a_ij * g(j) as one FMA chain in entry order: one FP64 instruction
-// per entry, the least work per row (the fast reduction order).
+// per entry, the least work per row (the fast reduction order); rows longer
+// than kLongRow summed by the whole warp (warp_row).
 template <class V, class G>
 __device__ __forceinline__ V row_chain(const Chunk<V> &c, const int32_t *__restrict__ col,
                                        const V *__restrict__ val, G g)
@@ -355,7 +389,15 @@ __device__ __forceinline__ V row_chain(const Chunk<V> &c, const int32_t *__restr
     if (c.ov >= 0) {
         for (int j = c.rs; j < c.re; ++j) acc = fma_t(c.sv[j - c.ov], g(c.sc[j - c.oc]), acc);
     } else {
-        for (int j = c.rs; j < c.re; ++j) acc = fma_t(__ldg(val + j), g(__ldg(col + j)), acc);
+        const int lane = threadIdx.x & 31;
+        if (!((c.lng >> lane) & 1u))
+            for (int j = c.rs; j < c.re; ++j) acc = fma_t(__ldg(val + j), g(__ldg(col + j)), acc);
+        for (unsigned m = c.lng; m; m &= m - 1) {
+            const int r = __ffs(m) - 1;
+            const int rs = __shfl_sync(kFull, c.rs, r), re = __shfl_sync(kFull, c.re, r);
+            const V s = warp_row(col + rs, val + rs, re - rs, 1, g);
+            if (lane == r) acc = s;
+        }
     }
     return acc;
 }
@@ -367,11 +409,24 @@ __device__ __forceinline__ void row_chain2(const Chunk<V> &c, const int32_t *__r
                                            G1 g1, G2 g2, V &y1, V &y2)
 {
     V a1 = V(0), a2 = V(0);
-    for (int j = c.rs; j < c.re; ++j) {
-        const int cc = (c.oc >= 0) ? c.sc[j - c.oc] : __ldg(col + j);
-        const V v1 = (c.ov >= 0) ? c.sv[j - c.ov] : __ldg(val1 + j);
-        a1 = fma_t(v1, g1(cc), a1);
-        a2 = fma_t(__ldg(val2 + j), g2(cc), a2);
+    const int lane = threadIdx.x & 31;
+    if (!((c.lng >> lane) & 1u)) {
+        for (int j = c.rs; j < c.re; ++j) {
+            const int cc = (c.oc >= 0) ? c.sc[j - c.oc] : __ldg(col + j);
+            const V v1 = (c.ov >= 0) ? c.sv[j - c.ov] : __ldg(val1 + j);
+            a1 = fma_t(v1, g1(cc), a1);
+            a2 = fma_t(__ldg(val2 + j), g2(cc), a2);
+        }
+    }
+    for (unsigned m = c.lng; m; m &= m - 1) {
+        const int r = __ffs(m) - 1;
+        const int rs = __shfl_sync(kFull, c.rs, r), re = __shfl_sync(kFull, c.re, r);
+        const V s1 = warp_row(col + rs, val1 + rs, re - rs, 1, g1);
+        const V s2 = warp_row(col + rs, val2 + rs, re - rs, 1, g2);
+        if (lane == r) {
+            a1 = s1;
+            a2 = s2;
+        }
     }
     y1 = a1;
     y2 = a2;
@@ -422,13 +477,65 @@ __device__ __forceinline__ int32_t ld_stream(const int32_t *p, uint64_t pol)
     return v;
 }
 
+// M entries of a SELL row (slots 32 elements apart): all loads and gathers
+// issued before the first FMA, then one FMA chain in slot order.
+template <class V, int M, class G>
+__device__ __forceinline__ void sell_batch(const int32_t *cp, const V *vp, uint64_t pol, G g, V &acc)
+{
+    int c[M];
+    V v[M], x[M];
+#pragma unroll
+    for (int u = 0; u < M; ++u) {
+        c[u] = ld_stream(cp + 32 * u, pol);
+        v[u] = ld_stream(vp + 32 * u, pol);
+    }
+#pragma unroll
+    for (int u = 0; u < M; ++u) x[u] = g(c[u]);
+#pragma unroll
+    for (int u = 0; u < M; ++u) acc = fma_t(v[u], x[u], acc);
+}
+
+// the last r < B entries of a row as one exact batch
+template <class V, int B, class G>
+__device__ __forceinline__ void sell_tail(int r, const int32_t *cp, const V *vp, uint64_t pol, G g, V &acc)
+{
+    if constexpr (B > 1) {
+        if (r == B - 1) {
+            sell_batch<V, B - 1>(cp, vp, pol, g, acc);
+            return;
+        }
+        sell_tail<V, B - 1>(r, cp, vp, pol, g, acc);
+    }
+}
+
+// A slice's rows longer than kLongRow (row lengths from the CSR offsets
+// `ro`) summed by the whole warp over their own slots, the bits of the CSR
+// passes (warp_row); `acc` is this lane's sum, replaced for those lanes.
+template <class V, class G>
+__device__ __forceinline__ void sell_long_rows(int n, int s, const int32_t *__restrict__ ro,
+                                               const int32_t *cp0, const V *vp0, G g, V &acc)
+{
+    const int lane = threadIdx.x & 31;
+    const int row = s * 32 + lane;
+    const int rl = row < n ? __ldg(ro + row + 1) - __ldg(ro + row) : 0;
+    for (unsigned m = __ballot_sync(kFull, rl > kLongRow); m; m &= m - 1) {
+        const int r = __ffs(m) - 1;
+        const V v = warp_row(cp0 + r, vp0 + r, __shfl_sync(kFull, rl, r), 32, g);
+        if (lane == r) acc = v;
+    }
+}
+
 // f(row, sum_t val[t] g(col[t])) for every row, one warp per slice; the
 // entries are taken B at a time (all B loads and gathers issued before the
-// first FMA).  The slice length is warp-uniform, so the guards never diverge.
+// first FMA), the row's last r < B entries as an exact batch: a guarded slot
+// of a full batch would still issue its FMA (measured: 9 DFMA per 7-entry
+// row).  The slice length is warp-uniform, so the branches never diverge.
+// Matrices with rows longer than kLongRow (has_long) sum those rows with
+// the whole warp (sell_long_rows), as the CSR passes do.
 template <class V, int B, class G, class F>
 __device__ __forceinline__ void sell_rows(int n, int n_slices, const int32_t *__restrict__ off,
                                           const int32_t *__restrict__ col, const V *__restrict__ val,
-                                          G g, F f)
+                                          const int32_t *__restrict__ ro, bool has_long, G g, F f)
 {
     const uint64_t pol = l2_evict_first_policy();
     const int lane = threadIdx.x & 31;
@@ -439,22 +546,10 @@ __device__ __forceinline__ void sell_rows(int n, int n_slices, const int32_t *__
         const int32_t *cp = col + b + lane;
         const V *vp = val + b + lane;
         V acc = V(0);
-        for (int t0 = 0; t0 < len; t0 += B) {
-            int c[B];
-            V v[B], x[B];
-#pragma unroll
-            for (int u = 0; u < B; ++u)
-                if (t0 + u < len) {
-                    c[u] = ld_stream(cp + 32 * (t0 + u), pol);
-                    v[u] = ld_stream(vp + 32 * (t0 + u), pol);
-                }
-#pragma unroll
-            for (int u = 0; u < B; ++u)
-                if (t0 + u < len) x[u] = g(c[u]);
-#pragma unroll
-            for (int u = 0; u < B; ++u)
-                if (t0 + u < len) acc = fma_t(v[u], x[u], acc);
-        }
+        int t0 = 0;
+        for (; t0 + B <= len; t0 += B) sell_batch<V, B>(cp + 32 * t0, vp + 32 * t0, pol, g, acc);
+        sell_tail<V, B>(len - t0, cp + 32 * t0, vp + 32 * t0, pol, g, acc);
+        if (has_long) sell_long_rows(n, s, ro, col + b, val + b, g, acc);
         const int row = s * 32 + lane;
         if (row < n) f(row, acc);
     }
@@ -464,7 +559,8 @@ __device__ __forceinline__ void sell_rows(int n, int n_slices, const int32_t *__
 template <class V, int B, class G1, class G2, class F>
 __device__ __forceinline__ void sell_rows2(int n, int n_slices, const int32_t *__restrict__ off,
                                            const int32_t *__restrict__ col, const V *__restrict__ val1,
-                                           const V *__restrict__ val2, G1 g1, G2 g2, F f)
+                                           const V *__restrict__ val2, const int32_t *__restrict__ ro,
+                                           bool has_long, G1 g1, G2 g2, F f)
 {
     const uint64_t pol = l2_evict_first_policy();
     const int lane = threadIdx.x & 31;
@@ -498,6 +594,10 @@ __device__ __forceinline__ void sell_rows2(int n, int n_slices, const int32_t *_
                     a1 = fma_t(v1[u], x1[u], a1);
                     a2 = fma_t(v2[u], x2[u], a2);
                 }
+        }
+        if (has_long) {
+            sell_long_rows(n, s, ro, col + b, val1 + b, g1, a1);
+            sell_long_rows(n, s, ro, col + b, val2 + b, g2, a2);
         }
         const int row = s * 32 + lane;
         if (row < n) f(row, a1, a2);

@@ -95,6 +95,7 @@ struct SolveArgs {
     const float *valT32;
     // SELL-32 copy of the matrix for the fast kernels (n_slices = 0: none)
     int32_t n_slices;
+    int32_t has_long;          // some row has more than kLongRow entries (device.cuh)
     const int32_t *s_off;      // [n_slices + 1] element offset of each slice
     const int32_t *s_col;
     const double *s_val;
@@ -226,7 +227,8 @@ struct Matrix {
     Context *ctx = nullptr;
     int32_t n = 0, nf = 0;
     int64_t nnz = 0;
-    int32_t max_chunk = 0;     // max nnz over 32-row chunks
+    int32_t max_chunk = 0;     // max nnz over 32-row chunks without a long row
+    bool has_long = false;     // some row has more than kLongRow entries (device.cuh)
     // CSR (reference layout) + transpose values on the same pattern
     DeviceBuffer ro, col, val, valT, val32, valT32;
     // LDU copy (for value updates, the transpose and adjoint scatter)

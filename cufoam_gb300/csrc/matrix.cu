@@ -186,16 +186,27 @@ __global__ void k_fill_csr(int n, const int32_t *__restrict__ ls, const int32_t 
     }
 }
 
-__global__ void k_max_chunk(int n, const int32_t *__restrict__ ro, int *out)
+// out[0]: max nnz over the 32-row chunks without a row longer than
+// kLongRow (the staging capacity the fast CSR passes need); out[1]: 1 if
+// some row is longer (those chunks are read unstaged, long rows by the
+// whole warp)
+__global__ void k_chunk_stats(int n, const int32_t *__restrict__ ro, int *out)
 {
-    int m = 0;
+    int m = 0, lng = 0;
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) * 32; base < n;
          base += gridDim.x * blockDim.x * 32) {
         const int top = base + 32 < n ? base + 32 : n;
-        const int c = ro[top] - ro[base];
-        m = c > m ? c : m;
+        bool has = false;
+        for (int r = base; r < top; ++r) has = has || (ro[r + 1] - ro[r] > kLongRow);
+        if (has) {
+            lng = 1;
+        } else {
+            const int c = ro[top] - ro[base];
+            m = c > m ? c : m;
+        }
     }
     atomicMax(out, m);
+    if (lng) atomicMax(out + 1, 1);
 }
 
 __global__ void k_diag_derived(int n, const double *__restrict__ diag, double *dinv,
@@ -345,10 +356,12 @@ __global__ void k_sell_fill(int n, int n_slices, const int32_t *__restrict__ ro,
 __global__ void CF_PLAIN_SPMV_BOUNDS k_spmv_sell(int n, int n_slices, const int32_t *__restrict__ off,
                                                       const int32_t *__restrict__ col,
                                                       const double *__restrict__ val,
+                                                      const int32_t *__restrict__ ro, int has_long,
                                                       const double *__restrict__ x, double *y)
 {
-    sell_rows<double, CF_PLAIN_SPMV_BATCH>(n, n_slices, off, col, val, [&](int c) { return __ldg(x + c); },
-                         [&](int row, double v) { y[row] = v; });
+    sell_rows<double, CF_PLAIN_SPMV_BATCH>(n, n_slices, off, col, val, ro, has_long != 0,
+                                           [&](int c) { return __ldg(x + c); },
+                                           [&](int row, double v) { y[row] = v; });
 }
 
 // ---------------------------------------------------------------------------
@@ -487,6 +500,24 @@ static int read_flag(Context *ctx, const int *d_flag)
     return h;
 }
 
+// chunk statistics of m's CSR pattern into m->max_chunk / m->has_long
+static void chunk_stats(Context *ctx, Matrix *m)
+{
+    DeviceBuffer buf;
+    buf.ensure(2 * sizeof(int));
+    CF_CUDA(cudaMemsetAsync(buf.ptr, 0, 2 * sizeof(int), ctx->stream));
+    if (m->n > 0) {
+        k_chunk_stats<<<grid_for(ctx, ((int64_t)m->n + 31) / 32), kBlock, 0, ctx->stream>>>(
+            m->n, m->ro.as<int32_t>(), buf.as<int>());
+        CF_CHECK_LAUNCH();
+    }
+    int h[2] = {0, 0};
+    CF_CUDA(cudaMemcpyAsync(h, buf.ptr, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CF_CUDA(cudaStreamSynchronize(ctx->stream));
+    m->max_chunk = h[0];
+    m->has_long = h[1] != 0;
+}
+
 // Copies the LDU arrays to `m`, validates and completes the addressing,
 // builds the CSR.  When `out_*` are given the CSR is written there instead.
 static void build_from_ldu(Context *ctx, Matrix *m, const cf_ldu_view &v)
@@ -587,13 +618,8 @@ static void build_from_ldu(Context *ctx, Matrix *m, const cf_ldu_view &v)
                                                    m->val.as<double>());
         CF_CHECK_LAUNCH();
     }
-    // staging capacity: max nnz over 32-row chunks
-    CF_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
-    if (n > 0) {
-        k_max_chunk<<<grid_for(ctx, (n + 31) / 32), kBlock, 0, ctx->stream>>>(n, m->ro.as<int32_t>(), d_err);
-        CF_CHECK_LAUNCH();
-    }
-    m->max_chunk = read_flag(ctx, d_err);
+    // staging capacity and long rows
+    chunk_stats(ctx, m);
     m->dinv.ensure(sizeof(double) * (n + pad));
     m->dinv_sqrt.ensure(sizeof(double) * (n + pad));
     if (n > 0) {
@@ -800,11 +826,7 @@ Matrix *matrix_from_csr(Context *ctx, int n, int64_t nnz, const int32_t *ro, con
         k_diag_derived<<<gc, kBlock, 0, ctx->stream>>>(n, m->diag.as<double>(), m->dinv.as<double>(),
                                                        m->dinv_sqrt.as<double>());
         CF_CHECK_LAUNCH();
-        CF_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int), ctx->stream));
-        k_max_chunk<<<grid_for(ctx, (n + 31) / 32), kBlock, 0, ctx->stream>>>(n, m->ro.as<int32_t>(),
-                                                                               flag.as<int>());
-        CF_CHECK_LAUNCH();
-        m->max_chunk = read_flag(ctx, flag.as<int>());
+        chunk_stats(ctx, m);
     } catch (...) {
         delete m;
         throw;
@@ -964,7 +986,8 @@ void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order)
         } else {
             const int g = ctx->fast_grid((const void *)k_spmv_sell, 0);
             k_spmv_sell<<<g, kBlock, 0, ctx->stream>>>(m->n, m->n_slices, m->s_off.as<int32_t>(),
-                                                       m->s_col.as<int32_t>(), sv, x, y);
+                                                       m->s_col.as<int32_t>(), sv, m->ro.as<int32_t>(),
+                                                       m->has_long ? 1 : 0, x, y);
         }
         CF_CHECK_LAUNCH();
         return;

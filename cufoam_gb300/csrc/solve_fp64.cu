@@ -553,6 +553,7 @@ double norm_factor(Matrix *m, const double *b, const double *x, int norm_type, b
     const bool sell = matrix_ensure_sell(m, false, false);
     if (sell) {
         A.n_slices = m->n_slices;
+        A.has_long = m->has_long ? 1 : 0;
         A.s_off = m->s_off.as<int32_t>();
         A.s_col = m->s_col.as<int32_t>();
         A.s_val = m->s_val.as<double>();
@@ -670,6 +671,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     A.valT = m->have_valT ? m->valT.as<double>() : nullptr;
     if (sell) {
         A.n_slices = m->n_slices;
+        A.has_long = m->has_long ? 1 : 0;
         A.s_off = m->s_off.as<int32_t>();
         A.s_col = m->s_col.as<int32_t>();
         A.s_val = m->s_val.as<double>();

@@ -50,7 +50,7 @@ __device__ __forceinline__ void for_rows(const SolveArgs *a, const V *val, const
 {
     if constexpr (FMT == kSell) {
         constexpr int B = BATCH > 0 ? BATCH : (sizeof(V) == 4 ? kSellBatch32 : kSellBatch);
-        sell_rows<V, B>(a->n, a->n_slices, a->s_off, a->s_col, sval, g, f);
+        sell_rows<V, B>(a->n, a->n_slices, a->s_off, a->s_col, sval, a->ro, a->has_long != 0, g, f);
     } else {
         const int n = a->n, cap = a->stage_cap;
         CF_STAGE(V, cap);
@@ -70,7 +70,7 @@ __device__ __forceinline__ void for_rows2(const SolveArgs *a, const V *val1, con
                                           const V *sval2, G1 g1, G2 g2, F f)
 {
     if constexpr (FMT == kSell) {
-        sell_rows2<V, 1>(a->n, a->n_slices, a->s_off, a->s_col, sval1, sval2, g1, g2, f);
+        sell_rows2<V, 1>(a->n, a->n_slices, a->s_off, a->s_col, sval1, sval2, a->ro, a->has_long != 0, g1, g2, f);
     } else {
         const int n = a->n, cap = a->stage_cap;
         CF_STAGE(V, cap);

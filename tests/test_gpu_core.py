@@ -103,14 +103,41 @@ def _star_ldu(n):
                  rng.standard_normal(n - 1), la, ua)
 
 
-@pytest.mark.parametrize("case", ["c1", "lognormal", "convdiff", "star", "permuted"])
+def _skewed_ldu(n, seed, hubs=40, spd=True):
+    """A chain of n cells plus `hubs` hub cells coupled to 40..2,000 random
+    higher-numbered cells (power-law-like degrees): rows from 2 to ~2,000
+    entries, so 32-row chunks mix short and long rows.  Symmetric
+    coefficients and a dominant diagonal make it SPD."""
+    rng = np.random.default_rng(seed)
+    edges = {(i, i + 1) for i in range(n - 1)}
+    hub_cells = rng.choice(n // 2, size=hubs, replace=False)
+    for h in hub_cells:
+        deg = int(min(n - h - 1, 40 * (1 + rng.pareto(1.2)), 2000))
+        for j in rng.choice(np.arange(h + 1, n), size=deg, replace=False):
+            edges.add((int(h), int(j)))
+    e = np.array(sorted(edges), dtype=np.int32)
+    la, ua = e[:, 0].copy(), e[:, 1].copy()
+    w = rng.uniform(0.5, 1.5, size=len(e))
+    up = -w
+    lo = -w if spd else -w * rng.uniform(0.5, 1.5, size=len(e))
+    diag = np.ones(n)
+    np.add.at(diag, la, np.abs(up) + np.abs(lo))
+    np.add.at(diag, ua, np.abs(up) + np.abs(lo))
+    return O.LDU(n, diag, lo, up, la, ua)
+
+
+SPMV_CASES = {"c1": lambda: O.grid_const(64, 64, 1),
+              "lognormal": lambda: O.grid_lognormal(20, 17, 9, 3),
+              "convdiff": lambda: O.grid_convdiff(16, 15, 14, 4)[0],
+              "star": lambda: _star_ldu(3000),
+              "skewed": lambda: _skewed_ldu(20000, 3, spd=False),
+              "permuted": lambda: O.permute_ldu(O.grid_lognormal(11, 10, 9, 6), O.permutation(6, 990)),
+              }
+
+
+@pytest.mark.parametrize("case", ["c1", "lognormal", "convdiff", "star", "skewed", "permuted"])
 def test_spmv_bit_exact(ctx, case):
-    L = {"c1": lambda: O.grid_const(64, 64, 1),
-         "lognormal": lambda: O.grid_lognormal(20, 17, 9, 3),
-         "convdiff": lambda: O.grid_convdiff(16, 15, 14, 4)[0],
-         "star": lambda: _star_ldu(3000),
-         "permuted": lambda: O.permute_ldu(O.grid_lognormal(11, 10, 9, 6), O.permutation(6, 990)),
-         }[case]()
+    L = SPMV_CASES[case]()
     M = _matrix(ctx, L)
     x = O.uniform(7, L.n)
     A = O.ldu2csr(L)
@@ -123,22 +150,18 @@ def test_spmv_bit_exact(ctx, case):
     assert np.allclose(y, ref, rtol=1e-14, atol=1e-14 * np.abs(ref).max())
 
 
-@pytest.mark.parametrize("case", ["c1", "lognormal", "convdiff", "star", "permuted", "ragged"])
+@pytest.mark.parametrize("case", ["c1", "lognormal", "convdiff", "star", "skewed", "permuted", "ragged"])
 def test_spmv_formats_agree(ctx, case):
     """The fast kernels read CSR (warp-chunk staging) or the SELL-32 copy;
-    both sum each row as one FMA chain in entry order, so they agree
-    exactly (zeros up to sign), for A and A^T, and after a value update."""
-    L = {"c1": lambda: O.grid_const(64, 64, 1),
-         "lognormal": lambda: O.grid_lognormal(20, 17, 9, 3),
-         "convdiff": lambda: O.grid_convdiff(16, 15, 14, 4)[0],
-         "star": lambda: _star_ldu(3000),
-         "permuted": lambda: O.permute_ldu(O.grid_lognormal(11, 10, 9, 6), O.permutation(6, 990)),
-         "ragged": lambda: O.grid_lognormal(7, 5, 3, 9),   # 105 rows: last slice partly empty
-         }[case]()
+    both sum each row of up to 32 entries as one FMA chain in entry order
+    and each longer row with the whole warp in the same lane partition, so
+    they agree exactly (zeros up to sign), for A and A^T, and after a value
+    update."""
+    L = SPMV_CASES[case]() if case != "ragged" else O.grid_lognormal(7, 5, 3, 9)  # 105 rows
     M = _matrix(ctx, L)
     fmt, stored = M.format()
     nnz = M.shape()[2]
-    if case == "star":
+    if case in ("star", "skewed"):
         assert fmt == "csr" and stored == nnz      # padding to the long row: too much
     else:
         assert fmt == "sell" and nnz <= stored <= 1.2 * nnz + 256
@@ -277,6 +300,31 @@ def test_bicg_defaults_to_the_reference_order(ctx, ref_grid, case):
     assert psi.tobytes() == want.psi.tobytes()
 
 
+@pytest.mark.parametrize("fmt", ["csr", "sell"])
+def test_solvers_on_skewed_rows(ctx, ref_grid, fmt):
+    """Rows from 2 to ~2,000 entries (hub cells): the reference order is the
+    oracle's bits on both storage formats; the fast order (long rows summed
+    by the whole warp) stays within the reference's one-ulp band for CG and
+    Jacobi."""
+    L = _skewed_ldu(6000, 8)
+    b = O.uniform(4, L.n)
+    tol, maxit = 1e-9, 20000
+    M = _matrix(ctx, L)
+    M.set_format(fmt)
+    for name, kind in (("cuFoamCG", O.CG), ("cuFoamJacobi", O.JACOBI)):
+        want = O.plugin_solve(kind, L, b, np.zeros(L.n), tol, maxit, grid=ref_grid)
+        psi = np.zeros(L.n)
+        perf = cf._TABLE[name]("p", M, {"tolerance": tol, "maxIter": maxit,
+                                        "reduction": "reference"}).solve(psi, b, history=maxit + 1)
+        assert perf.n_iterations == want.n_iterations
+        assert psi.tobytes() == want.psi.tobytes()
+        psi = np.zeros(L.n)
+        fast = cf._TABLE[name]("p", M, {"tolerance": tol, "maxIter": maxit}).solve(psi, b)
+        band = reference_band(kind, L, b, np.zeros(L.n), tol, maxit, grid=ref_grid)
+        assert_fast_order_parity(fast, want, band, tol)
+        assert O.true_residual_norm(O.ldu2csr(L), b, psi) / fast.norm_factor <= 1.5 * tol
+
+
 def test_graph_and_host_loop_agree(ctx):
     L = O.grid_lognormal(16, 16, 8, 4)
     b = O.uniform(5, L.n)
@@ -398,3 +446,32 @@ def test_small_system_cg_single_launch(ctx, case, fmt):
         assert perf.converged and perf.final_residual <= tol
         true_rel = O.true_residual_norm(O.ldu2csr(L), b, out) / perf.norm_factor
         assert true_rel <= 1.5 * tol
+
+
+@pytest.mark.parametrize("offset", [0, 1])
+def test_cg_odd_size_and_unaligned_device_vectors(ctx, offset):
+    """The fast CG prep pass takes element pairs as 16-byte loads when psi and
+    the work vectors are 16-byte aligned, and a scalar loop otherwise; an odd
+    row count leaves one element outside the pairs.  Both paths give the
+    same iterates (one FMA per element either way)."""
+    import torch
+    L = O.grid_lognormal(11, 9, 7, 3)            # 693 rows
+    b = O.uniform(5, L.n)
+    tol, maxit = 1e-10, 5000
+    M = _matrix(ctx, L)
+    want = O.plugin_solve(O.CG, L, b, np.zeros(L.n), tol, maxit)
+    buf = torch.zeros(L.n + 1, dtype=torch.float64, device="cuda")
+    psi = buf[offset:offset + L.n]               # offset 1: 8 bytes past a 16-byte boundary
+    src = torch.from_numpy(b).cuda()
+    perf = cf.cuFoamCG("p", M, {"tolerance": tol, "maxIter": maxit}).solve(psi, src, history=maxit + 1)
+    torch.cuda.synchronize()
+    band = reference_band(O.CG, L, b, np.zeros(L.n), tol, maxit)
+    assert_fast_order_parity(perf, want, band, tol)
+    x = psi.cpu().numpy()
+    assert O.true_residual_norm(O.ldu2csr(L), b, x) / perf.norm_factor <= 1.5 * tol
+    if offset == 1:   # the same bits as the aligned solve
+        buf2 = torch.zeros(L.n, dtype=torch.float64, device="cuda")
+        p2 = cf.cuFoamCG("p", M, {"tolerance": tol, "maxIter": maxit}).solve(buf2, src, history=maxit + 1)
+        torch.cuda.synchronize()
+        assert p2.history.tobytes() == perf.history.tobytes()
+        assert buf2.cpu().numpy().tobytes() == x.tobytes()
