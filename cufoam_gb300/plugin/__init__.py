@@ -31,8 +31,17 @@ def lib():
                                        C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                        C.c_void_p, C.c_char_p, C.c_int]
+        L.mf_solve_reused_addressing.restype = C.c_int
+        L.mf_solve_reused_addressing.argtypes = [C.c_int] + list(L.mf_solve.argtypes)
+        L.cuFoamGB300_matrix_builds.restype = C.c_long
+        L.cuFoamGB300_matrix_builds.argtypes = []
         _lib = L
     return _lib
+
+
+def matrix_builds() -> int:
+    """Device matrices the plugin has built so far (its cache misses)."""
+    return int(lib().cuFoamGB300_matrix_builds())
 
 
 class FoamError(RuntimeError):
@@ -41,12 +50,15 @@ class FoamError(RuntimeError):
 
 def foam_solve(solver: str, ldu, source, psi, tolerance: float = 1e-6, rel_tol: float = 0.0,
                max_iter: int = 1000, symmetric: bool | None = None, cyclic=None,
-               processor_patch: bool = False, **controls):
+               processor_patch: bool = False, reuse_addressing: int | None = None, **controls):
     """Run the plugin `solver` on an LDU matrix through the OpenFOAM-style
     interface; psi (float64 array) is updated in place.  Returns the
     solverPerformance fields as a dict.  cyclic = (faceCellsA, faceCellsB,
     coeffsA, coeffsB) adds a cyclic patch pair (interfaceBouCoeffs coeffs);
-    processor_patch adds a processor interface."""
+    processor_patch adds a processor interface; reuse_addressing = slot
+    (0..3) builds the mesh in the memory of the previous mesh of that slot
+    (same addressing object and list buffers), as a running case keeps its
+    meshes."""
     if symmetric is None:
         symmetric = np.array_equal(ldu.lower, ldu.upper)
     d = np.ascontiguousarray(ldu.diag, np.float64)
@@ -64,7 +76,9 @@ def foam_solve(solver: str, ldu, source, psi, tolerance: float = 1e-6, rel_tol: 
     out = np.zeros(4)
     err = C.create_string_buffer(1024)
     if cyclic is None and not processor_patch:
-        rc = lib().mf_solve(solver.encode(), ldu.n, lo.shape[0], d.ctypes.data,
+        fn = lib().mf_solve if reuse_addressing is None else \
+            (lambda *a: lib().mf_solve_reused_addressing(int(reuse_addressing), *a))
+        rc = fn(solver.encode(), ldu.n, lo.shape[0], d.ctypes.data,
                             None if symmetric else lo.ctypes.data, up.ctypes.data, la.ctypes.data,
                             ua.ctypes.data, b.ctypes.data, psi.ctypes.data, tolerance, rel_tol,
                             max_iter, len(keys), ck, cv, out.ctypes.data, err, 1024)

@@ -7,7 +7,9 @@
  *              NormFactor, the solver with tolerance*normFactor, copy back,
  *              free everything.
  *   here:      the lduAddressing is uploaded once and kept on the device
- *              (cached per addressing object); each call uploads the
+ *              (an LRU cache of four meshes, keyed on the addressing's
+ *              memory, sizes and a sampled fingerprint of its contents);
+ *              each call uploads the
  *              coefficients, converts them on the device, and runs
  *              normFactor + the solver inside one device-driven loop.
  * Fixed relative to the reference: the constructor forwards
@@ -16,8 +18,10 @@
  */
 #include "cuFoamGB300.H"
 
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -25,6 +29,15 @@
 namespace Foam {
 
 namespace {
+
+// One lock for the plugin's shared state: the context (one host thread at a
+// time) and the matrix cache.  solve() holds it from the matrix lookup to
+// the end of cf_solve.
+std::mutex &gb300Mutex()
+{
+    static std::mutex m;
+    return m;
+}
 
 cf_context *gb300Context()
 {
@@ -41,33 +54,85 @@ cf_context *gb300Context()
     return ctx;
 }
 
-// One device matrix per addressing object: reused by Ux/Uy/Uz and across
-// time steps; coefficients are refreshed on every solve.
-struct MatrixCache {
-    const void *addr = nullptr;
+// FNV-1a over the sizes and a fixed sample of the owner / neighbour lists
+// (their first and last 256 entries and 4,096 evenly spaced ones): a few
+// microseconds, and a new mesh that reuses an old one's memory (same
+// pointers, same sizes, other faces) gives another value.
+uint64_t addressingFingerprint(const lduAddressing &A, label n)
+{
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](uint64_t v) {
+        for (int k = 0; k < 8; ++k) {
+            h ^= (v >> (8 * k)) & 0xffu;
+            h *= 1099511628211ull;
+        }
+    };
+    const labelList &la = A.lowerAddr(), &ua = A.upperAddr();
+    const label nf = la.size();
+    mix((uint64_t)n);
+    mix((uint64_t)nf);
+    auto sample = [&](label f) {
+        mix((uint64_t)(uint32_t)la[f]);
+        mix((uint64_t)(uint32_t)ua[f]);
+    };
+    const label edge = nf < 256 ? nf : 256;
+    for (label f = 0; f < edge; ++f) sample(f);
+    for (label f = nf - edge; f < nf; ++f) sample(f);
+    if (nf > 0)
+        for (label k = 0; k < 4096; ++k) sample((label)(((int64_t)k * nf) / 4096));
+    return h;
+}
+
+// Device matrices kept across solve() calls: reused by Ux/Uy/Uz and across
+// time steps (coefficients refreshed on every solve), a few meshes at a time
+// (multi-region cases), the least recently used dropped first.  An entry
+// matches on the addressing lists' memory, the sizes and the fingerprint,
+// so a mesh that replaced another in the same memory is rebuilt.
+struct MatrixCacheEntry {
     const void *lowerAddr = nullptr;
     const void *upperAddr = nullptr;
     label n = -1, nFaces = -1;
+    uint64_t fingerprint = 0;
+    uint64_t lastUse = 0;
     cf_matrix *m = nullptr;
 };
 
-cf_matrix *deviceMatrix(const lduMatrix &M)
+constexpr size_t kMatrixCacheEntries = 4;
+std::vector<MatrixCacheEntry> gMatrixCache;
+uint64_t gMatrixClock = 0;
+long gMatrixBuilds = 0;
+
+cf_matrix *deviceMatrix(const lduMatrix &M)   // under gb300Mutex()
 {
-    static MatrixCache cache;
     const lduAddressing &A = M.lduAddr();
     const label n = M.diag().size();
     const label nFaces = A.lowerAddr().size();
+    const uint64_t fp = addressingFingerprint(A, n);
     cf_context *ctx = gb300Context();
-    const bool same = cache.m && cache.addr == &A && cache.n == n && cache.nFaces == nFaces &&
-                      cache.lowerAddr == A.lowerAddr().cdata() &&
-                      cache.upperAddr == A.upperAddr().cdata();
+    MatrixCacheEntry *hit = nullptr, *stale = nullptr;
+    for (MatrixCacheEntry &e : gMatrixCache) {
+        const bool same_memory = e.lowerAddr == A.lowerAddr().cdata() && e.upperAddr == A.upperAddr().cdata();
+        if (same_memory && e.n == n && e.nFaces == nFaces && e.fingerprint == fp) hit = &e;
+        else if (same_memory) stale = &e;   // other faces in the same memory: rebuild
+    }
     cf_status st = CF_OK;
-    if (same) {
-        st = cf_matrix_update_values(cache.m, M.diag().cdata(), M.lower().cdata(), M.upper().cdata(),
+    if (hit) {
+        st = cf_matrix_update_values(hit->m, M.diag().cdata(), M.lower().cdata(), M.upper().cdata(),
                                      CF_MEM_HOST);
     } else {
-        if (cache.m) cf_matrix_destroy(cache.m);
-        cache = MatrixCache();
+        MatrixCacheEntry *slot = stale;
+        if (!slot && gMatrixCache.size() < kMatrixCacheEntries) {
+            gMatrixCache.reserve(kMatrixCacheEntries);
+            gMatrixCache.emplace_back();
+            slot = &gMatrixCache.back();
+        }
+        if (!slot) {
+            slot = &gMatrixCache[0];
+            for (MatrixCacheEntry &e : gMatrixCache)
+                if (e.lastUse < slot->lastUse) slot = &e;
+        }
+        if (slot->m) cf_matrix_destroy(slot->m);
+        *slot = MatrixCacheEntry();
         cf_ldu_view v;
         std::memset(&v, 0, sizeof(v));
         v.n_cells = n;
@@ -81,20 +146,23 @@ cf_matrix *deviceMatrix(const lduMatrix &M)
         v.losort_start = A.losortStartAddr().cdata();
         v.owner_start = A.ownerStartAddr().cdata();
         v.memory = CF_MEM_HOST;
-        st = cf_matrix_create_ldu(ctx, &v, &cache.m);
+        st = cf_matrix_create_ldu(ctx, &v, &slot->m);
         if (st == CF_OK) {
-            cache.addr = &A;
-            cache.lowerAddr = A.lowerAddr().cdata();
-            cache.upperAddr = A.upperAddr().cdata();
-            cache.n = n;
-            cache.nFaces = nFaces;
+            slot->lowerAddr = A.lowerAddr().cdata();
+            slot->upperAddr = A.upperAddr().cdata();
+            slot->n = n;
+            slot->nFaces = nFaces;
+            slot->fingerprint = fp;
+            ++gMatrixBuilds;
+            hit = slot;
         }
     }
     if (st != CF_OK) {
         FatalErrorInFunction << "cuFoamGB300: cannot load the matrix: " << cf_status_string(st)
                              << ": " << cf_context_last_error(ctx) << exit(FatalError);
     }
-    return cache.m;
+    hit->lastUse = ++gMatrixClock;
+    return hit->m;
 }
 
 } // namespace
@@ -218,6 +286,7 @@ cf_matrix *cuFoamGB300Solver::coupledMatrix() const
 solverPerformance cuFoamGB300Solver::solve(scalarField &psi, const scalarField &source,
                                            const direction) const
 {
+    std::lock_guard<std::mutex> lock(gb300Mutex());
     cf_matrix *coupled = coupledMatrix();
     cf_matrix *m = coupled ? coupled : deviceMatrix(matrix());
     const cf_controls c = gb300Controls();
@@ -275,3 +344,11 @@ CUFOAM_GB300_DEFINE_SOLVER(cuFoamRichardson, CF_RICHARDSON)
 CUFOAM_GB300_DEFINE_SOLVER(cuFoamPCG, CF_PCG)
 
 } // namespace Foam
+
+// Device matrices the plugin has built since the library was loaded (a
+// diagnostic for tests of the matrix cache).
+extern "C" long cuFoamGB300_matrix_builds()
+{
+    std::lock_guard<std::mutex> lock(Foam::gb300Mutex());
+    return Foam::gMatrixBuilds;
+}

@@ -219,6 +219,16 @@ public:
     {
         calcAddressing();
     }
+    // New faces in the same memory (the stand-in's way to model a mesh that
+    // reuses an old one's storage: same object, same list buffers when the
+    // sizes match, other contents).
+    void reset(label nCells, const labelList &lowerAddr, const labelList &upperAddr)
+    {
+        size_ = nCells;
+        lower_.assign(lowerAddr.begin(), lowerAddr.end());
+        upper_.assign(upperAddr.begin(), upperAddr.end());
+        calcAddressing();
+    }
     label size() const { return size_; }
     const labelList &lowerAddr() const { return lower_; }
     const labelList &upperAddr() const { return upper_; }

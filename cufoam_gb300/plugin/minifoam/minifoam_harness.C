@@ -8,6 +8,7 @@
 #include "lduMatrix.H"
 
 #include <cstring>
+#include <memory>
 #include <exception>
 
 namespace Foam {
@@ -25,15 +26,29 @@ struct Coupling {
     bool processor = false;
 };
 
+// addressing objects (four slots) whose lists keep their memory between
+// calls, like the meshes of a running case
+Foam::lduAddressing *reusedAddressing(int slot, int n, const Foam::labelList &la, const Foam::labelList &ua)
+{
+    static Foam::lduAddressing *a[4] = {nullptr, nullptr, nullptr, nullptr};
+    Foam::lduAddressing *&p = a[slot & 3];
+    if (!p) p = new Foam::lduAddressing(n, la, ua);
+    else p->reset(n, la, ua);
+    return p;
+}
+
 int run(const char *solver_name, int n, int n_faces, const double *diag, const double *lower,
         const double *upper, const int *lower_addr, const int *upper_addr, const double *source,
         double *psi, double tolerance, double rel_tol, int max_iter, int n_extra, const char *const *keys,
-        const char *const *values, const Coupling &cpl, double *out, char *err, int err_len)
+        const char *const *values, const Coupling &cpl, double *out, char *err, int err_len,
+        int reuse_slot = -1)
 {
     try {
         using namespace Foam;
         labelList la(lower_addr, lower_addr + n_faces), ua(upper_addr, upper_addr + n_faces);
-        lduAddressing addr(n, la, ua);
+        std::unique_ptr<lduAddressing> own;
+        if (reuse_slot < 0) own.reset(new lduAddressing(n, la, ua));
+        const lduAddressing &addr = reuse_slot >= 0 ? *reusedAddressing(reuse_slot, n, la, ua) : *own;
         scalarField d(diag, diag + n), up(upper, upper + n_faces);
         scalarField lo;
         if (lower) lo.assign(lower, lower + n_faces);
@@ -116,6 +131,20 @@ int mf_solve(const char *solver_name, int n, int n_faces, const double *diag, co
 {
     return run(solver_name, n, n_faces, diag, lower, upper, lower_addr, upper_addr, source, psi, tolerance,
                rel_tol, max_iter, n_extra, keys, values, Coupling(), out, err, err_len);
+}
+
+/* mf_solve on the lduAddressing object of `slot` (0..3), kept between
+ * calls with its lists overwritten in place: the same mesh across calls, or
+ * a new mesh in an old mesh's memory (same addresses, and the same sizes
+ * when the meshes match). */
+int mf_solve_reused_addressing(int slot, const char *solver_name, int n, int n_faces, const double *diag,
+                               const double *lower, const double *upper, const int *lower_addr,
+                               const int *upper_addr, const double *source, double *psi, double tolerance,
+                               double rel_tol, int max_iter, int n_extra, const char *const *keys,
+                               const char *const *values, double *out, char *err, int err_len)
+{
+    return run(solver_name, n, n_faces, diag, lower, upper, lower_addr, upper_addr, source, psi, tolerance,
+               rel_tol, max_iter, n_extra, keys, values, Coupling(), out, err, err_len, slot);
 }
 
 /* The same with a cyclic patch pair: face f of patch A (cell fcA[f])

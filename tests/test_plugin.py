@@ -74,3 +74,36 @@ def test_plugin_controls_precision_and_reltol():
                     useRelTol="true")
     assert p2["nIterations"] < p1["nIterations"]
     assert p2["finalResidual"] <= 1e-2 * p2["initialResidual"] and p2["converged"]
+
+
+@pytest.mark.gpu
+def test_plugin_matrix_cache_is_keyed_on_the_mesh_not_its_memory():
+    """A new mesh built in the memory of an old one (same addressing object,
+    same list buffers, same sizes, other faces) must not reuse the old
+    device matrix; two meshes solved in turn (a multi-region case) both stay
+    cached."""
+    from cufoam_gb300.plugin import matrix_builds
+    LA = O.grid_lognormal(12, 10, 8, 3)
+    LB = O.permute_ldu(LA, O.permutation(7, LA.n))       # same sizes, other faces
+    assert LB.lower_addr.shape == LA.lower_addr.shape
+    assert not (np.array_equal(LB.lower_addr, LA.lower_addr) and np.array_equal(LB.upper_addr, LA.upper_addr))
+    b = O.uniform(3, LA.n)
+    for name, L in (("A", LA), ("B", LB), ("A again", LA)):
+        psi = np.zeros(L.n)
+        p = foam_solve("cuFoamCG", L, b, psi, tolerance=1e-10, max_iter=5000, reuse_addressing=0,
+                       reduction="reference")
+        want = O.plugin_solve(O.CG, L, b, np.zeros(L.n), 1e-10, 5000)
+        assert p["nIterations"] == want.n_iterations, name
+        assert psi.tobytes() == want.psi.tobytes(), name
+    # two meshes in turn, each kept in its own memory: after the first solve
+    # of each, no further device matrix is built
+    LC = O.grid_lognormal(9, 8, 7, 4)
+    bc = O.uniform(2, LC.n)
+    foam_solve("cuFoamCG", LA, b, np.zeros(LA.n), tolerance=1e-8, max_iter=5000, reuse_addressing=1)
+    foam_solve("cuFoamCG", LC, bc, np.zeros(LC.n), tolerance=1e-8, max_iter=5000, reuse_addressing=2)
+    before = matrix_builds()
+    for _ in range(3):
+        pa = foam_solve("cuFoamCG", LA, b, np.zeros(LA.n), tolerance=1e-8, max_iter=5000, reuse_addressing=1)
+        pc = foam_solve("cuFoamCG", LC, bc, np.zeros(LC.n), tolerance=1e-8, max_iter=5000, reuse_addressing=2)
+        assert pa["converged"] and pc["converged"]
+    assert matrix_builds() == before
