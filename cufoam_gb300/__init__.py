@@ -421,10 +421,16 @@ class LduSolver:
     symmetric_table = True
     asymmetric_table = True
 
-    def __init__(self, field_name: str, matrix: LduMatrix, controls: dict | None = None):
+    def __init__(self, field_name: str, matrix: LduMatrix, controls: dict | None = None,
+                 interfaces=None):
+        """`interfaces` (a decomposed.ProcessorInterfaces): this matrix is
+        one subdomain of a decomposed case, coupled to the others through
+        processor patches as OpenFOAM's interfaceBouCoeffs + interfaces
+        constructor arguments describe them (cf_solve_decomposed)."""
         self.field_name = field_name
         self.matrix = matrix
         self.controls = dict(controls or {})
+        self.interfaces = interfaces
 
     def _controls(self, memory: int, history_capacity: int):
         c = _capi.cf_controls()
@@ -474,8 +480,17 @@ class LduSolver:
         if mx == _capi.CF_MEM_DEVICE:
             import torch
             self.matrix.ctx.set_stream(torch.cuda.current_stream(kx.device))
-        st = self.matrix._lib.cf_solve(self.matrix.handle, self.kind, C.byref(c), pb, px,
-                                       C.byref(perf))
+        if self.interfaces is None:
+            st = self.matrix._lib.cf_solve(self.matrix.handle, self.kind, C.byref(c), pb, px,
+                                           C.byref(perf))
+        else:
+            ci, cc = self.interfaces.as_c()
+            comm = self.interfaces.comm
+            comm.error = None
+            st = self.matrix._lib.cf_solve_decomposed(self.matrix.handle, self.kind, C.byref(c),
+                                                      C.byref(ci), C.byref(cc), pb, px, C.byref(perf))
+            if comm.error is not None:
+                raise comm.error
         self.matrix.ctx.check(st, f"{self.type_name}::solve")
         h = hist[:perf.history_length].copy() if hist is not None else None
         return SolverPerformance(

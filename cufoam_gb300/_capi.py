@@ -55,6 +55,20 @@ class cf_perf(C.Structure):
                 ("reserved", C.c_int32 * 6)]
 
 
+# decomposed solves: the caller's exchange / all-reduce (cf_comm)
+EXCHANGE_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                          C.c_int32)
+ALLREDUCE_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.POINTER(C.c_double), C.c_int32)
+
+
+class cf_comm(C.Structure):
+    _fields_ = [("user", C.c_void_p), ("exchange", EXCHANGE_FN), ("allreduce_sum", ALLREDUCE_FN)]
+
+
+class cf_interfaces(C.Structure):
+    _fields_ = [("n_faces", C.c_int32), ("face_cells", C.c_void_p), ("coeffs", C.c_void_p)]
+
+
 class cf_device_info(C.Structure):
     _fields_ = [("device", C.c_int32), ("sm_count", C.c_int32),
                 ("cc_major", C.c_int32), ("cc_minor", C.c_int32),
@@ -128,6 +142,9 @@ def load(build_if_missing: bool = True):
                                        C.POINTER(C.c_double)]),
         "cf_solve": (C.c_int32, [P, C.c_int32, C.POINTER(cf_controls), P, P,
                                  C.POINTER(cf_perf)]),
+        "cf_solve_decomposed": (C.c_int32, [P, C.c_int32, C.POINTER(cf_controls),
+                                            C.POINTER(cf_interfaces), C.POINTER(cf_comm), P, P,
+                                            C.POINTER(cf_perf)]),
         "cf_adjoint_gradients": (C.c_int32, [P, P, P, P, P, P, C.c_int32]),
         "cf_norm_factor_noalloc": (C.c_int32, [C.c_int32, P, P, P, P, P, C.c_int32, P, P]),
     }

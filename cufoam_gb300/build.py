@@ -17,7 +17,7 @@ LIB_NAME = "libcufoam_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
 SOURCES = ["capi.cu", "matrix.cu", "solve_fp64.cu", "solve_fast.cu", "mixed.cu", "adjoint.cu", "batched.cu",
-           "noalloc.cu", "formats.cpp"]
+           "noalloc.cu", "distributed.cu", "formats.cpp"]
 HEADERS = ["internal.h", "device.cuh", "solver_common.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -52,6 +52,7 @@ def build_plugin(force: bool = False) -> str:
     srcs = [os.path.join(PLUGIN_DIR, "cuFoamGB300.C"),
             os.path.join(PLUGIN_DIR, "minifoam", "minifoam_harness.C")]
     deps = srcs + [os.path.join(PLUGIN_DIR, "cuFoamGB300.H"),
+                   os.path.join(PLUGIN_DIR, "cuFoamGB300Comm.H"),
                    os.path.join(PLUGIN_DIR, "minifoam", "lduMatrix.H"),
                    os.path.join(INCLUDE, "cufoam_gb300.h"), LIB_PATH]
     if force or not os.path.exists(PLUGIN_LIB) or os.path.getmtime(PLUGIN_LIB) < _newest(deps):

@@ -578,6 +578,21 @@ cf_status cf_solve(cf_matrix *m, int32_t solver, const cf_controls *controls, co
     return st;
 }
 
+cf_status cf_solve_decomposed(cf_matrix *m, int32_t solver, const cf_controls *controls,
+                              const cf_interfaces *interfaces, const cf_comm *comm, const double *source,
+                              double *psi, cf_perf *perf)
+{
+    if (!m || !source || !psi || !interfaces || !comm) return CF_BAD_INPUT;
+    cf_controls c;
+    if (controls) c = *controls;
+    else cf_controls_init(&c);
+    cf_status st = guarded(m->owner, [&] {
+        cf::solve_distributed(m->impl, solver, c, *interfaces, *comm, source, psi, perf);
+    });
+    if (st != CF_OK && perf) perf->status = st;
+    return st;
+}
+
 cf_status cf_adjoint_gradients(cf_matrix *m, const double *lambda, const double *x,
                                double *d_diag, double *d_lower, double *d_upper, int32_t memory)
 {

@@ -282,6 +282,9 @@ void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order)
 double norm_factor(Matrix *m, const double *b, const double *x, int norm_type, bool ref_order);
 void solve(Matrix *m, int solver, const cf_controls &c, const double *b, double *x,
            cf_perf *perf);
+// CG on one subdomain of a decomposed case (distributed.cu)
+void solve_distributed(Matrix *m, int solver, const cf_controls &c, const cf_interfaces &ifc,
+                       const cf_comm &comm, const double *b, double *x, cf_perf *perf);
 
 // CG on one small system in a single cluster-persistent launch (batched.cu)
 struct SmallSolveResult {

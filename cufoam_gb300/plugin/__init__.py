@@ -1,6 +1,8 @@
 """Access to the C++ plugin layer (cuFoamGB300.{H,C}) compiled against the
 minifoam stand-in: ``foam_solve`` runs a plugin exactly as OpenFOAM would
-(lduMatrix::solver::New by name, then solve(psi, source, cmpt))."""
+(lduMatrix::solver::New by name, then solve(psi, source, cmpt));
+``foam_solve_decomposed`` runs it on one subdomain of a parallel run, the
+stand-in's Pstream carried by ``torch.distributed`` (``ParallelRun``)."""
 from __future__ import annotations
 
 import ctypes as C
@@ -35,6 +37,15 @@ def lib():
         L.mf_solve_reused_addressing.argtypes = [C.c_int] + list(L.mf_solve.argtypes)
         L.cuFoamGB300_matrix_builds.restype = C.c_long
         L.cuFoamGB300_matrix_builds.argtypes = []
+        L.mf_set_transport.restype = None
+        L.mf_set_transport.argtypes = [C.c_void_p]
+        L.mf_solve_decomposed.restype = C.c_int
+        L.mf_solve_decomposed.argtypes = list(L.mf_solve.argtypes[:16]) + \
+            [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int]
+        L.mf_processor_comm_check.restype = C.c_int
+        L.mf_processor_comm_check.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                              C.c_char_p, C.c_int]
         _lib = L
     return _lib
 
@@ -98,3 +109,131 @@ def foam_solve(solver: str, ldu, source, psi, tolerance: float = 1e-6, rel_tol: 
         raise FoamError(err.value.decode())
     return {"initialResidual": out[0], "finalResidual": out[1], "nIterations": int(out[2]),
             "converged": bool(out[3])}
+
+
+# ---------------------------------------------------------------------------
+# parallel runs: minifoam's Pstream over torch.distributed
+# ---------------------------------------------------------------------------
+_COMPLETE_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                           C.POINTER(C.c_int32), C.POINTER(C.c_void_p), C.POINTER(C.c_int64))
+_ALLREDUCE_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.POINTER(C.c_double), C.c_int32)
+
+
+class _Transport(C.Structure):
+    _fields_ = [("myProcNo", C.c_int32), ("nProcs", C.c_int32), ("user", C.c_void_p),
+                ("complete", _COMPLETE_FN), ("allreduceSum", _ALLREDUCE_FN)]
+
+
+class ParallelRun:
+    """A parallel run of the stand-in, carried by this process's
+    torch.distributed group (gloo): the plugin's non-blocking processor
+    transfers become isend / irecv with their tags, its reductions an
+    all-gather summed in rank order (the same bits on every rank, as a
+    parallel solver needs).  Use as a context manager around the solves."""
+
+    def __init__(self, group=None):
+        import torch.distributed as dist
+        self.dist = dist
+        self.group = group
+        self.error: BaseException | None = None
+        self._complete = _COMPLETE_FN(self._on_complete)
+        self._reduce = _ALLREDUCE_FN(self._on_reduce)
+        self._t = _Transport(dist.get_rank(group), dist.get_world_size(group), None,
+                             self._complete, self._reduce)
+
+    def _on_complete(self, _user, n, kind, peer, tag, data, nbytes):
+        import torch
+        try:
+            reqs, keep = [], []
+            for i in range(n):
+                if nbytes[i] % 8:
+                    raise ValueError("transfers of doubles only")
+                buf = np.ctypeslib.as_array(C.cast(data[i], C.POINTER(C.c_double)), shape=(nbytes[i] // 8,)) \
+                    if nbytes[i] else np.zeros(0)
+                t = torch.from_numpy(buf)
+                keep.append(t)
+                op = self.dist.isend if kind[i] == 0 else self.dist.irecv
+                dst = peer[i] if self.group is None else self.dist.get_global_rank(self.group, peer[i])
+                reqs.append(op(t, dst, group=self.group, tag=int(tag[i])))
+            for r in reqs:
+                r.wait()
+            return 0
+        except BaseException as e:  # noqa: BLE001 -- reported through the status
+            self.error = e
+            return 1
+
+    def _on_reduce(self, _user, values, count):
+        from ..decomposed import ordered_allreduce_sum
+        try:
+            ordered_allreduce_sum(np.ctypeslib.as_array(values, shape=(count,)), self.group)
+            return 0
+        except BaseException as e:  # noqa: BLE001
+            self.error = e
+            return 1
+
+    def __enter__(self):
+        lib().mf_set_transport(C.addressof(self._t))
+        return self
+
+    def __exit__(self, *exc):
+        lib().mf_set_transport(None)
+        return False
+
+
+def _proc_arrays(sub):
+    neighbours = np.array([p.neighbour for p in sub.patches], np.int32)
+    sizes = np.array([len(p.face_cells) for p in sub.patches], np.int32)
+    cells, coeffs = sub.interface_arrays()
+    return neighbours, sizes, np.ascontiguousarray(cells, np.int32), np.ascontiguousarray(coeffs, np.float64)
+
+
+def foam_solve_decomposed(solver: str, sub, source, psi, tolerance: float = 1e-6, rel_tol: float = 0.0,
+                          max_iter: int = 1000, symmetric: bool | None = None, **controls):
+    """Run the plugin `solver` on subdomain `sub` (a decomposed.Subdomain)
+    of a parallel run (inside ``with ParallelRun():``), its processor
+    patches given to the solver as OpenFOAM's processor interfaces; psi
+    (this rank's cells) is updated in place.  Returns the solverPerformance
+    fields as a dict."""
+    if symmetric is None:
+        symmetric = np.array_equal(sub.lower, sub.upper)
+    d = np.ascontiguousarray(sub.diag, np.float64)
+    lo = np.ascontiguousarray(sub.lower, np.float64)
+    up = np.ascontiguousarray(sub.upper, np.float64)
+    la = np.ascontiguousarray(sub.lower_addr, np.int32)
+    ua = np.ascontiguousarray(sub.upper_addr, np.int32)
+    b = np.ascontiguousarray(source, np.float64)
+    if psi.dtype != np.float64 or not psi.flags["C_CONTIGUOUS"]:
+        raise TypeError("psi must be a contiguous float64 array")
+    nb, sz, fc, co = _proc_arrays(sub)
+    keys = [k.encode() for k in controls]
+    vals = [str(v).encode() for v in controls.values()]
+    ck = (C.c_char_p * max(1, len(keys)))(*keys)
+    cv = (C.c_char_p * max(1, len(vals)))(*vals)
+    out = np.zeros(4)
+    err = C.create_string_buffer(1024)
+    rc = lib().mf_solve_decomposed(solver.encode(), sub.n, lo.shape[0], d.ctypes.data,
+                                   None if symmetric else lo.ctypes.data, up.ctypes.data, la.ctypes.data,
+                                   ua.ctypes.data, b.ctypes.data, psi.ctypes.data, tolerance, rel_tol,
+                                   max_iter, len(keys), ck, cv, len(nb), nb.ctypes.data, sz.ctypes.data,
+                                   fc.ctypes.data, co.ctypes.data, out.ctypes.data, err, 1024)
+    if rc != 0:
+        raise FoamError(err.value.decode())
+    return {"initialResidual": out[0], "finalResidual": out[1], "nIterations": int(out[2]),
+            "converged": bool(out[3])}
+
+
+def processor_comm_check(sub, send, values):
+    """Drive the plugin's processor-patch callbacks (cuFoamGB300Comm.H)
+    once without a solve, inside ``with ParallelRun():``: returns (status,
+    recv, values) after one exchange of `send` and one sum of `values`."""
+    nb, sz, fc, co = _proc_arrays(sub)
+    s = np.ascontiguousarray(send, np.float64)
+    r = np.zeros(max(1, len(s)))
+    v = np.ascontiguousarray(values, np.float64).copy()
+    err = C.create_string_buffer(1024)
+    rc = lib().mf_processor_comm_check(len(nb), nb.ctypes.data, sz.ctypes.data, fc.ctypes.data,
+                                       co.ctypes.data, s.ctypes.data if len(s) else r.ctypes.data,
+                                       r.ctypes.data, len(s), v.ctypes.data, len(v), err, 1024)
+    if rc < 0:
+        raise FoamError(err.value.decode())
+    return rc, r[:len(s)], v

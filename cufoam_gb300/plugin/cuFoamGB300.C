@@ -15,8 +15,12 @@
  * Fixed relative to the reference: the constructor forwards
  * interfaceBouCoeffs (the reference passes interfaceIntCoeffs twice,
  * cuFoamCG/cuFoamCG.C:30-31).
+ * In a parallel run each rank solves its subdomain through
+ * cf_solve_decomposed, the processor patches exchanged by OpenFOAM's own
+ * Pstream (cuFoamGB300Comm.H); the reference solves each subdomain alone.
  */
 #include "cuFoamGB300.H"
+#include "cuFoamGB300Comm.H"
 
 #include <cstdint>
 #include <cstdlib>
@@ -215,10 +219,11 @@ cf_matrix *cuFoamGB300Solver::coupledMatrix() const
     for (label patchi = 0; patchi < ifs.size(); ++patchi) {
         if (!ifs.set(patchi)) continue;
         const lduInterface &ifc = ifs[patchi].interface();
+        if (isA<processorLduInterface>(ifc)) continue;   // solve(): the decomposed path
         if (!isA<cyclicLduInterface>(ifc)) {
             FatalErrorInFunction << type() << ": patch " << patchi
-                                 << " is a coupled interface other than cyclic (e.g. a processor "
-                                    "patch); only cyclic interfaces are solved on one GPU"
+                                 << " is a coupled interface other than cyclic or processor; "
+                                    "only those two are solved on the GPU"
                                  << exit(FatalError);
         }
         const cyclicLduInterface &cyc = refCast<const cyclicLduInterface>(ifc);
@@ -287,12 +292,28 @@ solverPerformance cuFoamGB300Solver::solve(scalarField &psi, const scalarField &
                                            const direction) const
 {
     std::lock_guard<std::mutex> lock(gb300Mutex());
+    // processor patches: this matrix is one subdomain of a decomposed case
+    const cuFoamGB300ProcessorComm procs(interfaces(), interfaceBouCoeffs());
+    const bool decomposed = Pstream::parRun();
+    if (!decomposed && procs.nPatches() > 0) {
+        FatalErrorInFunction << type() << ": processor patches outside a parallel run"
+                             << exit(FatalError);
+    }
     cf_matrix *coupled = coupledMatrix();
     cf_matrix *m = coupled ? coupled : deviceMatrix(matrix());
     const cf_controls c = gb300Controls();
     cf_perf perf;
     std::memset(&perf, 0, sizeof(perf));
-    const cf_status st = cf_solve(m, kind_, &c, source.cdata(), psi.data(), &perf);
+    cf_status st;
+    if (decomposed) {
+        // every rank takes part, with or without processor faces: the
+        // normFactor and the inner products are sums over all ranks
+        const cf_interfaces ifc = procs.interfaces();
+        const cf_comm comm = procs.comm();
+        st = cf_solve_decomposed(m, kind_, &c, &ifc, &comm, source.cdata(), psi.data(), &perf);
+    } else {
+        st = cf_solve(m, kind_, &c, source.cdata(), psi.data(), &perf);
+    }
     if (coupled) cf_matrix_destroy(coupled);
     if (st != CF_OK) {
         FatalErrorInFunction << type() << ": solve failed: " << cf_status_string(st) << ": "

@@ -20,9 +20,12 @@
  * Coupled interfaces: cyclic patches are folded into the device matrix
  * (OpenFOAM's interface update, result -= interfaceBouCoeffs * psi of the
  * neighbour patch's face cells, becomes the CSR entries (faceCell,
- * neighbour faceCell) = -coeff appended to each row); processor patches
- * couple to other ranks and are rejected.  The reference ignores all
- * interfaces.
+ * neighbour faceCell) = -coeff appended to each row).  In a parallel run
+ * (Pstream::parRun()) the processor patches couple each rank's subdomain
+ * to its neighbours: CG solves the decomposed system
+ * (cf_solve_decomposed, transfers through OpenFOAM's Pstream,
+ * cuFoamGB300Comm.H); the other solvers stop with a FatalError there.
+ * The reference ignores all interfaces.
  *
  * Residuals in the returned solverPerformance are normalised by normFactor
  * (OpenFOAM's convention); the stopping test is the reference's

@@ -45,6 +45,101 @@ public:
 
 typedef List<label> labelList;
 
+// a view of contiguous storage (OpenFOAM's UList; List is one here only
+// by conversion)
+template <class T>
+class UList {
+    T *v_;
+    label size_;
+
+public:
+    UList(T *v, label size) : v_(v), size_(size) {}
+    label size() const { return size_; }
+    T *data() { return v_; }
+    const T *cdata() const { return v_; }
+    T &operator[](label i) { return v_[i]; }
+    const T &operator[](label i) const { return v_[i]; }
+};
+
+// ---- the parallel run (OpenFOAM's UPstream / Pstream) ---------------------
+// The stand-in moves no data itself: a harness that emulates a parallel run
+// installs a transport, which completes the posted non-blocking sends and
+// receives together (waitRequests) and sums reductions over the ranks.
+// Without a transport the run is serial (parRun() false).
+struct mfTransport {
+    int32_t myProcNo, nProcs;
+    void *user;
+    // kind[i]: 0 send, 1 receive; the rest as MPI_Isend / MPI_Irecv
+    int32_t (*complete)(void *user, int32_t n, const int32_t *kind, const int32_t *peer,
+                        const int32_t *tag, void *const *data, const int64_t *bytes);
+    int32_t (*allreduceSum)(void *user, double *values, int32_t count);
+};
+
+class UPstream {
+public:
+    enum class commsTypes { blocking, scheduled, nonBlocking };
+
+    struct Request {
+        int32_t kind, peer, tag;
+        void *data;
+        int64_t bytes;
+    };
+
+    static const mfTransport *&transport()
+    {
+        static const mfTransport *t = nullptr;
+        return t;
+    }
+    static std::vector<Request> &requests()
+    {
+        static std::vector<Request> r;
+        return r;
+    }
+    static bool parRun() { return transport() != nullptr; }
+    static int myProcNo() { return parRun() ? transport()->myProcNo : 0; }
+    static int nProcs() { return parRun() ? transport()->nProcs : 1; }
+    static void post(int32_t kind, int32_t peer, int32_t tag, void *data, int64_t bytes)
+    {
+        if (!parRun()) throw std::runtime_error("Pstream: communication in a serial run");
+        requests().push_back(Request{kind, peer, tag, data, bytes});
+    }
+    static void waitRequests()
+    {
+        std::vector<Request> &r = requests();
+        if (r.empty()) return;
+        std::vector<int32_t> kind, peer, tag;
+        std::vector<void *> data;
+        std::vector<int64_t> bytes;
+        for (const Request &q : r) {
+            kind.push_back(q.kind);
+            peer.push_back(q.peer);
+            tag.push_back(q.tag);
+            data.push_back(q.data);
+            bytes.push_back(q.bytes);
+        }
+        r.clear();
+        const mfTransport *t = transport();
+        if (t->complete(t->user, (int32_t)kind.size(), kind.data(), peer.data(), tag.data(), data.data(),
+                        bytes.data()) != 0)
+            throw std::runtime_error("Pstream: a transfer failed");
+    }
+};
+
+class Pstream : public UPstream {};
+
+template <class T>
+struct sumOp {
+    T operator()(const T &a, const T &b) const { return a + b; }
+};
+
+// reduce(value, sumOp<scalar>()): the sum over all ranks, on every rank
+inline void reduce(double &v, const sumOp<double> &)
+{
+    if (!UPstream::parRun()) return;
+    const mfTransport *t = UPstream::transport();
+    if (t->allreduceSum(t->user, &v, 1) != 0) throw std::runtime_error("Pstream: a reduction failed");
+}
+
 template <class T>
 class Field : public List<T> {
 public:
@@ -76,13 +171,36 @@ public:
     const cyclicLduInterface &neighbPatch() const { return *nbr_; }
 };
 
-// a processor patch couples to cells of another MPI rank
+// a processor patch couples to cells of another MPI rank; its faces are
+// listed alike on both sides.  send / receive as OpenFOAM's
+// processorLduInterface (non-blocking only in the stand-in: completed by
+// UPstream::waitRequests()).
 class processorLduInterface : public lduInterface {
     labelList faceCells_;
+    int neighbProcNo_;
+    int tag_;
 
 public:
-    explicit processorLduInterface(const labelList &faceCells) : faceCells_(faceCells) {}
+    explicit processorLduInterface(const labelList &faceCells, int neighbProcNo = -1, int tag = 1)
+        : faceCells_(faceCells), neighbProcNo_(neighbProcNo), tag_(tag) {}
     const labelList &faceCells() const override { return faceCells_; }
+    int myProcNo() const { return UPstream::myProcNo(); }
+    int neighbProcNo() const { return neighbProcNo_; }
+    int tag() const { return tag_; }
+    template <class Type>
+    void send(const UPstream::commsTypes commsType, const UList<Type> &f) const
+    {
+        if (commsType != UPstream::commsTypes::nonBlocking)
+            throw std::runtime_error("processorLduInterface: only non-blocking transfers in the stand-in");
+        UPstream::post(0, neighbProcNo_, tag_, const_cast<Type *>(f.cdata()), (int64_t)sizeof(Type) * f.size());
+    }
+    template <class Type>
+    void receive(const UPstream::commsTypes commsType, UList<Type> &f) const
+    {
+        if (commsType != UPstream::commsTypes::nonBlocking)
+            throw std::runtime_error("processorLduInterface: only non-blocking transfers in the stand-in");
+        UPstream::post(1, neighbProcNo_, tag_, f.data(), (int64_t)sizeof(Type) * f.size());
+    }
 };
 
 class lduInterfaceField {

@@ -6,6 +6,7 @@
  * a C function so the tests can exercise the plugin layer end to end.
  */
 #include "lduMatrix.H"
+#include "../cuFoamGB300Comm.H"
 
 #include <cstring>
 #include <memory>
@@ -18,12 +19,41 @@ FatalErrorType FatalError;
 namespace {
 
 // One cyclic patch pair (faces of patch A coupled to patch B, and back),
-// an optional processor patch; n_cyc = 0: no interfaces.
+// an optional processor patch; n_cyc = 0: no interfaces.  Processor
+// patches of a decomposed case: n_proc patches, patch p to rank
+// proc_neighbour[p] with proc_size[p] faces; their face cells and
+// interfaceBouCoeffs patch after patch.
 struct Coupling {
     int n_cyc = 0;
     const int *fcA = nullptr, *fcB = nullptr;
     const double *coeffA = nullptr, *coeffB = nullptr;
     bool processor = false;
+    int n_proc = 0;
+    const int *proc_neighbour = nullptr, *proc_size = nullptr, *proc_cells = nullptr;
+    const double *proc_coeffs = nullptr;
+};
+
+// the processor interfaces of `cpl` appended to an interface list
+struct ProcessorPatches {
+    std::vector<std::unique_ptr<Foam::processorLduInterface>> patches;
+    std::vector<std::unique_ptr<Foam::lduInterfaceField>> fields;
+
+    void add(const Coupling &cpl, Foam::FieldField<Foam::Field, Foam::scalar> &bou,
+             Foam::FieldField<Foam::Field, Foam::scalar> &intc, Foam::lduInterfaceFieldPtrsList &interfaces)
+    {
+        using namespace Foam;
+        int o = 0;
+        for (int p = 0; p < cpl.n_proc; ++p) {
+            const int m = cpl.proc_size[p];
+            patches.emplace_back(new processorLduInterface(labelList(cpl.proc_cells + o, cpl.proc_cells + o + m),
+                                                           cpl.proc_neighbour[p]));
+            fields.emplace_back(new lduInterfaceField(*patches.back()));
+            interfaces.push_back(fields.back().get());
+            bou.push_back(scalarField(cpl.proc_coeffs + o, cpl.proc_coeffs + o + m));
+            intc.push_back(scalarField(cpl.proc_coeffs + o, cpl.proc_coeffs + o + m));
+            o += m;
+        }
+    }
 };
 
 // addressing objects (four slots) whose lists keep their memory between
@@ -88,6 +118,8 @@ int run(const char *solver_name, int n, int n_faces, const double *diag, const d
             intc.push_back(scalarField(cpl.coeffA, cpl.coeffA + cpl.n_cyc));
             intc.push_back(scalarField(cpl.coeffB, cpl.coeffB + cpl.n_cyc));
         }
+        ProcessorPatches procs;
+        procs.add(cpl, bou, intc, interfaces);
         if (cpl.processor) {
             proc.reset(new processorLduInterface(labelList(1, 0)));
             fields.emplace_back(new lduInterfaceField(*proc));
@@ -166,6 +198,75 @@ int mf_solve_coupled(const char *solver_name, int n, int n_faces, const double *
     c.processor = processor != 0;
     return run(solver_name, n, n_faces, diag, lower, upper, lower_addr, upper_addr, source, psi, tolerance,
                rel_tol, max_iter, n_extra, keys, values, c, out, err, err_len);
+}
+
+/* The parallel run's transport (minifoam's Pstream): NULL ends the
+ * parallel run.  The structure must stay valid while it is installed. */
+void mf_set_transport(const Foam::mfTransport *t)
+{
+    Foam::UPstream::transport() = t;
+    Foam::UPstream::requests().clear();
+}
+
+/* mf_solve on one subdomain of a decomposed case (a parallel run: install
+ * the transport first), with n_proc processor patches (see Coupling). */
+int mf_solve_decomposed(const char *solver_name, int n, int n_faces, const double *diag, const double *lower,
+                        const double *upper, const int *lower_addr, const int *upper_addr,
+                        const double *source, double *psi, double tolerance, double rel_tol, int max_iter,
+                        int n_extra, const char *const *keys, const char *const *values, int n_proc,
+                        const int *proc_neighbour, const int *proc_size, const int *proc_cells,
+                        const double *proc_coeffs, double *out, char *err, int err_len)
+{
+    Coupling c;
+    c.n_proc = n_proc;
+    c.proc_neighbour = proc_neighbour;
+    c.proc_size = proc_size;
+    c.proc_cells = proc_cells;
+    c.proc_coeffs = proc_coeffs;
+    return run(solver_name, n, n_faces, diag, lower, upper, lower_addr, upper_addr, source, psi, tolerance,
+               rel_tol, max_iter, n_extra, keys, values, c, out, err, err_len);
+}
+
+/* The plugin's processor-patch callbacks (cuFoamGB300Comm.H) without a
+ * solve: the interfaces of n_proc patches as in mf_solve_decomposed, one
+ * exchange of send[] (the values of the face cells, patch after patch)
+ * into recv[], then a sum over the ranks of values[0..n_values).  Returns
+ * 0, 1 when a callback failed, -1 on a FatalError (text in err). */
+int mf_processor_comm_check(int n_proc, const int *proc_neighbour, const int *proc_size, const int *proc_cells,
+                            const double *proc_coeffs, const double *send, double *recv, int count,
+                            double *values, int n_values, char *err, int err_len)
+{
+    try {
+        using namespace Foam;
+        Coupling c;
+        c.n_proc = n_proc;
+        c.proc_neighbour = proc_neighbour;
+        c.proc_size = proc_size;
+        c.proc_cells = proc_cells;
+        c.proc_coeffs = proc_coeffs;
+        FieldField<Field, scalar> bou, intc;
+        lduInterfaceFieldPtrsList interfaces;
+        bou.resize(1);
+        intc.resize(1);
+        interfaces.push_back(nullptr);
+        ProcessorPatches procs;
+        procs.add(c, bou, intc, interfaces);
+        const cuFoamGB300ProcessorComm comm(interfaces, bou);
+        const cf_interfaces ifc = comm.interfaces();
+        const cf_comm cc = comm.comm();
+        for (int f = 0; f < ifc.n_faces; ++f)
+            if (ifc.face_cells[f] != proc_cells[f] || ifc.coeffs[f] != proc_coeffs[f]) return 2;
+        if (cc.exchange(cc.user, send, recv, count) != 0) return 1;
+        if (cc.allreduce_sum(cc.user, values, n_values) != 0) return 1;
+        if (err && err_len > 0) err[0] = 0;
+        return 0;
+    } catch (const std::exception &e) {
+        if (err && err_len > 0) {
+            std::strncpy(err, e.what(), err_len - 1);
+            err[err_len - 1] = 0;
+        }
+        return -1;
+    }
 }
 
 } // extern "C"

@@ -264,6 +264,48 @@ cf_status cf_norm_factor(cf_matrix *m, const double *source, const double *psi,
 cf_status cf_solve(cf_matrix *m, int32_t solver, const cf_controls *controls,
                    const double *source, double *psi, cf_perf *perf);
 
+/* ---- decomposed cases (processor patches) ------------------------------- */
+/* The reference has no counterpart: its solvers take OpenFOAM's interface
+ * lists and ignore them (cuFoamCG/cuFoamCG.C:19-35), so a decomposed run
+ * solves every subdomain alone.  Here `m` is this rank's subdomain and the
+ * processor patches couple it to the others as OpenFOAM's lduMatrix::Amul
+ * does (initMatrixInterfaces / updateMatrixInterfaces): after the local
+ * product, row face_cells[f] loses coeffs[f] * (the neighbouring rank's
+ * value of the cell across face f), coeffs being interfaceBouCoeffs.
+ * Faces are listed patch after patch in the order every rank agrees on;
+ * the faces of one cell are applied in that order.
+ *
+ * The caller moves the data; the library never talks to another process.
+ *   exchange(user, send, recv, count): send[f] is this rank's value of
+ *     face_cells[f]; fill recv[f] with the neighbour's value of the cell on
+ *     the other side of face f.  Called once per product, by every rank,
+ *     also with count 0 on a rank without processor faces.
+ *   allreduce_sum(user, values, count): replace values[0..count) by their
+ *     sums over all ranks.
+ * Both return 0 on success; anything else ends the solve with
+ * CF_BAD_INPUT.  Buffers are host memory and valid during the call only. */
+typedef struct cf_comm {
+    void *user;
+    int32_t (*exchange)(void *user, const double *send, double *recv, int32_t count);
+    int32_t (*allreduce_sum)(void *user, double *values, int32_t count);
+} cf_comm;
+
+typedef struct cf_interfaces {
+    int32_t n_faces;            /* processor-patch faces of this subdomain */
+    const int32_t *face_cells;  /* [n_faces] host: local cell of each face */
+    const double *coeffs;       /* [n_faces] host: interfaceBouCoeffs */
+} cf_interfaces;
+
+/* cuFoam<X>::solve on a decomposed case: normFactor and every inner
+ * product summed over all ranks, the product coupled through the
+ * interfaces.  CG only (the other solvers return CF_UNSUPPORTED), FP64,
+ * no transpose; history, time_limit_s, norm_type, min/max_iter and
+ * rel_tol as in cf_solve.  Three host round trips per step (one exchange,
+ * two all-reduces); the loop is host-driven. */
+cf_status cf_solve_decomposed(cf_matrix *m, int32_t solver, const cf_controls *controls,
+                              const cf_interfaces *interfaces, const cf_comm *comm,
+                              const double *source, double *psi, cf_perf *perf);
+
 /* Gradient of a loss L through A x = b with respect to the LDU
  * coefficients, from the forward solution x and the adjoint solution
  * lambda of A^T lambda = dL/dx (solve with controls.transpose = 1):

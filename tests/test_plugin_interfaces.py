@@ -4,7 +4,8 @@ entries (faceCell, neighbour faceCell) = -interfaceBouCoeffs appended to
 each row (OpenFOAM's interface update, result -= coeffs * psi of the
 neighbour patch); the solve must equal the oracle's on that merged matrix
 (bit for bit in the reference summation order) and solve the periodic
-problem; processor interfaces are refused."""
+problem; processor interfaces outside a parallel run are refused
+(decomposed runs: test_gpu_decomposed.py)."""
 import numpy as np
 import pytest
 
@@ -73,7 +74,7 @@ def test_cyclic_nonsymmetric_bicg_fast_order():
     assert O.true_residual_norm(A, b, psi) / nf <= 1.5e-9
 
 
-def test_processor_interface_is_refused():
+def test_processor_interface_outside_a_parallel_run_is_refused():
     L = O.grid_const(8, 8, 1)
-    with pytest.raises(FoamError, match="cyclic"):
+    with pytest.raises(FoamError, match="outside a parallel run"):
         foam_solve("cuFoamCG", L, O.uniform(1, L.n), np.zeros(L.n), processor_patch=True)
