@@ -462,6 +462,9 @@ def compact_suite(extras: dict) -> dict:
                           "mixed_true": float(f"{m['true_rel_residual']:.3g}"),
                           "speedup": r["speedup"],
                           "err_vs_fp64": float(f"{m['rel_error_vs_fp64']:.3g}")}
+            for arm, k in (("FP64", "fp64_tightened_tol"), ("mixed", "mixed_tightened_tol")):
+                if "tightened_tolerance" in r[arm]:
+                    out[short][k] = float(f"{r[arm]['tightened_tolerance']:.3g}")
             if "FP64_fast" in r:
                 ff = r["FP64_fast"]
                 out[short].update({"fp64_fast_ms": ff["ms"], "fp64_fast_it": ff["iterations"],
@@ -765,27 +768,40 @@ def mixed_vs_fp64(ctx, device, solver: str = "cuFoamMR", n: int = 256, pe: float
             ctrl["reduction"] = "fast"
         psi = torch.zeros(L.n, dtype=torch.float64, device=dev)
         cf._TABLE[solver]("U", M, dict(ctrl, maxIter=5)).solve(psi, src)  # warm-up: graphs, FP32 copy
-        psi.zero_()
-        torch.cuda.synchronize()
-        w0 = time.perf_counter()
-        perf = cf._TABLE[solver]("U", M, ctrl).solve(psi, src)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - w0
-        r = src - M.spmv(psi, row_order="fast")
-        true_rel = float(torch.linalg.norm(r)) / perf.norm_factor
+        # the time to a TRUE relative residual <= tol: a solve that stops on
+        # its recurrence residual with the true one above tol (BiCG's
+        # recurrence drifts) is repeated with the tolerance tightened by the
+        # gap, at most twice; the solve that reached tol is the one timed
+        run_tol = tol
+        for attempt in range(3):
+            psi.zero_()
+            torch.cuda.synchronize()
+            w0 = time.perf_counter()
+            perf = cf._TABLE[solver]("U", M, dict(ctrl, tolerance=run_tol)).solve(psi, src)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - w0
+            r = src - M.spmv(psi, row_order="fast")
+            true_rel = float(torch.linalg.norm(r)) / perf.norm_factor
+            if perf.status_name != "ok" or true_rel <= tol or attempt == 2:
+                break
+            run_tol = run_tol * 0.8 * tol / true_rel
         res[prec] = (psi, perf)
         out[prec] = {"ms": round(perf.solve_ms, 2), "wall_ms": round(1e3 * wall, 2),
                      "iterations": perf.n_iterations, "status": perf.status_name,
                      "final_rel_residual": perf.final_residual, "true_rel_residual": true_rel}
+        if run_tol != tol:
+            out[prec]["tightened_tolerance"] = run_tol
         if prec == "mixed":
             out[prec]["refinements"] = perf.n_outer
     (x64, p64), (x32, p32) = res["FP64"], res["mixed"]
     out["mixed"]["rel_error_vs_fp64"] = float(torch.linalg.norm(x32 - x64) / torch.linalg.norm(x64))
-    both = p64.status_name == "ok" and p32.status_name == "ok"
+    def reached(prec):   # converged with the true residual at the target
+        return out[prec]["status"] == "ok" and out[prec]["true_rel_residual"] <= tol
+    both = reached("FP64") and reached("mixed")
     out["speedup"] = round(p64.solve_ms / p32.solve_ms, 3) if both else None
     if "FP64_fast" in res:
         pf = res["FP64_fast"][1]
-        ok = pf.status_name == "ok" and p32.status_name == "ok"
+        ok = reached("FP64_fast") and reached("mixed")
         out["speedup_vs_fast"] = round(pf.solve_ms / p32.solve_ms, 3) if ok else None
     M.close()
     return out

@@ -163,11 +163,28 @@ __device__ __forceinline__ bool grid_reduce(T (&acc)[NV], T *partials, int strid
 #pragma unroll
             for (int i = 0; i < NV; ++i) out[i] = run[i];
     } else {
+        // thread t adds partials t, t + 256, ... in that order; for grids of
+        // up to 5 * 256 blocks (the fast grid is at most 8 blocks per SM,
+        // 1,216 on 152 SMs) all its loads are issued before the first
+        // addition: one L2 round trip instead of one per partial
+        constexpr int kPer = 5;
         T v[NV];
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
             T s = T(0);
-            for (int b = threadIdx.x; b < G; b += kBlock) s += ld_cg(partials + i * stride + b);
+            if (G <= kPer * kBlock) {
+                T t[kPer];
+#pragma unroll
+                for (int u = 0; u < kPer; ++u) {
+                    const int b = threadIdx.x + u * kBlock;
+                    t[u] = b < G ? ld_cg(partials + i * stride + b) : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < kPer; ++u)
+                    if (threadIdx.x + u * kBlock < G) s += t[u];
+            } else {
+                for (int b = threadIdx.x; b < G; b += kBlock) s += ld_cg(partials + i * stride + b);
+            }
             v[i] = s;
         }
         __syncthreads();
@@ -475,6 +492,31 @@ __device__ __forceinline__ int32_t ld_stream(const int32_t *p, uint64_t pol)
     int32_t v;
     asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
     return v;
+}
+
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// L2 prefetch of the first (up to 8) entries of this warp's first slice:
+// constant matrix data a loop-body kernel may request before it waits for
+// its predecessor (programmatic launches start early), so that its first
+// loads after the wait hit L2.
+template <class V>
+__device__ __forceinline__ void sell_prefetch_first(int n_slices, const int32_t *__restrict__ off,
+                                                    const int32_t *__restrict__ col, const V *__restrict__ val)
+{
+    const int s = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    if (s >= n_slices) return;
+    const int lane = threadIdx.x & 31;
+    const int b = __ldg(off + s);
+    const int len = (__ldg(off + s + 1) - b) >> 5;
+    const int m = len < 8 ? len : 8;
+    for (int u = 0; u < m; ++u) {
+        prefetch_l2(col + b + lane + 32 * u);
+        prefetch_l2(val + b + lane + 32 * u);
+    }
 }
 
 // M entries of a SELL row (slots 32 elements apart): all loads and gathers

@@ -18,15 +18,19 @@
 #include <cmath>
 
 // Resident blocks per SM the FP32 SpMV passes ask for (five measured best
-// for the 256^3 MR inner solve: 276 us per step against 309 us with four
-// and 290 us with six).
+// for the 256^3 MR inner solve with batches of eight: 245 us per step
+// against 260 us with four), and the CG one (four: 49.2 us per step at
+// 128^3 against 53.0 us with five; its on-the-fly direction update needs
+// the registers).
 #ifndef CF_MX_MIN_BLOCKS
 #define CF_MX_MIN_BLOCKS 5
 #endif
-// SELL entries per thread and batch in the two BiCGStab SpMV passes: with
-// 8 the 256^3 convection-diffusion BiCGStab step took 735 us against 989 us
-// with the default 4 and 1,039 us with 2 (MR's SpMV: 273, 269 and 412 us,
-// so the others keep 4).
+#ifndef CF_MX_CG_MIN_BLOCKS
+#define CF_MX_CG_MIN_BLOCKS 4
+#endif
+// SELL entries per thread and batch in the two BiCGStab SpMV passes (8: the
+// 256^3 convection-diffusion BiCGStab step took 735 us against 989 us with
+// 4 and 1,039 us with 2).
 #ifndef CF_BCS_SELL_BATCH
 #define CF_BCS_SELL_BATCH 8
 #endif
@@ -126,9 +130,10 @@ __global__ void __launch_bounds__(kBlock) k_mx_setup(const SolveArgs *__restrict
 
 // CG: K1 p = r + beta p_old (on the fly), q = A32 p, (p, q); deferred d update
 template <int FMT>
-__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_cg_spmv(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_MX_CG_MIN_BLOCKS) k_mx_cg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
+    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val32);
     CF_EXIT_IF_DONE(a, st, false);
     const int k = ld_cg(&st->k) + 1;
     const bool first = (k == 1);
@@ -225,6 +230,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_bcs_spmv1(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
+    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val32);
     CF_EXIT_IF_DONE(a, st, false);
     const float *__restrict__ p = a->fp[0];
     const float *__restrict__ rh = a->frs;
@@ -251,6 +257,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_bcs_spmv2(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
+    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val32);
     CF_EXIT_IF_DONE(a, st, false);
     const float alpha = (float)ld_cg(&st->xi);
     const float *__restrict__ r = a->fr;
@@ -329,6 +336,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_mr_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
+    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val32);
     CF_EXIT_IF_DONE(a, st, false);
     const float *__restrict__ r = a->fr;
     float *__restrict__ y = a->fq;

@@ -38,35 +38,39 @@ namespace cf {
 __global__ void __launch_bounds__(kBlock) k_f_cg_prep(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
-    CF_EXIT_IF_DONE(a, st, false);
     const int n = a->n;
-    const int k = ld_cg(&st->k) + 1;
     double *__restrict__ p = a->p[0];
     const double *__restrict__ r = a->r[0];
     double *__restrict__ x = a->x;
+    const bool pairs = (((uintptr_t)x | (uintptr_t)p | (uintptr_t)r) & 15) == 0;
+    const int np = n >> 1;
+    const int stride = gridDim.x * kBlock;
+    int j = blockIdx.x * kBlock + threadIdx.x;
+    double2 *__restrict__ x2 = reinterpret_cast<double2 *>(x);
+    double2 *__restrict__ p2 = reinterpret_cast<double2 *>(p);
+    // p and x were last written by the previous step's prep, which completed
+    // before the update this launch follows could start: the first pair is
+    // loaded before the wait for the update (r, written by it, after)
+    double2 pv = make_double2(0.0, 0.0), xv = pv, rv = pv;
+    if (pairs && j < np) {
+        pv = p2[j];
+        xv = x2[j];
+    }
+    CF_EXIT_IF_DONE(a, st, false);
+    const int k = ld_cg(&st->k) + 1;
     if (k == 1) {
         CF_FOR_ELEMS(i, n) p[i] = r[i];
         return;
     }
     const double beta = ld_cg(&st->beta);
     const double xi = ld_cg(&st->xi);
-    if ((((uintptr_t)x | (uintptr_t)p | (uintptr_t)r) & 15) == 0) {
+    if (pairs) {
         // element pairs as 16-byte loads; each thread loads its next pair
         // before computing the current one, so the FP64 work of one pair
         // overlaps the loads of the next (measured 12.4 -> 10.4 us at 128^3
         // with L2-resident vectors)
-        const int np = n >> 1;
-        double2 *__restrict__ x2 = reinterpret_cast<double2 *>(x);
-        double2 *__restrict__ p2 = reinterpret_cast<double2 *>(p);
         const double2 *__restrict__ r2 = reinterpret_cast<const double2 *>(r);
-        const int stride = gridDim.x * kBlock;
-        int j = blockIdx.x * kBlock + threadIdx.x;
-        double2 pv = make_double2(0.0, 0.0), xv = pv, rv = pv;
-        if (j < np) {
-            pv = p2[j];
-            xv = x2[j];
-            rv = r2[j];
-        }
+        if (j < np) rv = r2[j];
         for (; j < np; j += stride) {
             const int jn = j + stride;
             double2 pn = make_double2(0.0, 0.0), xn = pn, rn = pn;
@@ -114,6 +118,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_cg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
+    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val);
     CF_EXIT_IF_DONE(a, st, false);
     const double *__restrict__ p = a->p[0];
     double *__restrict__ q = a->q;
@@ -130,33 +135,53 @@ __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_cg_spmv(const 
     }
 }
 
+// resident blocks per SM asked of nvcc for the update pass (five: 71.95 us
+// per 128^3 CG step against 72.8 us with six)
+#ifndef CF_CG_UPDATE_MIN_BLOCKS
+#define CF_CG_UPDATE_MIN_BLOCKS 5
+#endif
+
 // r -= xi q, (r, r)
-__global__ void __launch_bounds__(kBlock) k_f_cg_update(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_CG_UPDATE_MIN_BLOCKS) k_f_cg_update(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
-    CF_EXIT_IF_DONE(a, st, true);
     const int n = a->n;
-    const double xi = ld_cg(&st->xi);
     double *__restrict__ r = a->r[0];
     const double *__restrict__ q = a->q;
+    const int stride = gridDim.x * kBlock;
+    int i = blockIdx.x * kBlock + threadIdx.x;
+    // r was last written by the previous step's update, which completed
+    // before the SpMV this launch follows could start: its first loads are
+    // issued before the wait for the SpMV, and each step loads the next r
+    // group before its FP64 work
+    double rv[4];
+    if (i + 3 * stride < n) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) rv[u] = r[i + u * stride];
+    }
+    CF_EXIT_IF_DONE(a, st, true);
+    const double xi = ld_cg(&st->xi);
     // one accumulator: the FP64 unit, not the FMA latency, limits this pass
     // on GB300, and combining four partials cost 12% more FP64 instructions
     double acc[1] = {0.0};
-    CF_X4_LOOP(i, n) {
-        double qv[4], rv[4];
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        double qv[4], rn[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            qv[u] = q[CF_X4_IDX(i, u)];
-            rv[u] = r[CF_X4_IDX(i, u)];
+        for (int u = 0; u < 4; ++u) qv[u] = q[i + u * stride];
+        const int in = i + 4 * stride;
+        if (in + 3 * stride < n) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) rn[u] = r[in + u * stride];
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const double ri = fma_t(-xi, qv[u], rv[u]);
-            r[CF_X4_IDX(i, u)] = ri;
+            r[i + u * stride] = ri;
             acc[0] = fma_t(ri, ri, acc[0]);
+            rv[u] = rn[u];
         }
     }
-    CF_X4_TAIL(i, n) {
+    for (; i < n; i += stride) {
         const double ri = fma_t(-xi, q[i], r[i]);
         r[i] = ri;
         acc[0] = fma_t(ri, ri, acc[0]);
@@ -326,9 +351,13 @@ __global__ void __launch_bounds__(kBlock) k_f_bicg_prep(const SolveArgs *__restr
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS - 1) k_f_bicg_spmv(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_BICG_SPMV_MIN_BLOCKS) k_f_bicg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
+    if constexpr (FMT == kSell) {
+        sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val);
+        sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_valT);
+    }
     CF_EXIT_IF_DONE(a, st, false);
     const double *__restrict__ p = a->p[0];
     const double *__restrict__ ps = a->ps[0];
@@ -367,6 +396,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_jac_step(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
+    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->sc_val);
     CF_EXIT_IF_DONE(a, st, true);
     const int k = ld_cg(&st->k) + 1;
     const double *__restrict__ rin = a->r[(k + 1) & 1];
@@ -415,6 +445,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_rich_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
+    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val);
     CF_EXIT_IF_DONE(a, st, true);
     const double *__restrict__ x = a->x;
     const double *__restrict__ b = a->b;
@@ -453,6 +484,8 @@ template <int FORM, int FMT>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_mr_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
+    if constexpr (FMT == kSell)
+        sell_prefetch_first(a->n_slices, a->s_off, a->s_col, FORM == kMrScaled ? a->sc_val : a->s_val);
     CF_EXIT_IF_DONE(a, st, false);
     const double *__restrict__ r = a->r[0];
     const double *__restrict__ gv = FORM == kMrZ ? a->w[1] : a->r[0];

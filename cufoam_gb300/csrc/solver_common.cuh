@@ -24,22 +24,31 @@ namespace cf {
 enum { kCsr = 0, kSell = 1 };
 
 // SELL passes take CF_SELL_BATCH entries per thread per batch: all their
-// loads and gathers are issued before the first FMA.  With five resident
-// blocks per SM (48 registers) four measured best on the 7-point 128^3 CG
-// step: SpMV 49.8 us in the solve, against 52-68 us for batches of 2 or 8
-// and for 3, 4 or 6 blocks per SM.
+// loads and gathers are issued before the first FMA, and a row's last
+// entries form one exact batch.  With eight a 7-entry row is a single batch;
+// with four resident blocks per SM (64 registers) that measured best on
+// GB300 for the 7-point 128^3 system: CG step 71.4 us against 72.8 us with
+// batches of four at five blocks per SM (SpMV 41.8 against 43.3 us), Jacobi
+// 53.5 against 55.6 us, MR 62.8 against 64.7 us per step.
 #ifndef CF_SELL_BATCH
-#define CF_SELL_BATCH 4
+#define CF_SELL_BATCH 8
 #endif
 // Resident blocks per SM the SpMV passes ask nvcc for (it sizes their
-// register budget from it); the two-value BiCG passes ask for one fewer.
+// register budget from it).
 #ifndef CF_SPMV_MIN_BLOCKS
-#define CF_SPMV_MIN_BLOCKS 5
+#define CF_SPMV_MIN_BLOCKS 4
+#endif
+// the two-value BiCG passes
+#ifndef CF_BICG_SPMV_MIN_BLOCKS
+#define CF_BICG_SPMV_MIN_BLOCKS 4
 #endif
 constexpr int kSellBatch = CF_SELL_BATCH;
-// the same for the FP32 passes of the mixed-precision inner solves
+// the same for the FP32 passes of the mixed-precision inner solves: with
+// eight a 7-entry row is one exact batch (all seven loads in flight), which
+// measured best on GB300 for the 256^3 upwind MR inner solve (245 us per
+// step against 280 us with four and 320 us with two) and the 128^3 CG one
 #ifndef CF_SELL_BATCH32
-#define CF_SELL_BATCH32 4
+#define CF_SELL_BATCH32 8
 #endif
 constexpr int kSellBatch32 = CF_SELL_BATCH32;
 
