@@ -62,7 +62,8 @@ ALLREDUCE_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.POINTER(C.c_double), C.c_int
 
 
 class cf_comm(C.Structure):
-    _fields_ = [("user", C.c_void_p), ("exchange", EXCHANGE_FN), ("allreduce_sum", ALLREDUCE_FN)]
+    _fields_ = [("user", C.c_void_p), ("exchange", EXCHANGE_FN), ("allreduce_sum", ALLREDUCE_FN),
+                ("allreduce_max", ALLREDUCE_FN)]
 
 
 class cf_interfaces(C.Structure):

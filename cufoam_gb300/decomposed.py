@@ -135,6 +135,16 @@ def ordered_allreduce_sum(values: np.ndarray, group=None) -> None:
     values[:] = acc.numpy()
 
 
+def ordered_allreduce_max(values: np.ndarray, group=None) -> None:
+    """values[:] = their maximum over the ranks of `group`."""
+    import torch
+    import torch.distributed as dist
+    t = torch.from_numpy(np.ascontiguousarray(values, dtype=np.float64))
+    parts = [torch.empty_like(t) for _ in range(dist.get_world_size(group))]
+    dist.all_gather(parts, t, group=group)
+    values[:] = torch.stack(parts).max(dim=0).values.numpy()
+
+
 class ProcessorComm:
     """Processor-patch exchange and global sums over ``torch.distributed``.
 
@@ -143,7 +153,8 @@ class ProcessorComm:
     cells across the same faces come back, in the shared face order.
     ``allreduce_sum(values)``: every rank's values are gathered and added
     in rank order, so all ranks hold bit-identical sums (the solve's
-    stopping decisions must agree on every rank)."""
+    stopping decisions must agree on every rank); ``allreduce_max`` the
+    same with the maximum."""
 
     def __init__(self, patches, group=None):
         import torch.distributed as dist
@@ -180,6 +191,9 @@ class ProcessorComm:
     def allreduce_sum(self, values: np.ndarray) -> None:
         ordered_allreduce_sum(values, self.group)
 
+    def allreduce_max(self, values: np.ndarray) -> None:
+        ordered_allreduce_max(values, self.group)
+
     # ---- the C callbacks -------------------------------------------------
     def as_c(self) -> _capi.cf_comm:
         """A cf_comm whose callbacks call exchange / allreduce_sum; the
@@ -199,21 +213,24 @@ class ProcessorComm:
                 self.error = e
                 return 1
 
-        def red(_user, vp, count):
-            try:
-                v = np.ctypeslib.as_array(vp, shape=(count,))
-                self.allreduce_sum(v)
-                return 0
-            except BaseException as e:  # noqa: BLE001
-                self.error = e
-                return 1
+        def reducer(method):
+            def red(_user, vp, count):
+                try:
+                    method(np.ctypeslib.as_array(vp, shape=(count,)))
+                    return 0
+                except BaseException as e:  # noqa: BLE001
+                    self.error = e
+                    return 1
+            return red
 
         self._c_ex = _capi.EXCHANGE_FN(ex)
-        self._c_red = _capi.ALLREDUCE_FN(red)
+        self._c_red = _capi.ALLREDUCE_FN(reducer(self.allreduce_sum))
+        self._c_max = _capi.ALLREDUCE_FN(reducer(self.allreduce_max))
         c = _capi.cf_comm()
         c.user = None
         c.exchange = self._c_ex
         c.allreduce_sum = self._c_red
+        c.allreduce_max = self._c_max
         return c
 
 

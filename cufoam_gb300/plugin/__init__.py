@@ -44,8 +44,8 @@ def lib():
             [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int]
         L.mf_processor_comm_check.restype = C.c_int
         L.mf_processor_comm_check.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                              C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
-                                              C.c_char_p, C.c_int]
+                                              C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                              C.c_int, C.c_char_p, C.c_int]
         _lib = L
     return _lib
 
@@ -121,7 +121,8 @@ _ALLREDUCE_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.POINTER(C.c_double), C.c_in
 
 class _Transport(C.Structure):
     _fields_ = [("myProcNo", C.c_int32), ("nProcs", C.c_int32), ("user", C.c_void_p),
-                ("complete", _COMPLETE_FN), ("allreduceSum", _ALLREDUCE_FN)]
+                ("complete", _COMPLETE_FN), ("allreduceSum", _ALLREDUCE_FN),
+                ("allreduceMax", _ALLREDUCE_FN)]
 
 
 class ParallelRun:
@@ -138,8 +139,9 @@ class ParallelRun:
         self.error: BaseException | None = None
         self._complete = _COMPLETE_FN(self._on_complete)
         self._reduce = _ALLREDUCE_FN(self._on_reduce)
+        self._max = _ALLREDUCE_FN(self._on_max)
         self._t = _Transport(dist.get_rank(group), dist.get_world_size(group), None,
-                             self._complete, self._reduce)
+                             self._complete, self._reduce, self._max)
 
     def _on_complete(self, _user, n, kind, peer, tag, data, nbytes):
         import torch
@@ -166,6 +168,15 @@ class ParallelRun:
         from ..decomposed import ordered_allreduce_sum
         try:
             ordered_allreduce_sum(np.ctypeslib.as_array(values, shape=(count,)), self.group)
+            return 0
+        except BaseException as e:  # noqa: BLE001
+            self.error = e
+            return 1
+
+    def _on_max(self, _user, values, count):
+        from ..decomposed import ordered_allreduce_max
+        try:
+            ordered_allreduce_max(np.ctypeslib.as_array(values, shape=(count,)), self.group)
             return 0
         except BaseException as e:  # noqa: BLE001
             self.error = e
@@ -225,15 +236,17 @@ def foam_solve_decomposed(solver: str, sub, source, psi, tolerance: float = 1e-6
 def processor_comm_check(sub, send, values):
     """Drive the plugin's processor-patch callbacks (cuFoamGB300Comm.H)
     once without a solve, inside ``with ParallelRun():``: returns (status,
-    recv, values) after one exchange of `send` and one sum of `values`."""
+    recv, sums, maxima) after one exchange of `send` and one sum and one
+    maximum of `values` over the ranks."""
     nb, sz, fc, co = _proc_arrays(sub)
     s = np.ascontiguousarray(send, np.float64)
     r = np.zeros(max(1, len(s)))
     v = np.ascontiguousarray(values, np.float64).copy()
+    mx = v.copy()
     err = C.create_string_buffer(1024)
     rc = lib().mf_processor_comm_check(len(nb), nb.ctypes.data, sz.ctypes.data, fc.ctypes.data,
                                        co.ctypes.data, s.ctypes.data if len(s) else r.ctypes.data,
-                                       r.ctypes.data, len(s), v.ctypes.data, len(v), err, 1024)
+                                       r.ctypes.data, len(s), v.ctypes.data, mx.ctypes.data, len(v), err, 1024)
     if rc < 0:
         raise FoamError(err.value.decode())
-    return rc, r[:len(s)], v
+    return rc, r[:len(s)], v, mx

@@ -22,9 +22,9 @@
  * neighbour patch's face cells, becomes the CSR entries (faceCell,
  * neighbour faceCell) = -coeff appended to each row).  In a parallel run
  * (Pstream::parRun()) the processor patches couple each rank's subdomain
- * to its neighbours: CG solves the decomposed system
- * (cf_solve_decomposed, transfers through OpenFOAM's Pstream,
- * cuFoamGB300Comm.H); the other solvers stop with a FatalError there.
+ * to its neighbours: every solver runs on the decomposed system
+ * (cf_solve_decomposed, FP64, transfers through OpenFOAM's Pstream,
+ * cuFoamGB300Comm.H); `precision mixed` stops with a FatalError there.
  * The reference ignores all interfaces.
  *
  * Residuals in the returned solverPerformance are normalised by normFactor

@@ -16,6 +16,8 @@
  *   allreduce_sum: reduce(value, sumOp<scalar>()) per value -- OpenFOAM's
  *                  own solvers decide convergence on such sums on every rank,
  *                  so they are the same on every rank
+ *   allreduce_max: reduce(value, maxOp<scalar>()) (Richardson's power
+ *                  method: the smallest |a_ii| of the whole mesh)
  * Compiles against OpenFOAM or the minifoam stand-in.
  */
 #ifndef CUFOAM_GB300_COMM_H
@@ -72,6 +74,16 @@ class cuFoamGB300ProcessorComm {
         }
     }
 
+    static int32_t allreduceMax(void *, double *values, int32_t count)
+    {
+        try {
+            for (int32_t i = 0; i < count; ++i) reduce(values[i], maxOp<scalar>());
+            return 0;
+        } catch (const std::exception &) {
+            return 1;
+        }
+    }
+
 public:
     // The processor interfaces of `interfaces`, in patch order, with their
     // interfaceBouCoeffs; other (and unset) patches are skipped.
@@ -116,6 +128,7 @@ public:
         c.user = const_cast<cuFoamGB300ProcessorComm *>(this);
         c.exchange = &exchange;
         c.allreduce_sum = &allreduceSum;
+        c.allreduce_max = &allreduceMax;
         return c;
     }
 };

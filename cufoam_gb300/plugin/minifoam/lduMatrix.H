@@ -73,6 +73,7 @@ struct mfTransport {
     int32_t (*complete)(void *user, int32_t n, const int32_t *kind, const int32_t *peer,
                         const int32_t *tag, void *const *data, const int64_t *bytes);
     int32_t (*allreduceSum)(void *user, double *values, int32_t count);
+    int32_t (*allreduceMax)(void *user, double *values, int32_t count);
 };
 
 class UPstream {
@@ -132,12 +133,24 @@ struct sumOp {
     T operator()(const T &a, const T &b) const { return a + b; }
 };
 
-// reduce(value, sumOp<scalar>()): the sum over all ranks, on every rank
+template <class T>
+struct maxOp {
+    T operator()(const T &a, const T &b) const { return a > b ? a : b; }
+};
+
+// reduce(value, sumOp<scalar>()) / reduce(value, maxOp<scalar>()): the sum
+// or the maximum over all ranks, on every rank
 inline void reduce(double &v, const sumOp<double> &)
 {
     if (!UPstream::parRun()) return;
     const mfTransport *t = UPstream::transport();
     if (t->allreduceSum(t->user, &v, 1) != 0) throw std::runtime_error("Pstream: a reduction failed");
+}
+inline void reduce(double &v, const maxOp<double> &)
+{
+    if (!UPstream::parRun()) return;
+    const mfTransport *t = UPstream::transport();
+    if (t->allreduceMax(t->user, &v, 1) != 0) throw std::runtime_error("Pstream: a reduction failed");
 }
 
 template <class T>

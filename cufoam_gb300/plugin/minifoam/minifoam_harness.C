@@ -230,11 +230,12 @@ int mf_solve_decomposed(const char *solver_name, int n, int n_faces, const doubl
 /* The plugin's processor-patch callbacks (cuFoamGB300Comm.H) without a
  * solve: the interfaces of n_proc patches as in mf_solve_decomposed, one
  * exchange of send[] (the values of the face cells, patch after patch)
- * into recv[], then a sum over the ranks of values[0..n_values).  Returns
- * 0, 1 when a callback failed, -1 on a FatalError (text in err). */
+ * into recv[], then a sum over the ranks of values[0..n_values) and a
+ * maximum of max_values[0..n_values).  Returns 0, 1 when a callback
+ * failed, -1 on a FatalError (text in err). */
 int mf_processor_comm_check(int n_proc, const int *proc_neighbour, const int *proc_size, const int *proc_cells,
                             const double *proc_coeffs, const double *send, double *recv, int count,
-                            double *values, int n_values, char *err, int err_len)
+                            double *values, double *max_values, int n_values, char *err, int err_len)
 {
     try {
         using namespace Foam;
@@ -258,6 +259,7 @@ int mf_processor_comm_check(int n_proc, const int *proc_neighbour, const int *pr
             if (ifc.face_cells[f] != proc_cells[f] || ifc.coeffs[f] != proc_coeffs[f]) return 2;
         if (cc.exchange(cc.user, send, recv, count) != 0) return 1;
         if (cc.allreduce_sum(cc.user, values, n_values) != 0) return 1;
+        if (cc.allreduce_max(cc.user, max_values, n_values) != 0) return 1;
         if (err && err_len > 0) err[0] = 0;
         return 0;
     } catch (const std::exception &e) {

@@ -281,13 +281,18 @@ cf_status cf_solve(cf_matrix *m, int32_t solver, const cf_controls *controls,
  *     the other side of face f.  Called once per product, by every rank,
  *     also with count 0 on a rank without processor faces.
  *   allreduce_sum(user, values, count): replace values[0..count) by their
- *     sums over all ranks.
- * Both return 0 on success; anything else ends the solve with
+ *     sums over all ranks -- the same bits on every rank (the ranks take
+ *     their stopping decisions on them).
+ *   allreduce_max(user, values, count): the same with the maximum; only
+ *     Richardson without a given relaxation factor needs it (the smallest
+ *     |a_ii| of the whole mesh), and may be NULL otherwise.
+ * They return 0 on success; anything else ends the solve with
  * CF_BAD_INPUT.  Buffers are host memory and valid during the call only. */
 typedef struct cf_comm {
     void *user;
     int32_t (*exchange)(void *user, const double *send, double *recv, int32_t count);
     int32_t (*allreduce_sum)(void *user, double *values, int32_t count);
+    int32_t (*allreduce_max)(void *user, double *values, int32_t count);
 } cf_comm;
 
 typedef struct cf_interfaces {
@@ -298,10 +303,12 @@ typedef struct cf_interfaces {
 
 /* cuFoam<X>::solve on a decomposed case: normFactor and every inner
  * product summed over all ranks, the product coupled through the
- * interfaces.  CG only (the other solvers return CF_UNSUPPORTED), FP64,
- * no transpose; history, time_limit_s, norm_type, min/max_iter and
- * rel_tol as in cf_solve.  Three host round trips per step (one exchange,
- * two all-reduces); the loop is host-driven. */
+ * interfaces (A^T's, for BiCG, through the neighbours' coefficients of the
+ * same faces, exchanged once).  All nine solvers, FP64, the fast summation
+ * order, no transpose; history, time_limit_s, norm_type, min/max_iter,
+ * rel_tol, bicg_int_bound, richardson_omega and power_max_steps as in
+ * cf_solve.  The loop is host-driven: per step one exchange per product
+ * (BiCG two) and one or two all-reduces. */
 cf_status cf_solve_decomposed(cf_matrix *m, int32_t solver, const cf_controls *controls,
                               const cf_interfaces *interfaces, const cf_comm *comm,
                               const double *source, double *psi, cf_perf *perf);

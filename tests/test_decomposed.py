@@ -187,6 +187,9 @@ def _rank_main(rank, world, port, out_dir, case):
             return float(a[0])
 
         k, hist = _cg(apply, dot, b, x, 1e-8, 2000)
+        m = np.array([float(rank), -float(rank)])
+        rcm = cc.allreduce_max(None, m.ctypes.data_as(C.POINTER(C.c_double)), 2)
+        assert rcm == 0 and m.tolist() == [world - 1.0, 0.0], m
         # a wrong count is reported as a failure, not a crash
         bad = np.zeros(2)
         rc = cc.exchange(None, bad.ctypes.data_as(C.POINTER(C.c_double)),
@@ -243,10 +246,10 @@ def _plugin_rank_main(rank, world, port, out_dir):
         fc, _ = sub.interface_arrays()
         vals = np.array([rank + 0.5, 1e-3 * (rank + 1), -2.0 * rank])
         with ParallelRun() as run:
-            rc, recv, summed = processor_comm_check(sub, x[sub.cells][fc], vals)
+            rc, recv, summed, maxed = processor_comm_check(sub, x[sub.cells][fc], vals)
             assert run.error is None, run.error
             # a second round through the same patches
-            rc2, recv2, _ = processor_comm_check(sub, 2.0 * x[sub.cells][fc], vals)
+            rc2, recv2, _, _ = processor_comm_check(sub, 2.0 * x[sub.cells][fc], vals)
         want = []
         for p in sub.patches:
             for f, c in zip(p.faces, p.face_cells):
@@ -255,7 +258,7 @@ def _plugin_rank_main(rank, world, port, out_dir):
         with open(os.path.join(out_dir, f"rank{rank}.json"), "w") as f:
             json.dump({"rc": [rc, rc2], "recv_ok": bool(np.array_equal(recv, np.array(want))),
                        "recv2_ok": bool(np.array_equal(recv2, 2.0 * np.array(want))),
-                       "summed": summed.tolist(), "n": int(len(fc))}, f)
+                       "summed": summed.tolist(), "maxed": maxed.tolist(), "n": int(len(fc))}, f)
         dist.barrier()
     finally:
         dist.destroy_process_group()
@@ -268,12 +271,14 @@ def test_plugin_processor_callbacks_over_gloo_ranks(tmp_path):
                        start_method="spawn")
     got = [json.load(open(tmp_path / f"rank{r}.json")) for r in range(world)]
     want = np.zeros(3)
-    for r in range(world):
-        want += np.array([r + 0.5, 1e-3 * (r + 1), -2.0 * r])
+    vals = [np.array([r + 0.5, 1e-3 * (r + 1), -2.0 * r]) for r in range(world)]
+    for v in vals:
+        want += v
     for g in got:
         assert g["rc"] == [0, 0]
         assert g["n"] > 0 and g["recv_ok"] and g["recv2_ok"]
         assert g["summed"] == got[0]["summed"]
+        assert g["maxed"] == np.max(vals, axis=0).tolist()
     np.testing.assert_allclose(got[0]["summed"], want, rtol=1e-15)
 
 
@@ -288,5 +293,5 @@ def test_plugin_refuses_processor_patches_outside_a_parallel_run():
     sub = decompose(L.n, L.lower_addr, L.upper_addr, L.diag, L.lower, L.upper,
                     (np.arange(L.n) % 2))[0]
     fc, _ = sub.interface_arrays()
-    rc, _, _ = processor_comm_check(sub, np.zeros(len(fc)), np.zeros(1))
+    rc, _, _, _ = processor_comm_check(sub, np.zeros(len(fc)), np.zeros(1))
     assert rc == 1
