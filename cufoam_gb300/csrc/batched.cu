@@ -102,13 +102,27 @@ struct BatchArgs {
     int32_t max_outer;
 };
 
-// sum over the block (fixed order), then over the cluster in rank order
-template <int NV, int BT>
+struct NoPost {
+    __device__ void operator()(int, double) const {}
+};
+
+// Sum over the block, then over the cluster: warp sums by shuffle trees,
+// the block's warp sums by a shuffle tree in warp 0, then -- after a
+// hardware cluster barrier -- the CTAs' sums by a shuffle tree in warp 0
+// (lane k reads CTA k's slot through distributed shared memory).  Every CTA
+// runs the same trees on the same values, so all reach bit-identical
+// totals.  Trees rather than sequential sums: on GB300 every dependent FP64
+// addition of a single thread costs its sub-partition's FP64 pipe 64
+// cycles, so a tree's log2 levels replace W - 1 and CS - 1 chained adds.
+// post(i, total) runs in lane 0 of warp 0 for each value before the final
+// block barrier (the scalar step logic that every thread then reads).
+template <int NV, int BT, class Post = NoPost>
 __device__ __forceinline__ void cluster_sum(cgp::cluster_group &cl, double (&v)[NV],
                                             double *wsm /*[NV][BT/32]*/, double *slot /*[NV]*/,
-                                            double *out /*[NV]*/)
+                                            double *out /*[NV]*/, Post post = Post())
 {
     constexpr int W = BT / 32;
+    static_assert((W & (W - 1)) == 0 && W <= 32, "warps per block: a power of two");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
@@ -121,17 +135,28 @@ __device__ __forceinline__ void cluster_sum(cgp::cluster_group &cl, double (&v)[
         if (lane == 0) wsm[i * W + warp] = s;
     }
     __syncthreads();
-    if (threadIdx.x < NV) {
-        double s = 0.0;
-        for (int w = 0; w < W; ++w) s += wsm[threadIdx.x * W + w];
-        slot[threadIdx.x] = s;
+    if (warp == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double s = lane < W ? wsm[i * W + lane] : 0.0;
+#pragma unroll
+            for (int o = W / 2; o; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
+            if (lane == 0) slot[i] = s;
+        }
     }
     cl.sync(); // every CTA's slot is written and visible cluster-wide
-    if (threadIdx.x < NV) {
-        double s = 0.0;
+    if (warp == 0) {
         const int cs = (int)cl.num_blocks();
-        for (int rk = 0; rk < cs; ++rk) s += cl.map_shared_rank(slot, rk)[threadIdx.x];
-        out[threadIdx.x] = s;
+#pragma unroll 1
+        for (int i = 0; i < NV; ++i) {
+            double s = lane < cs ? cl.map_shared_rank(slot, lane)[i] : 0.0;
+#pragma unroll
+            for (int o = 8; o; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
+            if (lane == 0) {
+                out[i] = s;
+                post(i, s);
+            }
+        }
     }
     __syncthreads();
 }
@@ -271,6 +296,7 @@ template <int R>
 struct CompState {
     double rho[R], rho_old[R], nrm[R], tol[R], nf[R];
     double alpha[R];          // step length not yet applied to x (or e)
+    double beta[R];           // direction update factor of the next step
     float rho32[R], rho32_old[R], eta[R];
     int act[R], act_in[R], iters[R];
 };
@@ -651,7 +677,7 @@ __global__ void __launch_bounds__(BT, batch_min_blocks<BT>()) k_batch_cg(const B
                     double beta[R], pend[R];
 #pragma unroll
                     for (int j = 0; j < R; ++j) {
-                        beta[j] = (k > 1 && act[j]) ? st.rho[j] / st.rho_old[j] : 0.0;
+                        beta[j] = (k > 1 && act[j]) ? st.beta[j] : 0.0;
                         pend[j] = st.alpha[j];
                     }
                     const double *r = a.r + S.vec_offset * R;
@@ -701,14 +727,18 @@ __global__ void __launch_bounds__(BT, batch_min_blocks<BT>()) k_batch_cg(const B
                                 }
                         }
                     }
-                    cluster_sum<R, BT>(cl, acc, wsm, slot[parity], tot);
+                    // the step lengths, once per CTA (a division is a chain of
+                    // dependent FP64 instructions)
+                    cluster_sum<R, BT>(cl, acc, wsm, slot[parity], tot, [&](int j, double pq) {
+                        st.alpha[j] = st.act[j] ? st.rho[j] / pq : 0.0;
+                    });
                     parity ^= 1;
                 }
                 // B: r -= alpha q, (r, r)
                 {
                     double alpha[R];
 #pragma unroll
-                    for (int j = 0; j < R; ++j) alpha[j] = act[j] ? st.rho[j] / tot[j] : 0.0;
+                    for (int j = 0; j < R; ++j) alpha[j] = st.alpha[j];
                     const double *q = a.q + S.vec_offset * R;
                     double *r = a.r + S.vec_offset * R;
                     double acc2[R];
@@ -726,7 +756,6 @@ __global__ void __launch_bounds__(BT, batch_min_blocks<BT>()) k_batch_cg(const B
                                     acc2[j] = fma_t(ri, ri, acc2[j]);
                                 }
                     }
-                    if (threadIdx.x < R) st.alpha[threadIdx.x] = alpha[threadIdx.x];
                     cluster_sum<R, BT>(cl, acc2, wsm, slot[parity], tot);
                     parity ^= 1;
                 }
@@ -735,6 +764,7 @@ __global__ void __launch_bounds__(BT, batch_min_blocks<BT>()) k_batch_cg(const B
                     if (st.act[j]) {
                         st.rho_old[j] = st.rho[j];
                         st.rho[j] = tot[j];
+                        st.beta[j] = st.rho[j] / st.rho_old[j];
                         st.nrm[j] = sqrt(st.rho[j]);
                         st.iters[j] = k;
                         st.act[j] = isfinite(st.nrm[j]) && k < a.max_iter && st.nrm[j] > st.tol[j];

@@ -17,13 +17,16 @@
 #include <climits>
 #include <cmath>
 
-// Resident blocks per SM the FP32 SpMV passes ask for (five measured best
-// for the 256^3 MR inner solve with batches of eight: 245 us per step
-// against 260 us with four), and the CG one (four: 49.2 us per step at
-// 128^3 against 53.0 us with five; its on-the-fly direction update needs
-// the registers).
+// Resident blocks per SM the FP32 SpMV passes ask for: the MR one six
+// (the 256^3 upwind MR inner solve with batches of eight: 238 us per step
+// against 242 us with five and 258 us with four), the BiCGStab ones five,
+// and the CG one four (49.2 us per step at 128^3 against 53.0 us with
+// five; its on-the-fly direction update needs the registers).
 #ifndef CF_MX_MIN_BLOCKS
-#define CF_MX_MIN_BLOCKS 5
+#define CF_MX_MIN_BLOCKS 6
+#endif
+#ifndef CF_MX_BCS_MIN_BLOCKS
+#define CF_MX_BCS_MIN_BLOCKS 5
 #endif
 #ifndef CF_MX_CG_MIN_BLOCKS
 #define CF_MX_CG_MIN_BLOCKS 4
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_bcs_prep(const SolveArgs *__restr
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_bcs_spmv1(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_MX_BCS_MIN_BLOCKS) k_mx_bcs_spmv1(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val32);
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_bcs_spmv1(const
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_bcs_spmv2(const SolveArgs *__restrict__ a)
+__global__ void __launch_bounds__(kBlock, CF_MX_BCS_MIN_BLOCKS) k_mx_bcs_spmv2(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
     if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val32);
