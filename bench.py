@@ -1032,6 +1032,93 @@ def run_profile_all(args):
     return 0
 
 
+# Algorithmic bytes per launch of every kernel family in the `--profile-all`
+# run (128^3 7-point systems), as (label, bytes) from the sizes: N cells, F
+# faces, nnz CSR entries, S stored SELL-32 entries in `slices` slices.  V =
+# one FP64 vector, V32 = one FP32 vector; a gathered vector counts once.
+def _launch_bytes(N, F, nnz, S, slices):
+    V, V32 = 8 * N, 4 * N
+    Mcsr = 12 * nnz + 4 * (N + 1)
+    Msell = 12 * S + 4 * (slices + 1)
+    Msell32 = 8 * S + 4 * (slices + 1)
+    t = {
+        "k_pow_step": ("Mcsr + 2V", Mcsr + 2 * V), "k_pow_final": ("Mcsr + V", Mcsr + V),
+        "k_bicg_spmv": ("Mcsr + 8nnz + 10V", Mcsr + 8 * nnz + 10 * V),
+        "k_mr_spmv<0>": ("Mcsr + 2V", Mcsr + 2 * V), "k_mr_spmv<1>": ("Mcsr + 3V", Mcsr + 3 * V),
+        "k_mr_spmv<2>": ("Mcsr + 3V", Mcsr + 3 * V), "k_mr_spmv<3>": ("Mcsr + 4V", Mcsr + 4 * V),
+        "k_nf_dist": ("Mcsr + 2V", Mcsr + 2 * V), "k_nf_sum": ("V", V),
+        "k_jacobi_step": ("Mcsr + 5V", Mcsr + 5 * V), "k_rich_step": ("Mcsr + 5V", Mcsr + 5 * V),
+        "k_cg_spmv": ("Mcsr + 6V", Mcsr + 6 * V), "k_res_init": ("Mcsr + 3V", Mcsr + 3 * V),
+        "k_bicg_update": ("6V", 6 * V), "k_cg_update": ("3V", 3 * V),
+        "k_mr_update<0>": ("5V", 5 * V), "k_mr_update<1>": ("6V", 6 * V),
+        "k_mr_update<2>": ("6V", 6 * V), "k_mr_update<3>": ("6V", 6 * V),
+        "k_f_cg_spmv<1>": ("Msell + 2V", Msell + 2 * V), "k_f_cg_update": ("3V", 3 * V),
+        "k_f_cg_prep": ("5V", 5 * V), "k_f_pcg_prep": ("6V", 6 * V), "k_f_pcg_update": ("4V", 4 * V),
+        "k_f_bicg_spmv<1>": ("Msell + 8S + 4V", Msell + 8 * S + 4 * V),
+        "k_f_bicg_prep": ("8V", 8 * V), "k_f_bicg_update": ("6V", 6 * V),
+        "k_f_jac_step<1>": ("Msell + 5V", Msell + 5 * V),
+        "k_f_rich_spmv<1>": ("Msell + 3V", Msell + 3 * V), "k_f_rich_prep": ("3V", 3 * V),
+        "k_f_mr_spmv<0, 1>": ("Msell + 2V", Msell + 2 * V),
+        "k_f_mr_spmv<1, 1>": ("Msell + 2V", Msell + 2 * V),
+        "k_f_mr_spmv<2, 1>": ("Msell + 3V", Msell + 3 * V),
+        "k_f_mr_update<0>": ("5V", 5 * V), "k_f_mr_update<1>": ("6V", 6 * V),
+        "k_f_mr_update<2>": ("8V", 8 * V),
+        "k_f_flush_x": ("3V", 3 * V), "k_flush_x": ("3V", 3 * V), "k_rich_finish": ("2V", 2 * V),
+        "k_min_abs": ("V", V),
+        "k_mx_mr_spmv<1>": ("Msell32 + 2V32", Msell32 + 2 * V32), "k_mx_mr_update": ("5V32", 5 * V32),
+        "k_mx_cg_spmv<1>": ("Msell32 + 6V32", Msell32 + 6 * V32), "k_mx_cg_update": ("3V32", 3 * V32),
+        "k_mx_bcs_spmv1<1>": ("Msell32 + 3V32", Msell32 + 3 * V32),
+        "k_mx_bcs_spmv2<1>": ("Msell32 + 4V32", Msell32 + 4 * V32),
+        "k_mx_bcs_prep": ("4V32", 4 * V32), "k_mx_bcs_update": ("7V32", 7 * V32),
+        "k_mx_residual<1, 0>": ("Msell + 3V", Msell + 3 * V),
+        "k_mx_residual<1, 1>": ("Msell + 4V", Msell + 4 * V),
+        "k_mx_setup": ("V + 2V32", V + 2 * V32), "k_mx_correct": ("2V + V32", 2 * V + V32),
+        "k_mx_flush": ("3V32", 3 * V32),
+        "k_scaled_sell<float>": ("16S + V", 16 * S + V), "k_scaled_sell<double>": ("20S + V", 20 * S + V),
+        "k_spmv_sell": ("Msell + 2V", Msell + 2 * V),
+        "k_spmv_sell_ref": ("Msell + 4(N+1) + 2V", Msell + 4 * (N + 1) + 2 * V),
+        "k_adjoint_faces": ("24F + 2V", 24 * F + 2 * V), "k_adjoint_cells": ("3V", 3 * V),
+    }
+    return t
+
+
+def launch_table(csv_path: str, N: int = 2_097_152, F: int = 6_242_304, nnz: int = 14_581_760,
+                 S: int = 14_614_528, slices: int = 65_536) -> str:
+    """The markdown launch table of an ncu `gpu__time_duration.sum` CSV of
+    `--profile-all`: per kernel family its launches (working launches: those
+    of at least 40% of the family's longest -- host-driven loops launch
+    chunks whose steps after convergence return at once), total time,
+    share, mean working time, algorithmic bytes per launch and GB/s."""
+    import csv
+    import collections
+    rows = list(csv.reader(open(csv_path)))
+    hi = next(i for i, r in enumerate(rows) if r and r[0] == "ID")
+    h = rows[hi]
+    ki, vi, ui = h.index("Kernel Name"), h.index("Metric Value"), h.index("Metric Unit")
+    scale = {"ns": 1e-3, "nsecond": 1e-3, "us": 1.0, "usecond": 1.0, "ms": 1e3, "msecond": 1e3,
+             "s": 1e6, "second": 1e6}
+    times = collections.defaultdict(list)
+    for r in rows[hi + 1:]:
+        if len(r) <= vi or not r[vi]:
+            continue
+        name = r[ki].split("(")[0].replace("void ", "").replace("cf::", "").strip()
+        times[name].append(float(r[vi].replace(",", "")) * scale.get(r[ui], 1.0))
+    table = _launch_bytes(N, F, nnz, S, slices)
+    total = sum(sum(v) for v in times.values())
+    out = ["| kernel | launches (working) | total ms | share | mean µs (working) | "
+           "algorithmic bytes / launch | GB/s |", "|---|---|---|---|---|---|---|"]
+    for name, ts in sorted(times.items(), key=lambda kv: -sum(kv[1])):
+        work = [t for t in ts if t >= 0.4 * max(ts)]
+        mean = sum(work) / len(work)
+        label, nbytes = table.get(name, ("set-up / persistent (see note)", None))
+        gbs = f"{nbytes / (mean * 1e-6) / 1e9:,.0f}" if nbytes else "—"
+        lab = f"{label} = {nbytes / 1e6:.1f} MB" if nbytes else label
+        out.append(f"| `{name}` | {len(ts)} ({len(work)}) | {sum(ts) / 1e3:.3f} | "
+                   f"{100 * sum(ts) / total:.1f}% | {mean:,.2f} | {lab} | {gbs} |")
+    out.append(f"\n{len(times)} kernels, {total / 1e3:.1f} ms in total")
+    return "\n".join(out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1048,11 +1135,19 @@ def main():
                     help="short run launching every kernel family once, for an ncu launch list")
     ap.add_argument("--profile-mr", action="store_true",
                     help="short host-driven MR run (FP64 and mixed, 256^3) for an ncu capture")
+    ap.add_argument("--launch-table", metavar="CSV",
+                    help="print the markdown launch table of an ncu CSV of --profile-all")
+    ap.add_argument("--launch-sizes", metavar="N,F,NNZ,S,SLICES",
+                    help="system sizes for --launch-table (default: the 128^3 7-point system)")
     ap.add_argument("--profile-scaled", action="store_true",
                     help="6 Jacobi (FP64) and 6 mixed MRJacobi steps at 128^3, for an ncu capture")
     args = ap.parse_args()
     if args.profile_scaled:
         return run_profile_scaled(args)
+    if args.launch_table:
+        sizes = [int(v) for v in args.launch_sizes.split(",")] if args.launch_sizes else []
+        print(launch_table(args.launch_table, *sizes))
+        return 0
     if args.profile_mr:
         return run_profile_mr(args)
     if args.profile_all:
