@@ -1160,3 +1160,323 @@ int batch_systems(const Batch *B) { return (int)B->mats.size(); }
 int64_t batch_offset(const Batch *B, int s) { return B->offsets[s]; }
 
 } // namespace cf
+
+namespace cf {
+
+// ---------------------------------------------------------------------------
+// Jacobi, Richardson and the MR family on one small system in one
+// cluster-persistent launch (the CG kernel's schedule: one cluster of up to
+// 16 CTAs, rows split by 32-row slices, hardware cluster barriers where the
+// multi-kernel loop has kernel boundaries), fast summation order.  The
+// drivers are the reference's (SolverSingleGPU.h: Richardson 762-819 with
+// OptimizePower 723-752, MR 825-890, Jacobi 924-994, MRJacobi 1000-1073,
+// JMR 1079-1155, MRS 1236-1303); the stopping rule the library's.
+// ---------------------------------------------------------------------------
+struct SmallArgs {
+    const BatchSystem *sys;
+    int32_t solver;
+    int32_t max_iter;
+    double tolerance;
+    double omega;            // Richardson: 0 = the power method
+    int32_t power_steps;
+    const double *b;
+    double *x, *r, *d, *y;
+    const double *dinv, *dsq, *diag;
+    SmallSolveOut *out;
+};
+
+// all CTAs' values of one row owned by this thread, or 0
+template <class F>
+__device__ __forceinline__ void small_rows(int n, int s_lo, int s_hi, F f)
+{
+    constexpr int W = 256 / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int s = s_lo + warp; s < s_hi; s += W) {
+        const int row = s * 32 + lane;
+        f(s, row, row < n);
+    }
+}
+
+__global__ void __launch_bounds__(256, 1) k_small_solve(const SmallArgs a)
+{
+    cgp::cluster_group cl = cgp::this_cluster();
+    const int cs = (int)cl.num_blocks();
+    const int rank = (int)cl.block_rank();
+    __shared__ double wsm[3 * 8];
+    __shared__ double slot[2][3];
+    __shared__ double tot[3];
+    __shared__ BatchSystem S;
+    __shared__ double s_alpha, s_nrm, s_tol, s_omega;
+    __shared__ int s_act;
+    int parity = 0;
+    if (threadIdx.x == 0) S = *a.sys;
+    __syncthreads();
+    const int n = S.n;
+    const int ns = (n + 31) >> 5;
+    const int s_lo = (int)((int64_t)ns * rank / cs), s_hi = (int)((int64_t)ns * (rank + 1) / cs);
+    const int solver = a.solver;
+    const bool on[1] = {true};
+    double *x = a.x, *r = a.r, *d = a.d, *y = a.y;
+    const double *b = a.b;
+    auto gather = [](const double *v) {
+        return [v](int c, double(&o)[1]) { o[0] = __ldcg(v + c); };
+    };
+    auto reduce = [&](double (&acc)[1]) {
+        cluster_sum<1, 256>(cl, acc, wsm, slot[parity], tot);
+        parity ^= 1;
+        return tot[0];
+    };
+
+    // ---- normFactor and the initial residual -----------------------------
+    double acc1[1] = {0.0};
+    small_rows(n, s_lo, s_hi, [&](int, int row, bool ok) {
+        if (ok) acc1[0] += x[row];
+    });
+    const double xbar = reduce(acc1) / n;
+    {
+        double acc3[3] = {0.0, 0.0, 0.0};
+        small_rows(n, s_lo, s_hi, [&](int s, int row, bool ok) {
+            double yv[1], ys;
+            row_product<1, double, double>(S, S.s_val, S.val, s, row, on, gather(x), yv, ys);
+            if (ok) {
+                const double yb = ys * xbar, bi = b[row];
+                const double d1 = yv[0] - yb, d2 = bi - yb;
+                double ri = bi - yv[0];
+                if (solver == CF_JMR) ri = __dmul_rn(a.dsq[row], ri);
+                r[row] = ri;
+                acc3[0] = fma_t(d1, d1, acc3[0]);
+                acc3[1] = fma_t(d2, d2, acc3[1]);
+                acc3[2] = fma_t(ri, ri, acc3[2]);
+            }
+        });
+        cluster_sum<3, 256>(cl, acc3, wsm, slot[parity], tot);
+        parity ^= 1;
+    }
+    if (threadIdx.x == 0) {
+        const double nf = sqrt(tot[0]) + sqrt(tot[1]) + 1e-20;
+        s_tol = a.tolerance * nf;
+        s_nrm = sqrt(tot[2]);
+        s_omega = a.omega;
+        if (rank == 0) {
+            a.out->nf = nf;
+            a.out->norm0 = s_nrm;
+        }
+    }
+    __syncthreads();
+
+    // ---- Richardson's relaxation factor: OptimizePower on the system ------
+    if (solver == CF_RICHARDSON && s_omega > -1e-15 && s_omega < 1e-15) {
+        // x2 (in y) = 1/N; steps of x1 (in d) = x2, x2 = A x1 / ||A x1||
+        small_rows(n, s_lo, s_hi, [&](int, int row, bool ok) {
+            if (ok) y[row] = 1.0 / n;
+        });
+        for (int st = 0; st < a.power_steps; ++st) {
+            small_rows(n, s_lo, s_hi, [&](int, int row, bool ok) {
+                if (ok) d[row] = y[row];
+            });
+            cl.sync(); // every CTA's x1 rows are written before anyone gathers them
+            double acc[1] = {0.0};
+            small_rows(n, s_lo, s_hi, [&](int s, int row, bool ok) {
+                double yv[1], ys;
+                row_product<1, double, double>(S, S.s_val, S.val, s, row, on, gather(d), yv, ys);
+                if (ok) {
+                    y[row] = yv[0];
+                    acc[0] = fma_t(yv[0], yv[0], acc[0]);
+                }
+            });
+            const double inv = 1 / sqrt(reduce(acc));
+            small_rows(n, s_lo, s_hi, [&](int, int row, bool ok) {
+                if (ok) y[row] = __dmul_rn(y[row], inv);
+            });
+        }
+        cl.sync(); // x2 complete before anyone gathers it
+        double acc[1] = {0.0}, amin = HUGE_VAL;
+        small_rows(n, s_lo, s_hi, [&](int s, int row, bool ok) {
+            double yv[1], ys;
+            row_product<1, double, double>(S, S.s_val, S.val, s, row, on, gather(y), yv, ys);
+            if (ok) {
+                acc[0] = fma_t(y[row], yv[0], acc[0]);
+                amin = fmin(amin, fabs(a.diag[row]));
+            }
+        });
+        const double lmax = reduce(acc);
+        // the smallest |a_ii|: -max(-|a_ii|) through the same reduction slots
+        double m = -amin;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(kFull, m, o));
+        if ((threadIdx.x & 31) == 0) wsm[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double mm = wsm[0];
+            for (int w = 1; w < 8; ++w) mm = fmax(mm, wsm[w]);
+            slot[parity][0] = mm;
+        }
+        cl.sync();
+        if (threadIdx.x == 0) {
+            double mm = -HUGE_VAL;
+            for (int k = 0; k < cs; ++k) mm = fmax(mm, cl.map_shared_rank(slot[parity], k)[0]);
+            s_omega = 2.0 / (lmax + (-mm));
+            if (rank == 0) a.out->omega = s_omega;
+        }
+        parity ^= 1;
+        __syncthreads();
+    } else if (threadIdx.x == 0 && rank == 0) {
+        a.out->omega = s_omega;
+    }
+
+    // ---- the iterations ---------------------------------------------------
+    const double *w = solver == CF_MR ? nullptr : (solver == CF_JMR ? a.dsq : a.dinv);
+    int k = 0;
+    if (threadIdx.x == 0) s_act = isfinite(s_nrm) && a.max_iter >= 1 && s_nrm > s_tol;
+    __syncthreads();
+    while (s_act) {
+        ++k;
+        double acc[1] = {0.0};
+        if (solver == CF_RICHARDSON) {
+            const double om = s_omega;
+            small_rows(n, s_lo, s_hi, [&](int, int row, bool ok) {
+                if (ok) x[row] = fma_t(om, r[row], x[row]);
+            });
+            cl.sync(); // x complete before anyone gathers it
+            small_rows(n, s_lo, s_hi, [&](int s, int row, bool ok) {
+                double yv[1], ys;
+                row_product<1, double, double>(S, S.s_val, S.val, s, row, on, gather(x), yv, ys);
+                if (ok) {
+                    const double ri = b[row] - yv[0];
+                    r[row] = ri;
+                    acc[0] = fma_t(ri, ri, acc[0]);
+                }
+            });
+        } else {
+            // d = R r (MR: r itself), y = A d (JMR: D^-1/2 A d)
+            const double *dv = r;
+            if (w) {
+                small_rows(n, s_lo, s_hi, [&](int, int row, bool ok) {
+                    if (ok) d[row] = __dmul_rn(w[row], r[row]);
+                });
+                cl.sync(); // d complete before anyone gathers it
+                dv = d;
+            }
+            double t2[2] = {0.0, 0.0};
+            small_rows(n, s_lo, s_hi, [&](int s, int row, bool ok) {
+                double yv[1], ys;
+                row_product<1, double, double>(S, S.s_val, S.val, s, row, on, gather(dv), yv, ys);
+                if (ok) {
+                    double yi = yv[0];
+                    if (solver == CF_JMR) yi = __dmul_rn(a.dsq[row], yi);
+                    y[row] = yi;
+                    if (solver != CF_JACOBI) {
+                        t2[0] = fma_t(r[row], yi, t2[0]);
+                        t2[1] = fma_t(yi, yi, t2[1]);
+                    }
+                }
+            });
+            if (solver != CF_JACOBI) {
+                // every CTA has gathered r (MR) before anyone updates it
+                cluster_sum<2, 256>(cl, t2, wsm, slot[parity], tot, [&](int i, double v) {
+                    if (i == 1) s_alpha = tot[0] / v;
+                });
+                parity ^= 1;
+            } else if (threadIdx.x == 0) {
+                s_alpha = 1.0;
+            }
+            if (solver == CF_JACOBI) __syncthreads();
+            const double al = s_alpha;
+            small_rows(n, s_lo, s_hi, [&](int, int row, bool ok) {
+                if (ok) {
+                    x[row] = fma_t(al, dv[row], x[row]);
+                    const double ri = fma_t(-al, y[row], r[row]);
+                    r[row] = ri;
+                    acc[0] = fma_t(ri, ri, acc[0]);
+                }
+            });
+        }
+        const double nrm = sqrt(reduce(acc));
+        if (threadIdx.x == 0) {
+            s_nrm = nrm;
+            s_act = isfinite(nrm) && k < a.max_iter && nrm > s_tol;
+        }
+        __syncthreads();
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        a.out->norm = s_nrm;
+        a.out->iters = k;
+        a.out->status = !isfinite(s_nrm) ? CF_NONFINITE : (s_nrm > s_tol ? CF_NOT_CONVERGED : CF_OK);
+    }
+    cl.sync(); // no CTA leaves while a peer may still read its shared memory
+}
+
+SmallSolveResult solve_small_single_cluster(Matrix *m, int solver, const cf_controls &c, const double *b,
+                                            double *x, double *r, double *d, double *y)
+{
+    Context *ctx = m->ctx;
+    const int n = m->n;
+    const bool sell = matrix_ensure_sell(m, false, false);
+    struct Block {
+        BatchSystem sys;
+        SmallSolveOut out;
+    };
+    DeviceBuffer &blk = ctx->vec[23];
+    blk.ensure(sizeof(Block));
+    Block h{};
+    h.sys.n = n;
+    h.sys.sell = sell ? 1 : 0;
+    h.sys.ro = m->ro.as<int32_t>();
+    h.sys.col = m->col.as<int32_t>();
+    h.sys.val = m->val.as<double>();
+    h.sys.s_off = sell ? m->s_off.as<int32_t>() : nullptr;
+    h.sys.s_col = sell ? m->s_col.as<int32_t>() : nullptr;
+    h.sys.s_val = sell ? m->s_val.as<double>() : nullptr;
+    Block *dblk = blk.as<Block>();
+    CF_CUDA(cudaMemcpyAsync(dblk, &h, sizeof(Block), cudaMemcpyHostToDevice, ctx->stream));
+    SmallArgs a{};
+    a.sys = &dblk->sys;
+    a.solver = solver;
+    a.max_iter = c.max_iter <= 0 ? INT_MAX : c.max_iter;
+    a.tolerance = c.tolerance;
+    a.omega = c.richardson_omega;
+    a.power_steps = c.power_max_steps > 0 ? c.power_max_steps : 30;
+    a.b = b;
+    a.x = x;
+    a.r = r;
+    a.d = d;
+    a.y = y;
+    a.dinv = m->dinv.as<double>();
+    a.dsq = m->dinv_sqrt.as<double>();
+    a.diag = m->diag.as<double>();
+    a.out = &dblk->out;
+    int cs = 1;
+    while (cs < 16 && (int64_t)cs * CF_SMALL_CG_ROWS_PER_CTA < n) cs <<= 1;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(256);
+    cfg.gridDim = dim3(cs);
+    cfg.stream = ctx->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cs > 8)
+        CF_CUDA(cudaFuncSetAttribute((const void *)k_small_solve, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    CF_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
+    CF_CUDA(cudaLaunchKernelEx(&cfg, k_small_solve, a));
+    CF_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
+    SmallSolveOut res;
+    CF_CUDA(cudaMemcpyAsync(&res, &dblk->out, sizeof(res), cudaMemcpyDeviceToHost, ctx->stream));
+    CF_CUDA(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    CF_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+    SmallSolveResult o;
+    o.nf = res.nf;
+    o.norm0 = res.norm0;
+    o.norm = res.norm;
+    o.iters = res.iters;
+    o.status = res.status;
+    o.ms = ms;
+    o.omega = res.omega;
+    return o;
+}
+
+} // namespace cf

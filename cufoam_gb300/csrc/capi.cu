@@ -66,6 +66,7 @@ int Context::fast_grid(const void *kernel, size_t dyn_smem) const
 Context::~Context()
 {
     cudaSetDevice(device);
+    delete ldu_scratch;
     for (auto &kv : graphs) {
         if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
         if (kv.second.graph) cudaGraphDestroy(kv.second.graph);

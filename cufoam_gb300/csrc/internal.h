@@ -191,6 +191,11 @@ struct Context {
     int grid_cap = 0;
     int small_cg_ok = -1;      // 16-CTA clusters schedulable (-1: not asked yet)
 
+    // scratch of the matrix builds (grow-only: a conversion after the first
+    // allocates nothing) and the matrix of one-shot ldu2csr conversions
+    DeviceBuffer scratch_flag, scratch_tmp, scratch_cnt, scratch_stats;
+    struct Matrix *ldu_scratch = nullptr;
+
     int fast_grid(const void *kernel, size_t dyn_smem) const;
     ~Context();
 };
@@ -286,14 +291,22 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b, double 
 void solve_distributed(Matrix *m, int solver, const cf_controls &c, const cf_interfaces &ifc,
                        const cf_comm &comm, const double *b, double *x, cf_perf *perf);
 
-// CG on one small system in a single cluster-persistent launch (batched.cu)
+// CG, and Jacobi, Richardson and the MR family, on one small system in a
+// single cluster-persistent launch (batched.cu)
 struct SmallSolveResult {
     double nf, norm0, norm;
     int32_t iters, status;
     float ms;
+    double omega = 0.0;
+};
+struct SmallSolveOut {
+    double nf, norm0, norm, omega;
+    int32_t iters, status;
 };
 SmallSolveResult solve_cg_single_cluster(Matrix *m, const cf_controls &c, const double *b, double *x,
                                          double *r, double *p, double *q);
+SmallSolveResult solve_small_single_cluster(Matrix *m, int solver, const cf_controls &c, const double *b,
+                                            double *x, double *r, double *d, double *y);
 bool small_cg_ok(Context *ctx);
 
 struct Batch;

@@ -503,7 +503,7 @@ static int read_flag(Context *ctx, const int *d_flag)
 // chunk statistics of m's CSR pattern into m->max_chunk / m->has_long
 static void chunk_stats(Context *ctx, Matrix *m)
 {
-    DeviceBuffer buf;
+    DeviceBuffer &buf = ctx->scratch_stats;
     buf.ensure(2 * sizeof(int));
     CF_CUDA(cudaMemsetAsync(buf.ptr, 0, 2 * sizeof(int), ctx->stream));
     if (m->n > 0) {
@@ -520,7 +520,9 @@ static void chunk_stats(Context *ctx, Matrix *m)
 
 // Copies the LDU arrays to `m`, validates and completes the addressing,
 // builds the CSR.  When `out_*` are given the CSR is written there instead.
-static void build_from_ldu(Context *ctx, Matrix *m, const cf_ldu_view &v)
+// full = false: the CSR arrays only (a one-shot conversion), without the
+// staging statistics and the diagonal-derived vectors the solvers use
+static void build_from_ldu(Context *ctx, Matrix *m, const cf_ldu_view &v, bool full = true)
 {
     const int n = v.n_cells, nf = v.n_faces;
     require(n >= 0 && nf >= 0, CF_BAD_INPUT, "negative matrix size");
@@ -550,7 +552,7 @@ static void build_from_ldu(Context *ctx, Matrix *m, const cf_ldu_view &v)
     upload(ctx, m->la.ptr, v.lower_addr, sizeof(int32_t) * nf, v.memory);
     upload(ctx, m->ua.ptr, v.upper_addr, sizeof(int32_t) * nf, v.memory);
 
-    DeviceBuffer flag, tmp, cnt;
+    DeviceBuffer &flag = ctx->scratch_flag, &tmp = ctx->scratch_tmp, &cnt = ctx->scratch_cnt;
     flag.ensure(sizeof(int) * 4);
     CF_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int) * 4, ctx->stream));
     int *d_err = flag.as<int>();
@@ -618,6 +620,7 @@ static void build_from_ldu(Context *ctx, Matrix *m, const cf_ldu_view &v)
                                                    m->val.as<double>());
         CF_CHECK_LAUNCH();
     }
+    if (!full) return;
     // staging capacity and long rows
     chunk_stats(ctx, m);
     m->dinv.ensure(sizeof(double) * (n + pad));
@@ -732,12 +735,18 @@ void matrix_ensure_dmin(Matrix *m)
     m->have_dmin = true;
 }
 
+// The conversion runs in the context's scratch matrix, whose buffers only
+// grow: after the first call of a size a conversion allocates nothing
+// (device allocations and frees would dominate a small mesh's conversion).
 void ldu2csr_into(Context *ctx, const cf_ldu_view &v, int32_t *ro, int32_t *col, double *val,
                   int memory)
 {
-    Matrix tmp;
-    tmp.ctx = ctx;
-    build_from_ldu(ctx, &tmp, v);
+    if (!ctx->ldu_scratch) {
+        ctx->ldu_scratch = new Matrix();
+        ctx->ldu_scratch->ctx = ctx;
+    }
+    Matrix &tmp = *ctx->ldu_scratch;
+    build_from_ldu(ctx, &tmp, v, false);
     download(ctx, ro, tmp.ro.ptr, sizeof(int32_t) * (size_t)(tmp.n + 1), memory);
     download(ctx, col, tmp.col.ptr, sizeof(int32_t) * (size_t)tmp.nnz, memory);
     download(ctx, val, tmp.val.ptr, sizeof(double) * (size_t)tmp.nnz, memory);

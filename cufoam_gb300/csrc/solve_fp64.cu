@@ -636,14 +636,21 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     const bool hist_time = want_hist && c.history_time != 0;
     if (hist_time) ctx->hist_t.ensure(sizeof(unsigned long long) * (size_t)hist_cap);
 
-    // ---- a small system's CG: one cluster-persistent launch -------------
-    // (kernel boundaries, not bytes, set a small system's step time; the
-    // batched kernel runs the whole solve behind hardware cluster barriers)
-    if (solver == CF_CG && !ref && !mixed && !tr && n <= kSmallCgRows && !want_hist &&
+    // ---- a small system: one cluster-persistent launch -----------------
+    // (kernel boundaries, not bytes, set a small system's step time; CG runs
+    // in the batched kernel, Jacobi, Richardson and the MR family in
+    // k_small_solve, the whole solve behind hardware cluster barriers)
+    const bool small_kind = solver == CF_CG || solver == CF_JACOBI || solver == CF_RICHARDSON ||
+                            solver == CF_MR || solver == CF_MRJACOBI || solver == CF_MRS || solver == CF_JMR;
+    if (small_kind && !ref && !mixed && !tr && n <= kSmallCgRows && !want_hist &&
         c.time_limit_s <= 0 && c.profile_kernels == 0 && c.rel_tol == 0 && c.min_iter <= 0 &&
-        c.norm_type == CF_NORM_REFERENCE_L2 && !c.absolute_tolerance && small_cg_ok(ctx)) {
-        const SmallSolveResult R = solve_cg_single_cluster(m, c, b, x, ctx->vec[2].as<double>(),
-                                                           ctx->vec[4].as<double>(), ctx->vec[6].as<double>());
+        c.norm_type == CF_NORM_REFERENCE_L2 && !c.absolute_tolerance && c.use_graph != 0 && small_cg_ok(ctx)) {
+        const SmallSolveResult R =
+            solver == CF_CG
+                ? solve_cg_single_cluster(m, c, b, x, ctx->vec[2].as<double>(), ctx->vec[4].as<double>(),
+                                          ctx->vec[6].as<double>())
+                : solve_small_single_cluster(m, solver, c, b, x, ctx->vec[2].as<double>(),
+                                             ctx->vec[4].as<double>(), ctx->vec[6].as<double>());
         if (c.memory == CF_MEM_HOST) download(ctx, x_io, x, sizeof(double) * n, CF_MEM_HOST);
         CF_CUDA(cudaStreamSynchronize(ctx->stream));
         if (perf) {
@@ -657,6 +664,7 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
             perf->status = R.status;
             perf->solve_ms = R.ms;
             perf->true_residual = -1.0;
+            perf->omega = R.omega;
         }
         return;
     }

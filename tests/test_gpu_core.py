@@ -448,6 +448,65 @@ def test_small_system_cg_single_launch(ctx, case, fmt):
         assert true_rel <= 1.5 * tol
 
 
+SMALL_SOLVERS = ["cuFoamJacobi", "cuFoamRichardson", "cuFoamMR", "cuFoamMRJacobi", "cuFoamMRS", "cuFoamJMR"]
+_SMALL_WANT = {}
+
+
+def _small_case(name, case):
+    """(L, tol, maxit, b, oracle result, band), computed once per case; the
+    constant-coefficient 64^2 system's counts do not move under one-ulp
+    source changes, so two trials bound its band."""
+    key = (name, case)
+    if key not in _SMALL_WANT:
+        if case == "c1":
+            L, tol, maxit = O.grid_const(64, 64, 1), 1e-6, 40000
+        elif case == "const3d":
+            L, tol, maxit = O.grid_const(12, 12, 12), 1e-8, 40000
+        else:
+            L, tol, maxit = O.grid_convdiff(14, 12, 10, 5, 1.0)[0], 1e-8, 40000
+        kind = O.SOLVER_NAMES[name.replace("cuFoam", "")]
+        b = O.uniform(3, L.n)
+        want = O.plugin_solve(kind, L, b, np.zeros(L.n), tol, maxit)
+        band = reference_band(kind, L, b, np.zeros(L.n), tol, maxit, trials=2 if case == "c1" else 8)
+        _SMALL_WANT[key] = (L, tol, maxit, b, want, band)
+    return _SMALL_WANT[key]
+
+
+# (solver, system, format): the 64^2 system in SELL-32, the 3-D ones in both
+# formats; Richardson is registered for symmetric matrices only
+SMALL_CASES = [(name, case, fmt) for name in SMALL_SOLVERS
+               for case, fmt in (("c1", "sell"), ("const3d", "sell"), ("const3d", "csr"),
+                                 ("convdiff", "sell"), ("convdiff", "csr"))
+               if not (case == "convdiff" and name == "cuFoamRichardson")]
+
+
+@pytest.mark.parametrize("name,case,fmt", SMALL_CASES)
+def test_small_system_solvers_single_launch(ctx, name, case, fmt):
+    """Jacobi, Richardson and the MR family on a small system without a
+    residual history run as one cluster-persistent launch (k_small_solve):
+    the same normFactor and initial residual to rounding, iterations within
+    the reference's one-ulp band, Richardson's power-method factor to
+    rounding, the answer's true residual at the tolerance."""
+    import torch
+    L, tol, maxit, b, want, band = _small_case(name, case)
+    M = _matrix(ctx, L)
+    M.set_format(fmt)
+    for where in ("host", "device"):
+        psi = np.zeros(L.n) if where == "host" else torch.zeros(L.n, dtype=torch.float64, device="cuda")
+        src = b if where == "host" else torch.from_numpy(b).cuda()
+        perf = cf._TABLE[name]("p", M, {"tolerance": tol, "maxIter": maxit}).solve(psi, src)
+        out = psi if where == "host" else psi.cpu().numpy()
+        assert_fast_order_parity(perf, want, band, tol)
+        assert abs(perf.norm_factor - want.norm_factor) <= 1e-13 * want.norm_factor
+        assert abs(perf.initial_residual - want.initial_residual) <= 1e-13 * want.initial_residual
+        if name == "cuFoamRichardson":
+            assert perf.omega == pytest.approx(want.solve.omega, rel=1e-12)
+        assert perf.converged and perf.final_residual <= tol
+        if name != "cuFoamJMR":   # JMR's recorded residual is the scaled one
+            true_rel = O.true_residual_norm(O.ldu2csr(L), b, out) / perf.norm_factor
+            assert true_rel <= 1.5 * tol
+
+
 @pytest.mark.parametrize("offset", [0, 1])
 def test_cg_odd_size_and_unaligned_device_vectors(ctx, offset):
     """The fast CG prep pass takes element pairs as 16-byte loads when psi and
