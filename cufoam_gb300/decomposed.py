@@ -162,9 +162,15 @@ class ProcessorComm:
         self.group = group
         self.slices = []
         o = 0
+        seen = {}
         for p in patches:
             m = len(p.face_cells)
-            self.slices.append((int(p.neighbour), o, o + m))
+            nb = int(p.neighbour)
+            # the k-th patch to a neighbour sends with tag k, so that two
+            # patches between the same pair of ranks cannot be confused
+            tag = seen.get(nb, 0)
+            seen[nb] = tag + 1
+            self.slices.append((nb, o, o + m, tag))
             o += m
         self.n_faces = o
         self.error: BaseException | None = None
@@ -179,12 +185,12 @@ class ProcessorComm:
         dist = self._dist
         reqs = []
         keep = []
-        for nb, a, b in self.slices:
+        for nb, a, b, tag in self.slices:
             s = torch.from_numpy(np.ascontiguousarray(send[a:b]))
             t = torch.from_numpy(recv[a:b])
             keep += [s, t]
-            reqs.append(dist.isend(s, self._global(nb), group=self.group))
-            reqs.append(dist.irecv(t, self._global(nb), group=self.group))
+            reqs.append(dist.isend(s, self._global(nb), group=self.group, tag=tag))
+            reqs.append(dist.irecv(t, self._global(nb), group=self.group, tag=tag))
         for q in reqs:
             q.wait()
 

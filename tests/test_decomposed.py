@@ -295,3 +295,36 @@ def test_plugin_refuses_processor_patches_outside_a_parallel_run():
     fc, _ = sub.interface_arrays()
     rc, _, _, _ = processor_comm_check(sub, np.zeros(len(fc)), np.zeros(1))
     assert rc == 1
+
+
+def _two_patch_rank_main(rank, world, port, out_dir):
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    from cufoam_gb300.decomposed import ProcessorComm, ProcessorPatch
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        other = 1 - rank
+        # two patches between the same two ranks (as a processorCyclic patch
+        # beside a plain processor patch), of different sizes
+        patches = [ProcessorPatch(other, np.array([0, 1, 2], np.int32), np.ones(3), np.arange(3)),
+                   ProcessorPatch(other, np.array([3, 4], np.int32), np.ones(2), np.arange(3, 5))]
+        comm = ProcessorComm(patches)
+        send = 10.0 * rank + np.arange(5, dtype=np.float64)
+        recv = np.zeros(5)
+        comm.exchange(send, recv)
+        with open(os.path.join(out_dir, f"rank{rank}.json"), "w") as f:
+            json.dump({"recv": recv.tolist()}, f)
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_patches_to_one_neighbour_are_kept_apart(tmp_path):
+    import torch.multiprocessing as mp
+    mp.start_processes(_two_patch_rank_main, args=(2, _free_port(), str(tmp_path)), nprocs=2,
+                       start_method="spawn")
+    got = [json.load(open(tmp_path / f"rank{r}.json")) for r in range(2)]
+    assert got[0]["recv"] == [10.0, 11.0, 12.0, 13.0, 14.0]
+    assert got[1]["recv"] == [0.0, 1.0, 2.0, 3.0, 4.0]
