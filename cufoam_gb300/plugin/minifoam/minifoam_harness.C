@@ -9,8 +9,9 @@
 #include "../cuFoamGB300Comm.H"
 
 #include <cstring>
-#include <memory>
 #include <exception>
+#include <map>
+#include <memory>
 
 namespace Foam {
 FatalErrorType FatalError;
@@ -43,10 +44,12 @@ struct ProcessorPatches {
     {
         using namespace Foam;
         int o = 0;
+        std::map<int, int> per_neighbour;   // the k-th patch to a rank: tag k + 1
         for (int p = 0; p < cpl.n_proc; ++p) {
             const int m = cpl.proc_size[p];
+            const int tag = ++per_neighbour[cpl.proc_neighbour[p]];
             patches.emplace_back(new processorLduInterface(labelList(cpl.proc_cells + o, cpl.proc_cells + o + m),
-                                                           cpl.proc_neighbour[p]));
+                                                           cpl.proc_neighbour[p], tag));
             fields.emplace_back(new lduInterfaceField(*patches.back()));
             interfaces.push_back(fields.back().get());
             bou.push_back(scalarField(cpl.proc_coeffs + o, cpl.proc_coeffs + o + m));
