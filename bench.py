@@ -45,8 +45,10 @@ WORKLOAD = "poisson7_128^3_fp64_cuFoamCG_tol1e-8"
 # algorithmic bytes of the fused CG schedule (FP64 values, int32 indices)
 # ---------------------------------------------------------------------------
 # The iteration kernels stream the matrix in the format the library picked
-# for it (SELL-32 for this stencil: 12 B per stored entry incl. padding, one
-# int32 offset per 32-row slice); the set-up kernels read the CSR arrays.
+# for it (SELL-32 with one-byte column codes for this stencil: 9 B per
+# stored entry incl. padding, one int32 offset per 32-row slice, a 128 B
+# offset table; 12 B per entry with 32-bit columns); the set-up kernels read
+# the CSR arrays.
 # Every figure below counts each vector a kernel touches once.
 def csr_matrix_bytes(n: int, nnz: int) -> int:
     return 12 * nnz + 4 * (n + 1)
@@ -54,6 +56,26 @@ def csr_matrix_bytes(n: int, nnz: int) -> int:
 
 def sell_matrix_bytes(n: int, stored: int) -> int:
     return 12 * stored + 4 * ((n + 31) // 32 + 1)
+
+
+def sell8_matrix_bytes(n: int, stored: int) -> int:
+    """SELL-32 with one-byte column codes: 8 B value + 1 B code per stored
+    entry, one int32 offset per slice, the 32-entry offset table."""
+    return 9 * stored + 4 * ((n + 31) // 32 + 1) + 4 * 32
+
+
+def iter_matrix_bytes(fmt: str, n: int, nnz: int, stored: int, fp64_loop: bool = False) -> int:
+    """FP64 matrix bytes per pass of the fast kernels in the format in use.
+    fp64_loop: a pass of an FP64 solver loop, which reads the 32-bit columns
+    when the codes exist by default (the codes serve the plain product and
+    the FP32 sweeps)."""
+    if fmt == "sell8" and fp64_loop:
+        fmt = "sell"
+    if fmt == "sell8":
+        return sell8_matrix_bytes(n, stored)
+    if fmt == "sell":
+        return sell_matrix_bytes(n, stored)
+    return csr_matrix_bytes(n, nnz)
 
 
 def spmv_bytes(mat: int, n: int) -> int:
@@ -379,7 +401,7 @@ def suite_c2(ctx, device):
         M = cf.LduMatrix.from_ldu(L, ctx)
         n, _, nnz = M.shape()
         fmt, stored = M.format()
-        mat = sell_matrix_bytes(n, stored) if fmt == "sell" else csr_matrix_bytes(n, nnz)
+        mat = iter_matrix_bytes(fmt, n, nnz, stored, fp64_loop=True)
         res = {}
         for name, key, per in (("cuFoamCG", "cg", cg_iteration_bytes),
                                ("cuFoamJacobi", "jacobi", jacobi_step_bytes),
@@ -532,7 +554,8 @@ def run_ours(args):
     n, nf, nnz = M.shape()
     fmt, stored = M.format()
     mat_csr = csr_matrix_bytes(n, nnz)
-    mat_it = sell_matrix_bytes(n, stored) if fmt == "sell" else mat_csr
+    mat_it = iter_matrix_bytes(fmt, n, nnz, stored, fp64_loop=True)    # the CG loop's passes
+    mat_spmv = iter_matrix_bytes(fmt, n, nnz, stored)                  # the plain product
     src = torch.from_numpy(b).to(f"cuda:{device}")
     psi = torch.zeros(n, dtype=torch.float64, device=f"cuda:{device}")
     solver = cf.cuFoamCG("p", M, {"tolerance": TOL, "maxIter": MAX_ITER})
@@ -649,7 +672,7 @@ def run_ours(args):
     s1.record(stream)
     torch.cuda.synchronize()
     spmv_ms = s0.elapsed_time(s1) / reps
-    spmv_gbs = spmv_bytes(mat_it, n) / (spmv_ms * 1e-3) / 1e9
+    spmv_gbs = spmv_bytes(mat_spmv, n) / (spmv_ms * 1e-3) / 1e9
 
     if rank != 0:
         if dist:
@@ -691,7 +714,8 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "rows": n, "nnz": nnz, "faces": nf,
                    "iterations": iters, "tolerance": TOL, "reduction": "auto (fast for CG)",
-                   "spmv_format": fmt, "stored_entries": stored,
+                   "spmv_format": fmt, "cg_loop_format": "sell" if fmt == "sell8" else fmt,
+                   "stored_entries": stored,
                    "l2": f"inputs larger than L2 ({spmv_bytes(mat_it, n) / 1e6:.1f} MB per SpMV "
                          f"pass vs 129 MB L2)",
                    "parallelism": f"replicas x{world}",
@@ -1041,6 +1065,8 @@ def _launch_bytes(N, F, nnz, S, slices):
     Mcsr = 12 * nnz + 4 * (N + 1)
     Msell = 12 * S + 4 * (slices + 1)
     Msell32 = 8 * S + 4 * (slices + 1)
+    Msell8 = 9 * S + 4 * (slices + 1) + 128           # one-byte column codes (format 2)
+    Msell8_32 = 5 * S + 4 * (slices + 1) + 128
     t = {
         "k_pow_step": ("Mcsr + 2V", Mcsr + 2 * V), "k_pow_final": ("Mcsr + V", Mcsr + V),
         "k_bicg_spmv": ("Mcsr + 8nnz + 10V", Mcsr + 8 * nnz + 10 * V),
@@ -1079,6 +1105,23 @@ def _launch_bytes(N, F, nnz, S, slices):
         "k_spmv_sell_ref": ("Msell + 4(N+1) + 2V", Msell + 4 * (N + 1) + 2 * V),
         "k_adjoint_faces": ("24F + 2V", 24 * F + 2 * V), "k_adjoint_cells": ("3V", 3 * V),
     }
+    # the same passes over the one-byte column codes: format 2 in the kernel
+    # name, Msell8 (Msell8_32 for FP32 values) in place of Msell (Msell32)
+    for name, (formula, val) in list(t.items()):
+        if not (name.startswith("k_f_") or name.startswith("k_mx_")) or "Msell" not in formula:
+            continue
+        if name.startswith("k_mx_residual"):
+            n2 = name.replace("<1, ", "<2, ")
+        elif name.startswith("k_f_mr_spmv"):
+            n2 = name.replace(", 1>", ", 2>")
+        else:
+            n2 = name.replace("<1>", "<2>")
+        if "Msell32" in formula:
+            t[n2] = (formula.replace("Msell32", "Msell8_32"), val - Msell32 + Msell8_32)
+        else:
+            t[n2] = (formula.replace("Msell", "Msell8"), val - Msell + Msell8)
+    t["k_spmv_sell<SellCodes8>"] = ("Msell8 + 2V", Msell8 + 2 * V)
+    t["k_spmv_sell<SellCols32>"] = t["k_spmv_sell"]
     return t
 
 

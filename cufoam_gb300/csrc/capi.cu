@@ -5,9 +5,19 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <set>
 
+struct cf_matrix;
+struct cf_batch;
+
+// A context owns the device memory of the matrices and batches made on it:
+// cf_context_destroy releases it and leaves their handles orphaned (owner
+// null), so that a later cf_matrix_destroy / cf_batch_destroy -- in any
+// order, e.g. from a garbage collector -- only frees the handle.
 struct cf_context {
     cf::Context *impl;
+    std::set<cf_matrix *> matrices;
+    std::set<cf_batch *> batches;
 };
 
 struct cf_matrix {
@@ -335,6 +345,18 @@ cf_status cf_context_create(int32_t device, cf_context **out)
 void cf_context_destroy(cf_context *ctx)
 {
     if (!ctx) return;
+    cudaSetDevice(ctx->impl->device);
+    cudaStreamSynchronize(ctx->impl->stream);
+    for (cf_matrix *m : ctx->matrices) {
+        delete m->impl;
+        m->impl = nullptr;
+        m->owner = nullptr;
+    }
+    for (cf_batch *b : ctx->batches) {
+        cf::batch_destroy(b->impl);
+        b->impl = nullptr;
+        b->owner = nullptr;
+    }
     delete ctx->impl;
     delete ctx;
 }
@@ -381,6 +403,24 @@ cf_status cf_device_query(cf_context *ctx, cf_device_info *out)
     });
 }
 
+// a new matrix handle, registered with its context (or the matrix freed)
+static cf_status register_matrix(cf_context *ctx, cf::Matrix *m, cf_matrix **out)
+{
+    cf_matrix *h = new (std::nothrow) cf_matrix{m, ctx};
+    try {
+        if (h) ctx->matrices.insert(h);
+    } catch (...) {
+        delete h;
+        h = nullptr;
+    }
+    if (!h) {
+        delete m;
+        return CF_OUT_OF_MEMORY;
+    }
+    *out = h;
+    return CF_OK;
+}
+
 cf_status cf_matrix_create_ldu(cf_context *ctx, const cf_ldu_view *ldu, cf_matrix **out)
 {
     if (!ctx || !ldu || !out) return CF_BAD_INPUT;
@@ -393,12 +433,7 @@ cf_status cf_matrix_create_ldu(cf_context *ctx, const cf_ldu_view *ldu, cf_matri
         CF_CUDA(cudaStreamSynchronize(ctx->impl->stream));
     });
     if (st != CF_OK) return st;
-    *out = new (std::nothrow) cf_matrix{m, ctx};
-    if (!*out) {
-        delete m;
-        return CF_OUT_OF_MEMORY;
-    }
-    return CF_OK;
+    return register_matrix(ctx, m, out);
 }
 
 cf_status cf_matrix_create_csr(cf_context *ctx, int32_t n, int64_t nnz, const int32_t *row_offsets,
@@ -429,18 +464,13 @@ cf_status cf_matrix_create_csr(cf_context *ctx, int32_t n, int64_t nnz, const in
         }
     });
     if (st != CF_OK) return st;
-    *out = new (std::nothrow) cf_matrix{m, ctx};
-    if (!*out) {
-        delete m;
-        return CF_OUT_OF_MEMORY;
-    }
-    return CF_OK;
+    return register_matrix(ctx, m, out);
 }
 
 cf_status cf_matrix_update_values(cf_matrix *m, const double *diag, const double *lower,
                                   const double *upper, int32_t memory)
 {
-    if (!m) return CF_BAD_INPUT;
+    if (!m || !m->owner) return CF_BAD_INPUT;
     return guarded(m->owner, [&] {
         cf::require(memory == CF_MEM_HOST || memory == CF_MEM_DEVICE, CF_BAD_INPUT, "bad memory kind");
         cf::matrix_update_values(m->impl, diag, lower, upper, memory);
@@ -449,9 +479,10 @@ cf_status cf_matrix_update_values(cf_matrix *m, const double *diag, const double
 
 cf_status cf_matrix_set_format(cf_matrix *m, int32_t format)
 {
-    if (!m) return CF_BAD_INPUT;
+    if (!m || !m->owner) return CF_BAD_INPUT;
     return guarded(m->owner, [&] {
-        cf::require(format == CF_FORMAT_AUTO || format == CF_FORMAT_CSR || format == CF_FORMAT_SELL,
+        cf::require(format == CF_FORMAT_AUTO || format == CF_FORMAT_CSR || format == CF_FORMAT_SELL ||
+                        format == CF_FORMAT_SELL_C8,
                     CF_BAD_INPUT, "bad format");
         cf::Matrix *mi = m->impl;
         if (mi->format_request != format) {
@@ -465,11 +496,11 @@ cf_status cf_matrix_set_format(cf_matrix *m, int32_t format)
 
 cf_status cf_matrix_format(cf_matrix *m, int32_t *format, int64_t *stored_entries)
 {
-    if (!m) return CF_BAD_INPUT;
+    if (!m || !m->owner) return CF_BAD_INPUT;
     return guarded(m->owner, [&] {
         const bool sell = cf::matrix_ensure_sell(m->impl, false, false);
         CF_CUDA(cudaStreamSynchronize(m->owner->impl->stream));
-        if (format) *format = sell ? CF_FORMAT_SELL : CF_FORMAT_CSR;
+        if (format) *format = !sell ? CF_FORMAT_CSR : (m->impl->n_codes > 0 ? CF_FORMAT_SELL_C8 : CF_FORMAT_SELL);
         if (stored_entries) *stored_entries = sell ? m->impl->sell_nnz : m->impl->nnz;
     });
 }
@@ -477,15 +508,18 @@ cf_status cf_matrix_format(cf_matrix *m, int32_t *format, int64_t *stored_entrie
 void cf_matrix_destroy(cf_matrix *m)
 {
     if (!m) return;
-    cudaSetDevice(m->owner->impl->device);
-    cudaStreamSynchronize(m->owner->impl->stream);
-    delete m->impl;
+    if (m->owner) {   // else orphaned: its context already released the memory
+        cudaSetDevice(m->owner->impl->device);
+        cudaStreamSynchronize(m->owner->impl->stream);
+        delete m->impl;
+        m->owner->matrices.erase(m);
+    }
     delete m;
 }
 
 cf_status cf_matrix_shape(const cf_matrix *m, int32_t *n_rows, int32_t *n_faces, int64_t *nnz)
 {
-    if (!m) return CF_BAD_INPUT;
+    if (!m || !m->owner) return CF_BAD_INPUT;
     if (n_rows) *n_rows = m->impl->n;
     if (n_faces) *n_faces = m->impl->nf;
     if (nnz) *nnz = m->impl->nnz;
@@ -495,7 +529,7 @@ cf_status cf_matrix_shape(const cf_matrix *m, int32_t *n_rows, int32_t *n_faces,
 cf_status cf_matrix_export_csr(cf_matrix *m, int32_t transpose, int32_t *row_offsets, int32_t *cols,
                                double *vals, int32_t memory)
 {
-    if (!m || !row_offsets || !cols || !vals) return CF_BAD_INPUT;
+    if (!m || !m->owner || !row_offsets || !cols || !vals) return CF_BAD_INPUT;
     return guarded(m->owner, [&] {
         cf::Matrix *mm = m->impl;
         cf::Context *c = mm->ctx;
@@ -517,7 +551,7 @@ cf_status cf_ldu2csr(cf_context *ctx, const cf_ldu_view *ldu, int32_t *row_offse
 
 cf_status cf_spmv_async(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t row_order)
 {
-    if (!m || !x || !y) return CF_BAD_INPUT;
+    if (!m || !m->owner || !x || !y) return CF_BAD_INPUT;
     return guarded(m->owner, [&] {
         cf::spmv(m->impl, transpose != 0, x, y, row_order == CF_REDUCE_REFERENCE);
     });
@@ -526,7 +560,7 @@ cf_status cf_spmv_async(cf_matrix *m, int32_t transpose, const double *x, double
 cf_status cf_spmv(cf_matrix *m, int32_t transpose, const double *x, double *y, int32_t memory,
                   int32_t row_order)
 {
-    if (!m || !x || !y) return CF_BAD_INPUT;
+    if (!m || !m->owner || !x || !y) return CF_BAD_INPUT;
     return guarded(m->owner, [&] {
         cf::Matrix *mm = m->impl;
         cf::Context *c = mm->ctx;
@@ -549,7 +583,7 @@ cf_status cf_spmv(cf_matrix *m, int32_t transpose, const double *x, double *y, i
 cf_status cf_norm_factor(cf_matrix *m, const double *source, const double *psi, int32_t memory,
                          int32_t norm_type, int32_t reduction, double *out)
 {
-    if (!m || !source || !psi || !out) return CF_BAD_INPUT;
+    if (!m || !m->owner || !source || !psi || !out) return CF_BAD_INPUT;
     return guarded(m->owner, [&] {
         cf::Matrix *mm = m->impl;
         cf::Context *c = mm->ctx;
@@ -570,7 +604,7 @@ cf_status cf_norm_factor(cf_matrix *m, const double *source, const double *psi, 
 cf_status cf_solve(cf_matrix *m, int32_t solver, const cf_controls *controls, const double *source,
                    double *psi, cf_perf *perf)
 {
-    if (!m || !source || !psi) return CF_BAD_INPUT;
+    if (!m || !m->owner || !source || !psi) return CF_BAD_INPUT;
     cf_controls c;
     if (controls) c = *controls;
     else cf_controls_init(&c);
@@ -583,7 +617,7 @@ cf_status cf_solve_decomposed(cf_matrix *m, int32_t solver, const cf_controls *c
                               const cf_interfaces *interfaces, const cf_comm *comm, const double *source,
                               double *psi, cf_perf *perf)
 {
-    if (!m || !source || !psi || !interfaces || !comm) return CF_BAD_INPUT;
+    if (!m || !m->owner || !source || !psi || !interfaces || !comm) return CF_BAD_INPUT;
     cf_controls c;
     if (controls) c = *controls;
     else cf_controls_init(&c);
@@ -597,7 +631,7 @@ cf_status cf_solve_decomposed(cf_matrix *m, int32_t solver, const cf_controls *c
 cf_status cf_adjoint_gradients(cf_matrix *m, const double *lambda, const double *x,
                                double *d_diag, double *d_lower, double *d_upper, int32_t memory)
 {
-    if (!m || !lambda || !x) return CF_BAD_INPUT;
+    if (!m || !m->owner || !lambda || !x) return CF_BAD_INPUT;
     return guarded(m->owner, [&] {
         cf::Matrix *mm = m->impl;
         cf::Context *c = mm->ctx;
@@ -634,27 +668,37 @@ cf_status cf_batch_create(cf_context *ctx, int32_t n_systems, const cf_ldu_view 
     cf::Batch *b = nullptr;
     cf_status st = guarded(ctx, [&] { b = cf::batch_create(ctx->impl, n_systems, systems); });
     if (st != CF_OK) return st;
-    *out = new (std::nothrow) cf_batch{b, ctx};
-    if (!*out) {
+    cf_batch *h = new (std::nothrow) cf_batch{b, ctx};
+    try {
+        if (h) ctx->batches.insert(h);
+    } catch (...) {
+        delete h;
+        h = nullptr;
+    }
+    if (!h) {
         cf::batch_destroy(b);
         return CF_OUT_OF_MEMORY;
     }
+    *out = h;
     return CF_OK;
 }
 
 void cf_batch_destroy(cf_batch *b)
 {
     if (!b) return;
-    cudaSetDevice(b->owner->impl->device);
-    cudaStreamSynchronize(b->owner->impl->stream);
-    cf::batch_destroy(b->impl);
+    if (b->owner) {   // else orphaned: its context already released the memory
+        cudaSetDevice(b->owner->impl->device);
+        cudaStreamSynchronize(b->owner->impl->stream);
+        cf::batch_destroy(b->impl);
+        b->owner->batches.erase(b);
+    }
     delete b;
 }
 
 cf_status cf_batch_shape(const cf_batch *b, int32_t *n_systems, int64_t *total_rows,
                          int64_t *row_offsets)
 {
-    if (!b) return CF_BAD_INPUT;
+    if (!b || !b->owner) return CF_BAD_INPUT;
     const int s = cf::batch_systems(b->impl);
     if (n_systems) *n_systems = s;
     if (total_rows) *total_rows = cf::batch_rows(b->impl);
@@ -667,7 +711,7 @@ cf_status cf_batch_solve(cf_batch *b, int32_t solver, const cf_controls *control
                          const cf_batch_config *config, int32_t n_rhs, const double *sources,
                          double *psi, cf_batch_result *results, double *device_ms)
 {
-    if (!b || !sources || !psi) return CF_BAD_INPUT;
+    if (!b || !b->owner || !sources || !psi) return CF_BAD_INPUT;
     if (solver != CF_CG) return CF_UNSUPPORTED;
     cf_controls c;
     if (controls) c = *controls;

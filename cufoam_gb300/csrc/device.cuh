@@ -493,6 +493,60 @@ __device__ __forceinline__ int32_t ld_stream(const int32_t *p, uint64_t pol)
     asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
     return v;
 }
+__device__ __forceinline__ uint32_t ld_stream(const uint8_t *p, uint64_t pol)
+{
+    uint32_t v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u8 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+// Column indices of a SELL-32 copy, read slot by slot.  SellCols32 holds
+// the 32-bit column of every slot.  SellCodes8 holds one byte per slot: an
+// index into a table of the pattern's distinct offsets col - row (at most
+// kMaxCodes; a 7-point stencil has 7, a 27-point one 27), so a slot costs 1
+// byte instead of 4: 9 instead of 12 bytes per FP64 entry, 5 instead of 8
+// per FP32 entry.  A padding slot holds offset 0 from its row base rb -- the
+// row itself, or column 0 for the rows past n of the last slice -- which is
+// the column the 32-bit copy stores there, so both give the same gathers
+// and the same sums.
+//
+// Lane l keeps table entry l in a register and a code is decoded by a warp
+// shuffle (col(), called by all 32 lanes together).  Measured on GB300
+// against an L1-cached table load and a select tree over eight registers
+// (7-point systems): plain FP64 SpMV at 128^3 33.2 us (table 37.2, select
+// tree 36.4, 32-bit columns 35.7), FP32 MR step at 256^3 214 us (224, 228;
+// 237).  A row longer than 32 entries has more than 32 offsets, so
+// matrices with long rows keep 32-bit columns; col_div() (any lanes) reads
+// the table from memory.
+constexpr int kMaxCodes = 32;
+
+struct SellCols32 {
+    using raw_t = int32_t;
+    const int32_t *p;
+    __device__ __forceinline__ int32_t load(int64_t o, uint64_t pol) const { return ld_stream(p + o, pol); }
+    __device__ __forceinline__ int32_t plain(int64_t o) const { return p[o]; }
+    __device__ __forceinline__ int col(int32_t raw, int) const { return raw; }
+    __device__ __forceinline__ int col_div(int32_t raw, int) const { return raw; }
+    __device__ __forceinline__ const void *addr(int64_t o) const { return p + o; }
+};
+struct SellCodes8 {
+    using raw_t = uint32_t;
+    const uint8_t *p;
+    const int32_t *tab;  // offsets col - row (kMaxCodes entries, unused ones 0)
+    int treg;            // tab[lane]
+    __device__ __forceinline__ SellCodes8(const uint8_t *p_, const int32_t *tab_)
+        : p(p_), tab(tab_), treg(__ldg(tab_ + (threadIdx.x & 31)))
+    {
+    }
+    __device__ __forceinline__ uint32_t load(int64_t o, uint64_t pol) const { return ld_stream(p + o, pol); }
+    __device__ __forceinline__ uint32_t plain(int64_t o) const { return p[o]; }
+    __device__ __forceinline__ int col(uint32_t raw, int rb) const { return rb + __shfl_sync(kFull, treg, (int)raw); }
+    __device__ __forceinline__ int col_div(uint32_t raw, int rb) const { return rb + __ldg(tab + raw); }
+    __device__ __forceinline__ const void *addr(int64_t o) const { return p + o; }
+};
+
+// the row base a slot's code is relative to: the row, or 0 past n
+__device__ __forceinline__ int sell_row_base(int row, int n) { return row < n ? row : 0; }
 
 __device__ __forceinline__ void prefetch_l2(const void *p)
 {
@@ -505,9 +559,9 @@ __device__ __forceinline__ void prefetch_l2(const void *p)
 // loads after the wait hit L2.  Only for matrices with more slices than
 // the grid has warps: the slice offset it must load first would otherwise
 // lengthen the short steps of a small system (64^2 Jacobi: 8.0 -> 8.4 us).
-template <class V>
-__device__ __forceinline__ void sell_prefetch_first(int n_slices, const int32_t *__restrict__ off,
-                                                    const int32_t *__restrict__ col, const V *__restrict__ val)
+template <class C, class V>
+__device__ __forceinline__ void sell_prefetch_first(int n_slices, const int32_t *__restrict__ off, const C &cs,
+                                                    const V *__restrict__ val)
 {
     const int s = blockIdx.x * kWarps + (threadIdx.x >> 5);
     if (n_slices <= (int)gridDim.x * kWarps) return;
@@ -516,55 +570,64 @@ __device__ __forceinline__ void sell_prefetch_first(int n_slices, const int32_t 
     const int len = (__ldg(off + s + 1) - b) >> 5;
     const int m = len < 8 ? len : 8;
     for (int u = 0; u < m; ++u) {
-        prefetch_l2(col + b + lane + 32 * u);
+        prefetch_l2(cs.addr(b + lane + 32 * u));
         prefetch_l2(val + b + lane + 32 * u);
     }
 }
 
-// M entries of a SELL row (slots 32 elements apart): all loads and gathers
-// issued before the first FMA, then one FMA chain in slot order.
-template <class V, int M, class G>
-__device__ __forceinline__ void sell_batch(const int32_t *cp, const V *vp, uint64_t pol, G g, V &acc)
+// M entries of a SELL row (slots 32 elements apart, the first at element o
+// of the column and value arrays): all loads and gathers issued before the
+// first FMA, then one FMA chain in slot order.
+template <class V, int M, class C, class G>
+__device__ __forceinline__ void sell_batch(const C &cs, int64_t o, int rb, const V *vp, uint64_t pol, G g, V &acc)
 {
-    int c[M];
+    typename C::raw_t c[M];
     V v[M], x[M];
 #pragma unroll
     for (int u = 0; u < M; ++u) {
-        c[u] = ld_stream(cp + 32 * u, pol);
+        c[u] = cs.load(o + 32 * u, pol);
         v[u] = ld_stream(vp + 32 * u, pol);
     }
 #pragma unroll
-    for (int u = 0; u < M; ++u) x[u] = g(c[u]);
+    for (int u = 0; u < M; ++u) x[u] = g(cs.col(c[u], rb));
 #pragma unroll
     for (int u = 0; u < M; ++u) acc = fma_t(v[u], x[u], acc);
 }
 
 // the last r < B entries of a row as one exact batch
-template <class V, int B, class G>
-__device__ __forceinline__ void sell_tail(int r, const int32_t *cp, const V *vp, uint64_t pol, G g, V &acc)
+template <class V, int B, class C, class G>
+__device__ __forceinline__ void sell_tail(int r, const C &cs, int64_t o, int rb, const V *vp, uint64_t pol, G g,
+                                          V &acc)
 {
     if constexpr (B > 1) {
         if (r == B - 1) {
-            sell_batch<V, B - 1>(cp, vp, pol, g, acc);
+            sell_batch<V, B - 1>(cs, o, rb, vp, pol, g, acc);
             return;
         }
-        sell_tail<V, B - 1>(r, cp, vp, pol, g, acc);
+        sell_tail<V, B - 1>(r, cs, o, rb, vp, pol, g, acc);
     }
 }
 
 // A slice's rows longer than kLongRow (row lengths from the CSR offsets
 // `ro`) summed by the whole warp over their own slots, the bits of the CSR
-// passes (warp_row); `acc` is this lane's sum, replaced for those lanes.
-template <class V, class G>
-__device__ __forceinline__ void sell_long_rows(int n, int s, const int32_t *__restrict__ ro,
-                                               const int32_t *cp0, const V *vp0, G g, V &acc)
+// passes (warp_row: lane j takes slots j, j + 32, ... as one FMA chain,
+// then the xor-shuffle tree); `acc` is this lane's sum, replaced for those
+// lanes.  b is the slice's first element, vp0 its first value.
+template <class V, class C, class G>
+__device__ __forceinline__ void sell_long_rows(int n, int s, const int32_t *__restrict__ ro, const C &cs,
+                                               int64_t b, const V *vp0, G g, V &acc)
 {
     const int lane = threadIdx.x & 31;
     const int row = s * 32 + lane;
     const int rl = row < n ? __ldg(ro + row + 1) - __ldg(ro + row) : 0;
     for (unsigned m = __ballot_sync(kFull, rl > kLongRow); m; m &= m - 1) {
         const int r = __ffs(m) - 1;
-        const V v = warp_row(cp0 + r, vp0 + r, __shfl_sync(kFull, rl, r), 32, g);
+        const int len = __shfl_sync(kFull, rl, r);
+        const int rb = s * 32 + r;
+        V a = V(0);
+        for (int t = lane; t < len; t += 32)
+            a = fma_t(vp0[r + (int64_t)32 * t], g(cs.col_div(cs.plain(b + r + (int64_t)32 * t), rb)), a);
+        const V v = warp_sum(a);
         if (lane == r) acc = v;
     }
 }
@@ -575,11 +638,12 @@ __device__ __forceinline__ void sell_long_rows(int n, int s, const int32_t *__re
 // of a full batch would still issue its FMA (measured: 9 DFMA per 7-entry
 // row).  The slice length is warp-uniform, so the branches never diverge.
 // Matrices with rows longer than kLongRow (has_long) sum those rows with
-// the whole warp (sell_long_rows), as the CSR passes do.
-template <class V, int B, class G, class F>
-__device__ __forceinline__ void sell_rows(int n, int n_slices, const int32_t *__restrict__ off,
-                                          const int32_t *__restrict__ col, const V *__restrict__ val,
-                                          const int32_t *__restrict__ ro, bool has_long, G g, F f)
+// the whole warp (sell_long_rows), as the CSR passes do.  cs: the columns
+// (SellCols32 or SellCodes8).
+template <class V, int B, class C, class G, class F>
+__device__ __forceinline__ void sell_rows(int n, int n_slices, const int32_t *__restrict__ off, const C &cs,
+                                          const V *__restrict__ val, const int32_t *__restrict__ ro,
+                                          bool has_long, G g, F f)
 {
     const uint64_t pol = l2_evict_first_policy();
     const int lane = threadIdx.x & 31;
@@ -587,24 +651,24 @@ __device__ __forceinline__ void sell_rows(int n, int n_slices, const int32_t *__
     for (int s = blockIdx.x * kWarps + (threadIdx.x >> 5); s < n_slices; s += nw) {
         const int b = __ldg(off + s);
         const int len = (__ldg(off + s + 1) - b) >> 5;
-        const int32_t *cp = col + b + lane;
-        const V *vp = val + b + lane;
+        const int row = s * 32 + lane;
+        const int rb = sell_row_base(row, n);
+        const int64_t o = (int64_t)b + lane;
+        const V *vp = val + o;
         V acc = V(0);
         int t0 = 0;
-        for (; t0 + B <= len; t0 += B) sell_batch<V, B>(cp + 32 * t0, vp + 32 * t0, pol, g, acc);
-        sell_tail<V, B>(len - t0, cp + 32 * t0, vp + 32 * t0, pol, g, acc);
-        if (has_long) sell_long_rows(n, s, ro, col + b, val + b, g, acc);
-        const int row = s * 32 + lane;
+        for (; t0 + B <= len; t0 += B) sell_batch<V, B>(cs, o + 32 * t0, rb, vp + 32 * t0, pol, g, acc);
+        sell_tail<V, B>(len - t0, cs, o + 32 * t0, rb, vp + 32 * t0, pol, g, acc);
+        if (has_long) sell_long_rows(n, s, ro, cs, b, val + b, g, acc);
         if (row < n) f(row, acc);
     }
 }
 
 // Two products over one SELL pattern (A and A^T values): f(row, y1, y2).
-template <class V, int B, class G1, class G2, class F>
-__device__ __forceinline__ void sell_rows2(int n, int n_slices, const int32_t *__restrict__ off,
-                                           const int32_t *__restrict__ col, const V *__restrict__ val1,
-                                           const V *__restrict__ val2, const int32_t *__restrict__ ro,
-                                           bool has_long, G1 g1, G2 g2, F f)
+template <class V, int B, class C, class G1, class G2, class F>
+__device__ __forceinline__ void sell_rows2(int n, int n_slices, const int32_t *__restrict__ off, const C &cs,
+                                           const V *__restrict__ val1, const V *__restrict__ val2,
+                                           const int32_t *__restrict__ ro, bool has_long, G1 g1, G2 g2, F f)
 {
     const uint64_t pol = l2_evict_first_policy();
     const int lane = threadIdx.x & 31;
@@ -612,25 +676,28 @@ __device__ __forceinline__ void sell_rows2(int n, int n_slices, const int32_t *_
     for (int s = blockIdx.x * kWarps + (threadIdx.x >> 5); s < n_slices; s += nw) {
         const int b = __ldg(off + s);
         const int len = (__ldg(off + s + 1) - b) >> 5;
-        const int32_t *cp = col + b + lane;
-        const V *vp1 = val1 + b + lane;
-        const V *vp2 = val2 + b + lane;
+        const int row = s * 32 + lane;
+        const int rb = sell_row_base(row, n);
+        const int64_t o = (int64_t)b + lane;
+        const V *vp1 = val1 + o;
+        const V *vp2 = val2 + o;
         V a1 = V(0), a2 = V(0);
         for (int t0 = 0; t0 < len; t0 += B) {
-            int c[B];
+            typename C::raw_t c[B];
             V v1[B], v2[B], x1[B], x2[B];
 #pragma unroll
             for (int u = 0; u < B; ++u)
                 if (t0 + u < len) {
-                    c[u] = ld_stream(cp + 32 * (t0 + u), pol);
+                    c[u] = cs.load(o + 32 * (t0 + u), pol);
                     v1[u] = ld_stream(vp1 + 32 * (t0 + u), pol);
                     v2[u] = ld_stream(vp2 + 32 * (t0 + u), pol);
                 }
 #pragma unroll
             for (int u = 0; u < B; ++u)
                 if (t0 + u < len) {
-                    x1[u] = g1(c[u]);
-                    x2[u] = g2(c[u]);
+                    const int cc = cs.col(c[u], rb);
+                    x1[u] = g1(cc);
+                    x2[u] = g2(cc);
                 }
 #pragma unroll
             for (int u = 0; u < B; ++u)
@@ -640,10 +707,9 @@ __device__ __forceinline__ void sell_rows2(int n, int n_slices, const int32_t *_
                 }
         }
         if (has_long) {
-            sell_long_rows(n, s, ro, col + b, val1 + b, g1, a1);
-            sell_long_rows(n, s, ro, col + b, val2 + b, g2, a2);
+            sell_long_rows(n, s, ro, cs, b, val1 + b, g1, a1);
+            sell_long_rows(n, s, ro, cs, b, val2 + b, g2, a2);
         }
-        const int row = s * 32 + lane;
         if (row < n) f(row, a1, a2);
     }
 }

@@ -98,6 +98,8 @@ struct SolveArgs {
     int32_t has_long;          // some row has more than kLongRow entries (device.cuh)
     const int32_t *s_off;      // [n_slices + 1] element offset of each slice
     const int32_t *s_col;
+    const uint8_t *s_code;     // one-byte column codes of the same slots (null: none)
+    const int32_t *s_dtab;     // [256] offsets col - row the codes stand for
     const double *s_val;
     const double *s_valT;
     const float *s_val32;
@@ -194,6 +196,7 @@ struct Context {
     // scratch of the matrix builds (grow-only: a conversion after the first
     // allocates nothing) and the matrix of one-shot ldu2csr conversions
     DeviceBuffer scratch_flag, scratch_tmp, scratch_cnt, scratch_stats;
+    DeviceBuffer scratch_codes;   // offset set of the one-byte column codes (matrix.cu)
     struct Matrix *ldu_scratch = nullptr;
 
     int fast_grid(const void *kernel, size_t dyn_smem) const;
@@ -250,6 +253,10 @@ struct Matrix {
     int32_t n_slices = 0;
     int64_t sell_nnz = 0;      // stored entries including padding
     DeviceBuffer s_off, s_col, s_val, s_valT, s_val32, s_valT32;
+    // one-byte column codes of the SELL-32 slots and the table of offsets
+    // col - row they index (n_codes distinct offsets; 0: 32-bit columns only)
+    DeviceBuffer s_code, s_dtab;
+    int32_t n_codes = 0;
     bool have_sval = false, have_svalT = false, have_sval32 = false, have_svalT32 = false;
     // bumped by every change of the values, of 1/a_ii or of the format
     uint64_t gen = 1;

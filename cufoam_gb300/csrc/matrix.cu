@@ -8,6 +8,7 @@
 // (relative to the first entries), which is the reference's running count.
 #include "device.cuh"
 
+#include <algorithm>
 #include <cmath>
 
 namespace cf {
@@ -337,6 +338,82 @@ __global__ void k_sell_fill(int n, int n_slices, const int32_t *__restrict__ ro,
     }
 }
 
+// One-byte column codes of the SELL-32 slots (SellCodes8, device.cuh): the
+// distinct offsets d = col - row of the CSR entries, and 0 (the padding
+// slots' offset), go into an open-addressing set on the device while the
+// SELL-32 layout is sized; when there are at most kMaxCodes of them the host
+// numbers them in ascending order and a pass over the slots writes each
+// slot's number.
+constexpr int kCodeHash = 1024;              // slots of the set (power of two, > 2 kMaxCodes)
+constexpr int kCodeTable = kMaxCodes;        // entries of the offset table (unused ones 0)
+constexpr int32_t kNoOffset = INT32_MIN;     // empty slot (|d| < n < 2^31)
+
+__device__ __forceinline__ uint32_t offset_hash(int32_t d) { return ((uint32_t)d * 2654435761u) >> 22; }
+
+// d into the set; every probe sequence ends within kCodeHash steps
+__device__ void offset_insert(int32_t *keys, int32_t *count, int32_t d)
+{
+    uint32_t h = offset_hash(d);
+    for (int probe = 0; probe < kCodeHash; ++probe, h = (h + 1) & (kCodeHash - 1)) {
+        const int32_t k = *(volatile int32_t *)(keys + h);
+        if (k == d) return;
+        if (k == kNoOffset) {
+            const int32_t old = atomicCAS(keys + h, kNoOffset, d);
+            if (old == kNoOffset) {
+                atomicAdd(count, 1);
+                return;
+            }
+            if (old == d) return;
+        }
+    }
+}
+
+// keys = empty, count = 0
+__global__ void k_offsets_clear(int32_t *keys, int32_t *count)
+{
+    CF_FOR_ELEMS(i, kCodeHash) keys[i] = kNoOffset;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *count = 0;
+}
+
+// every CSR entry's offset, and 0; stops early once more than kMaxCodes
+// distinct offsets are in the set (the codes cannot be used then)
+__global__ void k_csr_offsets(int n, const int32_t *__restrict__ ro, const int32_t *__restrict__ col,
+                              int32_t *keys, int32_t *count)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) offset_insert(keys, count, 0);
+    CF_FOR_ELEMS(i, n) {
+        int32_t last = kNoOffset;
+        const int re = ro[i + 1];
+        for (int j = ro[i]; j < re; ++j) {
+            if (*(volatile int32_t *)count > kMaxCodes) return;
+            const int32_t d = col[j] - i;
+            if (d == last) continue;
+            last = d;
+            offset_insert(keys, count, d);
+        }
+    }
+}
+
+// each slot's code: the number of its offset (slot_code, by set position);
+// every offset is in the set, found within kCodeHash probes
+__global__ void k_sell_encode(int n, int n_slices, const int32_t *__restrict__ soff,
+                              const int32_t *__restrict__ scol, const int32_t *__restrict__ keys,
+                              const uint8_t *__restrict__ slot_code, uint8_t *code)
+{
+    CF_FOR_ELEMS(i, 32 * n_slices) {
+        const int s = i >> 5, lane = i & 31;
+        const int b = soff[s], len = (soff[s + 1] - b) >> 5;
+        const int rb = sell_row_base(i, n);
+        for (int t = 0; t < len; ++t) {
+            const int o = b + 32 * t + lane;
+            const int32_t d = scol[o] - rb;
+            uint32_t h = offset_hash(d);
+            for (int probe = 0; probe < kCodeHash && keys[h] != d; ++probe) h = (h + 1) & (kCodeHash - 1);
+            code[o] = slot_code[h];
+        }
+    }
+}
+
 // y = A x over the SELL-32 copy (the fast order of k_spmv_fast).  Entries
 // per batch and resident blocks per SM (0: no register constraint) are
 // tuning constants; measured on the 7-point 128^3 product (100 launches
@@ -353,15 +430,20 @@ __global__ void k_sell_fill(int n, int n_slices, const int32_t *__restrict__ ro,
 #else
 #define CF_PLAIN_SPMV_BOUNDS __launch_bounds__(kBlock)
 #endif
+// (CODES: the columns from the one-byte codes and their offset table)
+template <bool CODES>
 __global__ void CF_PLAIN_SPMV_BOUNDS k_spmv_sell(int n, int n_slices, const int32_t *__restrict__ off,
-                                                      const int32_t *__restrict__ col,
-                                                      const double *__restrict__ val,
-                                                      const int32_t *__restrict__ ro, int has_long,
-                                                      const double *__restrict__ x, double *y)
+                                                 const int32_t *__restrict__ col, const uint8_t *__restrict__ code,
+                                                 const int32_t *__restrict__ tab, const double *__restrict__ val,
+                                                 const int32_t *__restrict__ ro, int has_long,
+                                                 const double *__restrict__ x, double *y)
 {
-    sell_rows<double, CF_PLAIN_SPMV_BATCH>(n, n_slices, off, col, val, ro, has_long != 0,
-                                           [&](int c) { return __ldg(x + c); },
-                                           [&](int row, double v) { y[row] = v; });
+    auto g = [&](int c) { return __ldg(x + c); };
+    auto f = [&](int row, double v) { y[row] = v; };
+    if constexpr (CODES)
+        sell_rows<double, CF_PLAIN_SPMV_BATCH>(n, n_slices, off, SellCodes8(code, tab), val, ro, has_long != 0, g, f);
+    else
+        sell_rows<double, CF_PLAIN_SPMV_BATCH>(n, n_slices, off, SellCols32{col}, val, ro, has_long != 0, g, f);
 }
 
 // ---------------------------------------------------------------------------
@@ -478,6 +560,55 @@ static int grid_for(Context *ctx, int64_t work, int per_block = kBlock)
     if (g > cap) g = cap;
     if (g < 1) g = 1;
     return (int)g;
+}
+
+// The offset set of m's pattern (one-byte column codes) into the context's
+// scratch: keys [kCodeHash], count, then the slot -> code map [kCodeHash]
+// bytes.  Enqueued only; read back with the SELL-32 size.
+static void queue_offsets(Matrix *m)
+{
+    Context *ctx = m->ctx;
+    ctx->scratch_codes.ensure(sizeof(int32_t) * (kCodeHash + 4) + kCodeHash);
+    int32_t *keys = ctx->scratch_codes.as<int32_t>();
+    k_offsets_clear<<<grid_for(ctx, kCodeHash), kBlock, 0, ctx->stream>>>(keys, keys + kCodeHash);
+    CF_CHECK_LAUNCH();
+    k_csr_offsets<<<grid_for(ctx, m->n), kBlock, 0, ctx->stream>>>(m->n, m->ro.as<int32_t>(), m->col.as<int32_t>(),
+                                                                  keys, keys + kCodeHash);
+    CF_CHECK_LAUNCH();
+}
+
+// The codes of m's SELL-32 copy from the offset set read back into hk /
+// count, when the pattern has at most kMaxCodes distinct offsets (m->n_codes
+// > 0 then).  Asynchronous: the host tables are staged by the copies.
+static void build_sell_codes(Matrix *m, const std::vector<int32_t> &hk, int32_t count)
+{
+    Context *ctx = m->ctx;
+    m->n_codes = 0;
+    if (count <= 0 || count > kMaxCodes) return;
+    std::vector<int32_t> offs;
+    for (int32_t k : hk)
+        if (k != kNoOffset) offs.push_back(k);
+    if ((int)offs.size() != count) return;
+    std::sort(offs.begin(), offs.end());
+    std::vector<int32_t> tab(kCodeTable, 0);
+    std::copy(offs.begin(), offs.end(), tab.begin());
+    std::vector<uint8_t> slot_code(kCodeHash, 0);
+    for (int h = 0; h < kCodeHash; ++h)
+        if (hk[h] != kNoOffset)
+            slot_code[h] = (uint8_t)(std::lower_bound(offs.begin(), offs.end(), hk[h]) - offs.begin());
+    int32_t *keys = ctx->scratch_codes.as<int32_t>();
+    uint8_t *map = reinterpret_cast<uint8_t *>(keys + kCodeHash + 4);
+    m->s_dtab.ensure(sizeof(int32_t) * kCodeTable);
+    m->s_code.ensure((size_t)m->sell_nnz + 64);
+    // pageable sources: each copy returns once its bytes are staged
+    CF_CUDA(cudaMemcpyAsync(m->s_dtab.ptr, tab.data(), sizeof(int32_t) * kCodeTable, cudaMemcpyHostToDevice,
+                            ctx->stream));
+    CF_CUDA(cudaMemcpyAsync(map, slot_code.data(), kCodeHash, cudaMemcpyHostToDevice, ctx->stream));
+    const int ns = m->n_slices;
+    k_sell_encode<<<grid_for(ctx, 32 * (int64_t)ns), kBlock, 0, ctx->stream>>>(
+        m->n, ns, m->s_off.as<int32_t>(), m->s_col.as<int32_t>(), keys, map, m->s_code.as<uint8_t>());
+    CF_CHECK_LAUNCH();
+    m->n_codes = count;
 }
 
 static void exclusive_scan(Context *ctx, int m, const int32_t *in, int32_t *out, DeviceBuffer &tmp)
@@ -902,15 +1033,21 @@ bool matrix_ensure_sell(Matrix *m, bool transpose, bool fp32)
             k_sell_len<<<grid_for(ctx, (int64_t)ns + 1), kBlock, 0, ctx->stream>>>(
                 m->n, ns, m->ro.as<int32_t>(), slen.as<int32_t>(), tot.as<unsigned long long>());
             CF_CHECK_LAUNCH();
+            const bool want_codes = m->format_request != CF_FORMAT_SELL;
+            if (want_codes) queue_offsets(m);
             unsigned long long total = 0;
+            std::vector<int32_t> hk(want_codes ? kCodeHash + 1 : 0);
             CF_CUDA(cudaMemcpyAsync(&total, tot.ptr, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
+            if (want_codes)
+                CF_CUDA(cudaMemcpyAsync(hk.data(), ctx->scratch_codes.ptr, sizeof(int32_t) * (kCodeHash + 1),
+                                        cudaMemcpyDeviceToHost, ctx->stream));
             CF_CUDA(cudaStreamSynchronize(ctx->stream));
             const bool fits = total < (unsigned long long)INT32_MAX - 64;
             const bool good = fits && (double)total <= 1.2 * (double)m->nnz + 32.0 * 8 &&
                               m->nnz <= 32 * (int64_t)m->n;
-            require(m->format_request != CF_FORMAT_SELL || fits, CF_UNSUPPORTED,
-                    "SELL-32 copy exceeds 2^31 entries");
-            if (m->format_request == CF_FORMAT_SELL || good) {
+            const bool forced = m->format_request == CF_FORMAT_SELL || m->format_request == CF_FORMAT_SELL_C8;
+            require(!forced || fits, CF_UNSUPPORTED, "SELL-32 copy exceeds 2^31 entries");
+            if (forced || good) {
                 exclusive_scan(ctx, ns + 1, slen.as<int32_t>(), m->s_off.as<int32_t>(), tmp);
                 m->n_slices = ns;
                 m->sell_nnz = (int64_t)total;
@@ -920,6 +1057,18 @@ bool matrix_ensure_sell(Matrix *m, bool transpose, bool fp32)
                     m->s_col.as<int32_t>(), (double *)nullptr);
                 CF_CHECK_LAUNCH();
                 m->sell = 1;
+                m->n_codes = 0;
+                if (want_codes) {
+                    const int32_t count = hk[kCodeHash];
+                    hk.resize(kCodeHash);
+                    build_sell_codes(m, hk, count);
+                }
+                if (m->format_request == CF_FORMAT_SELL_C8 && m->n_codes == 0) {
+                    m->sell = -1;   // decided again (and refused again) by the next call
+                    throw Error{CF_UNSUPPORTED,
+                                "one-byte column codes need at most " + std::to_string(kMaxCodes) +
+                                    " distinct column offsets col - row"};
+                }
             }
         }
         m->have_sval = m->have_svalT = m->have_sval32 = m->have_svalT32 = false;
@@ -993,10 +1142,13 @@ void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order)
             k_spmv_sell_ref<<<g, kBlock, 0, ctx->stream>>>(m->n, m->n_slices, m->s_off.as<int32_t>(),
                                                            m->s_col.as<int32_t>(), sv, m->ro.as<int32_t>(), x, y);
         } else {
-            const int g = ctx->fast_grid((const void *)k_spmv_sell, 0);
-            k_spmv_sell<<<g, kBlock, 0, ctx->stream>>>(m->n, m->n_slices, m->s_off.as<int32_t>(),
-                                                       m->s_col.as<int32_t>(), sv, m->ro.as<int32_t>(),
-                                                       m->has_long ? 1 : 0, x, y);
+            const bool codes = m->n_codes > 0;
+            const void *kern = codes ? (const void *)k_spmv_sell<true> : (const void *)k_spmv_sell<false>;
+            const int g = ctx->fast_grid(kern, 0);
+            (codes ? k_spmv_sell<true> : k_spmv_sell<false>)<<<g, kBlock, 0, ctx->stream>>>(
+                m->n, m->n_slices, m->s_off.as<int32_t>(), m->s_col.as<int32_t>(),
+                codes ? m->s_code.as<uint8_t>() : nullptr, codes ? m->s_dtab.as<int32_t>() : nullptr, sv,
+                m->ro.as<int32_t>(), m->has_long ? 1 : 0, x, y);
         }
         CF_CHECK_LAUNCH();
         return;

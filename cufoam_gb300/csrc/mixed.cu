@@ -136,7 +136,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_MX_CG_MIN_BLOCKS) k_mx_cg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
-    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val32);
+    sell_prefetch<FMT>(a, a->s_val32);
     CF_EXIT_IF_DONE(a, st, false);
     const int k = ld_cg(&st->k) + 1;
     const bool first = (k == 1);
@@ -233,7 +233,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_MX_BCS_MIN_BLOCKS) k_mx_bcs_spmv1(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
-    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val32);
+    sell_prefetch<FMT>(a, a->s_val32);
     CF_EXIT_IF_DONE(a, st, false);
     const float *__restrict__ p = a->fp[0];
     const float *__restrict__ rh = a->frs;
@@ -260,7 +260,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_MX_BCS_MIN_BLOCKS) k_mx_bcs_spmv2(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
-    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val32);
+    sell_prefetch<FMT>(a, a->s_val32);
     CF_EXIT_IF_DONE(a, st, false);
     const float alpha = (float)ld_cg(&st->xi);
     const float *__restrict__ r = a->fr;
@@ -339,7 +339,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_MX_MIN_BLOCKS) k_mx_mr_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st_in;
-    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val32);
+    sell_prefetch<FMT>(a, a->s_val32);
     CF_EXIT_IF_DONE(a, st, false);
     const float *__restrict__ r = a->fr;
     float *__restrict__ y = a->fq;
@@ -424,9 +424,17 @@ static Kernels inner_kernels_t(int solver)
     return k;
 }
 
-static Kernels inner_kernels(int solver, bool sell)
+static Kernels inner_kernels(int solver, int format)
 {
-    return sell ? inner_kernels_t<kSell>(solver) : inner_kernels_t<kCsr>(solver);
+    return format == kSellC ? inner_kernels_t<kSellC>(solver)
+           : format == kSell ? inner_kernels_t<kSell>(solver)
+                             : inner_kernels_t<kCsr>(solver);
+}
+
+template <int FMT>
+static const void *residual_kernel(bool scaled)
+{
+    return scaled ? (const void *)k_mx_residual<FMT, true> : (const void *)k_mx_residual<FMT, false>;
 }
 
 bool mixed_supported(int solver)
@@ -492,17 +500,17 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
     SolveArgs &A = *ctx->h_args;
     void *args1[] = {&d_args};
     const bool sell = A.n_slices > 0;
-    const Kernels kk = inner_kernels(solver, sell);
+    const int fmt = solve_format(A);
+    const Kernels kk = inner_kernels(solver, fmt);
     const bool scaled = solver == CF_JMR;
-    const void *k_residual = sell ? (scaled ? (const void *)k_mx_residual<kSell, true>
-                                            : (const void *)k_mx_residual<kSell, false>)
-                                  : (scaled ? (const void *)k_mx_residual<kCsr, true>
-                                            : (const void *)k_mx_residual<kCsr, false>);
+    const void *k_residual = fmt == kSellC ? residual_kernel<kSellC>(scaled)
+                             : fmt == kSell ? residual_kernel<kSell>(scaled)
+                                            : residual_kernel<kCsr>(scaled);
     bool use_graph = use_graph_in;
     GraphEntry *ge = nullptr;
     if (use_graph) {
         try {
-            ge = loop_graph(ctx, kk, solver, CF_PREC_MIXED, cap, false, d_args, sell ? 1 : 0);
+            ge = loop_graph(ctx, kk, solver, CF_PREC_MIXED, cap, false, d_args, fmt);
         } catch (const Error &) {
             ctx->graphs_ok = false;
             use_graph = false;

@@ -118,7 +118,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_cg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
-    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val);
+    sell_prefetch<FMT>(a, a->s_val);
     CF_EXIT_IF_DONE(a, st, false);
     const double *__restrict__ p = a->p[0];
     double *__restrict__ q = a->q;
@@ -354,10 +354,8 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_BICG_SPMV_MIN_BLOCKS) k_f_bicg_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
-    if constexpr (FMT == kSell) {
-        sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val);
-        sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_valT);
-    }
+    sell_prefetch<FMT>(a, a->s_val);
+    sell_prefetch<FMT>(a, a->s_valT);
     CF_EXIT_IF_DONE(a, st, false);
     const double *__restrict__ p = a->p[0];
     const double *__restrict__ ps = a->ps[0];
@@ -396,7 +394,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_jac_step(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
-    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->sc_val);
+    sell_prefetch<FMT>(a, a->sc_val);
     CF_EXIT_IF_DONE(a, st, true);
     const int k = ld_cg(&st->k) + 1;
     const double *__restrict__ rin = a->r[(k + 1) & 1];
@@ -445,7 +443,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_rich_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
-    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, a->s_col, a->s_val);
+    sell_prefetch<FMT>(a, a->s_val);
     CF_EXIT_IF_DONE(a, st, true);
     const double *__restrict__ x = a->x;
     const double *__restrict__ b = a->b;
@@ -484,8 +482,7 @@ template <int FORM, int FMT>
 __global__ void __launch_bounds__(kBlock, CF_SPMV_MIN_BLOCKS) k_f_mr_spmv(const SolveArgs *__restrict__ a)
 {
     DevState *st = a->st;
-    if constexpr (FMT == kSell)
-        sell_prefetch_first(a->n_slices, a->s_off, a->s_col, FORM == kMrScaled ? a->sc_val : a->s_val);
+    sell_prefetch<FMT>(a, FORM == kMrScaled ? a->sc_val : a->s_val);
     CF_EXIT_IF_DONE(a, st, false);
     const double *__restrict__ r = a->r[0];
     const double *__restrict__ gv = FORM == kMrZ ? a->w[1] : a->r[0];
@@ -673,9 +670,11 @@ static Kernels fast_kernels(int solver)
     return k;
 }
 
-Kernels fast_body_kernels(int solver, bool sell)
+Kernels fast_body_kernels(int solver, int format)
 {
-    return sell ? fast_kernels<kSell>(solver) : fast_kernels<kCsr>(solver);
+    return format == kSellC ? fast_kernels<kSellC>(solver)
+           : format == kSell ? fast_kernels<kSell>(solver)
+                             : fast_kernels<kCsr>(solver);
 }
 
 const void *fast_flush_kernel() { return (const void *)k_f_flush_x; }

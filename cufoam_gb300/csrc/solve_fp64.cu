@@ -684,6 +684,15 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
         A.s_col = m->s_col.as<int32_t>();
         A.s_val = m->s_val.as<double>();
         A.s_valT = m->have_svalT ? m->s_valT.as<double>() : nullptr;
+        // one-byte column codes: read by the FP32 sweeps, and by the FP64
+        // fast passes when asked for (CF_FORMAT_SELL_C8).  Those passes are
+        // bound by FP64 issue on GB300 (8 FP64 instructions per row of the CG
+        // SpMV), so saving bytes does not shorten them (128^3 CG step 71.2 us
+        // either way); the FP32 MR step at 256^3 drops from 237 to 214 us.
+        if (m->n_codes > 0 && !ref && (mixed || m->format_request == CF_FORMAT_SELL_C8)) {
+            A.s_code = m->s_code.as<uint8_t>();
+            A.s_dtab = m->s_dtab.as<int32_t>();
+        }
     }
     if (tr) {
         std::swap(A.val, A.valT); // A^T on the same pattern; its transpose is A
@@ -735,11 +744,12 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
     const bool prof = c.profile_kernels != 0;
     bool use_graph = c.use_graph != 0 && ctx->graphs_ok && !prof;
     GraphEntry *ge = nullptr;
-    const Kernels kk = ref ? body_kernels(solver, sell) : fast_body_kernels(solver, sell);
+    const int fmt = solve_format(A);
+    const Kernels kk = ref ? body_kernels(solver, sell) : fast_body_kernels(solver, fmt);
     SolveArgs *d_args = ctx->args.as<SolveArgs>();
     if (use_graph && !mixed) {
         try {
-            ge = loop_graph(ctx, kk, solver, CF_PREC_FP64, cap, ref, d_args, sell ? 1 : 0);
+            ge = loop_graph(ctx, kk, solver, CF_PREC_FP64, cap, ref, d_args, fmt);
         } catch (const Error &) {
             ctx->graphs_ok = false; // fall back to host-driven launches
             use_graph = false;

@@ -21,7 +21,8 @@ namespace cf {
 // row as one FMA chain in entry order.  for_rows calls f(row, sum_j a_ij g(j))
 // for every row; val is the CSR value array, sval its SELL-32 copy.
 // ---------------------------------------------------------------------------
-enum { kCsr = 0, kSell = 1 };
+// kSellC: the SELL-32 copy with one-byte column codes (SellCodes8)
+enum { kCsr = 0, kSell = 1, kSellC = 2 };
 
 // SELL passes take CF_SELL_BATCH entries per thread per batch: all their
 // loads and gathers are issued before the first FMA, and a row's last
@@ -52,6 +53,7 @@ constexpr int kSellBatch = CF_SELL_BATCH;
 #endif
 constexpr int kSellBatch32 = CF_SELL_BATCH32;
 
+
 // (BATCH > 0 overrides the SELL batch of the value type for one kernel; the
 // sums do not depend on it: every row is one FMA chain in entry order)
 template <int FMT, class V, int BATCH = 0, class G, class F>
@@ -59,7 +61,11 @@ __device__ __forceinline__ void for_rows(const SolveArgs *a, const V *val, const
 {
     if constexpr (FMT == kSell) {
         constexpr int B = BATCH > 0 ? BATCH : (sizeof(V) == 4 ? kSellBatch32 : kSellBatch);
-        sell_rows<V, B>(a->n, a->n_slices, a->s_off, a->s_col, sval, a->ro, a->has_long != 0, g, f);
+        sell_rows<V, B>(a->n, a->n_slices, a->s_off, SellCols32{a->s_col}, sval, a->ro, a->has_long != 0, g, f);
+    } else if constexpr (FMT == kSellC) {
+        constexpr int B = BATCH > 0 ? BATCH : (sizeof(V) == 4 ? kSellBatch32 : kSellBatch);
+        sell_rows<V, B>(a->n, a->n_slices, a->s_off, SellCodes8(a->s_code, a->s_dtab), sval, a->ro,
+                        a->has_long != 0, g, f);
     } else {
         const int n = a->n, cap = a->stage_cap;
         CF_STAGE(V, cap);
@@ -79,7 +85,11 @@ __device__ __forceinline__ void for_rows2(const SolveArgs *a, const V *val1, con
                                           const V *sval2, G1 g1, G2 g2, F f)
 {
     if constexpr (FMT == kSell) {
-        sell_rows2<V, 1>(a->n, a->n_slices, a->s_off, a->s_col, sval1, sval2, a->ro, a->has_long != 0, g1, g2, f);
+        sell_rows2<V, 1>(a->n, a->n_slices, a->s_off, SellCols32{a->s_col}, sval1, sval2, a->ro, a->has_long != 0,
+                         g1, g2, f);
+    } else if constexpr (FMT == kSellC) {
+        sell_rows2<V, 1>(a->n, a->n_slices, a->s_off, SellCodes8(a->s_code, a->s_dtab), sval1, sval2, a->ro,
+                         a->has_long != 0, g1, g2, f);
     } else {
         const int n = a->n, cap = a->stage_cap;
         CF_STAGE(V, cap);
@@ -92,6 +102,15 @@ __device__ __forceinline__ void for_rows2(const SolveArgs *a, const V *val1, con
             __syncwarp();
         }
     }
+}
+
+// L2 prefetch of this warp's first slice in the format in use (nothing for
+// CSR): sval is the value array the kernel streams.
+template <int FMT, class V>
+__device__ __forceinline__ void sell_prefetch(const SolveArgs *a, const V *sval)
+{
+    if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, SellCols32{a->s_col}, sval);
+    if constexpr (FMT == kSellC) sell_prefetch_first(a->n_slices, a->s_off, SellCodes8(a->s_code, a->s_dtab), sval);
 }
 
 // ---------------------------------------------------------------------------
@@ -377,7 +396,12 @@ static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int p
     return &(ctx->graphs[key] = ge);
 }
 
-Kernels fast_body_kernels(int solver, bool sell);
+// format: kCsr, kSell or kSellC (solve_format)
+Kernels fast_body_kernels(int solver, int format);
+
+// The format of a solve's fast kernels from its arguments: CSR (no SELL-32
+// copy), SELL-32 with 32-bit columns, or with one-byte column codes.
+inline int solve_format(const SolveArgs &A) { return A.n_slices == 0 ? kCsr : (A.s_code ? kSellC : kSell); }
 const void *fast_flush_kernel();
 
 // ---------------------------------------------------------------------------

@@ -197,6 +197,11 @@ cf_status cf_solver_from_name(const char *name, int32_t *solver);
 void cf_controls_init(cf_controls *c);
 
 cf_status cf_context_create(int32_t device, cf_context **out);
+/* Also releases the device memory of the matrices and batches made on the
+ * context.  Their handles stay valid for cf_matrix_destroy /
+ * cf_batch_destroy only (any order; every other call on them returns
+ * CF_BAD_INPUT), so a garbage collector may free handles after their
+ * context. */
 void cf_context_destroy(cf_context *ctx);
 /* Orders the context's work on `cuda_stream` (a cudaStream_t the caller
  * keeps alive; cudaStreamLegacy and cudaStreamPerThread are accepted), or on
@@ -225,14 +230,25 @@ void cf_matrix_destroy(cf_matrix *m);
  * (the default) picks SELL-32 -- slices of 32 rows padded to their longest
  * row, entry-major, read with coalesced loads and no staging -- when the
  * padding adds at most 20% to nnz and rows average at most 32 entries, and
- * the CSR arrays with warp-chunk staging otherwise.  Both formats sum each
- * row in entry order, so results do not depend on the choice.  The
- * reference-order kernels always read the CSR arrays.  No reference
+ * the CSR arrays with warp-chunk staging otherwise.  SELL-32 stores each
+ * slot's column as a one-byte code (CF_FORMAT_SELL_C8) when the pattern has
+ * at most 32 distinct column offsets col - row (a structured mesh has one
+ * per stencil point), else as a 32-bit index (CF_FORMAT_SELL); a code costs
+ * 1 byte instead of 4, i.e. 9 instead of 12 bytes per FP64 entry and 5
+ * instead of 8 per FP32 entry.  With AUTO the codes are read by the
+ * product (cf_spmv) and the FP32 sweeps of mixed-precision solves; the FP64
+ * solver loops keep the 32-bit columns (GB300's FP64 issue rate, not HBM,
+ * bounds them).  SELL and SELL_C8 may be asked for: SELL_C8 makes every
+ * fast pass read the codes, and fails with CF_UNSUPPORTED on a pattern with
+ * more offsets.  Every format
+ * sums each row in entry order, so results do not depend on the choice.
+ * The reference-order kernels read the 32-bit columns.  No reference
  * counterpart (the reference has CSR only). */
-enum { CF_FORMAT_AUTO = 0, CF_FORMAT_CSR = 1, CF_FORMAT_SELL = 2 };
+enum { CF_FORMAT_AUTO = 0, CF_FORMAT_CSR = 1, CF_FORMAT_SELL = 2, CF_FORMAT_SELL_C8 = 3 };
 cf_status cf_matrix_set_format(cf_matrix *m, int32_t format);
-/* The format the fast kernels use now (CF_FORMAT_CSR or CF_FORMAT_SELL;
- * decides AUTO first) and the stored entries including padding. */
+/* The format the fast kernels use now (CF_FORMAT_CSR, CF_FORMAT_SELL or
+ * CF_FORMAT_SELL_C8; decides AUTO first) and the stored entries including
+ * padding. */
 cf_status cf_matrix_format(cf_matrix *m, int32_t *format, int64_t *stored_entries);
 cf_status cf_matrix_shape(const cf_matrix *m, int32_t *n_rows, int32_t *n_faces, int64_t *nnz);
 /* CSR arrays of A (transpose = 0) or A^T (transpose = 1; the reference's

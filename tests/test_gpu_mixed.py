@@ -68,7 +68,7 @@ def test_mixed_respects_max_iter(ctx):
     assert perf.status == 1
 
 
-@pytest.mark.parametrize("fmt", ["sell", "csr"])
+@pytest.mark.parametrize("fmt", ["sell8", "sell", "csr"])
 @pytest.mark.parametrize("name", ["MRJacobi", "JMR"])
 @pytest.mark.parametrize("transpose", [False, True])
 def test_mixed_mr_family_formats_and_transpose(ctx, fmt, name, transpose):

@@ -25,7 +25,7 @@ def _scaled_true_rel(L, b, psi, nf, jmr):
     return np.linalg.norm(r) / nf
 
 
-@pytest.mark.parametrize("fmt", ["sell", "csr"])
+@pytest.mark.parametrize("fmt", ["sell8", "sell", "csr"])
 @pytest.mark.parametrize("name", ["Jacobi", "MRJacobi", "MRS", "JMR"])
 def test_scaled_matrix_solvers_transpose_and_value_update(ctx, name, fmt):
     """Transposed solves and new coefficient values in the fast order:
