@@ -660,19 +660,29 @@ def run_ours(args):
     # ---- plain SpMV (y = A x) with CUDA events ---------------------------
     x = torch.from_numpy(W.uniform(5, n)).to(f"cuda:{device}")
     y = torch.empty_like(x)
-    for _ in range(3):
-        M.spmv(x, row_order="fast", out=y)
-    torch.cuda.synchronize()
-    reps = 50
-    s0 = torch.cuda.Event(enable_timing=True)
-    s1 = torch.cuda.Event(enable_timing=True)
-    s0.record(stream)
-    for _ in range(reps):
-        M.spmv(x, row_order="fast", out=y)   # enqueued back to back on the stream
-    s1.record(stream)
-    torch.cuda.synchronize()
-    spmv_ms = s0.elapsed_time(s1) / reps
+
+    def time_spmv(reps=50):
+        for _ in range(3):
+            M.spmv(x, row_order="fast", out=y)
+        torch.cuda.synchronize()
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        for _ in range(reps):
+            M.spmv(x, row_order="fast", out=y)   # enqueued back to back on the stream
+        s1.record(stream)
+        torch.cuda.synchronize()
+        return s0.elapsed_time(s1) / reps
+
+    spmv_ms = time_spmv()                     # the default format (one-byte column codes here)
     spmv_gbs = spmv_bytes(mat_spmv, n) / (spmv_ms * 1e-3) / 1e9
+    spmv32_ms = spmv32_gbs = None
+    if fmt == "sell8":                        # the same product over the 32-bit columns
+        M.set_format("sell")
+        spmv32_ms = time_spmv()
+        spmv32_gbs = spmv_bytes(sell_matrix_bytes(n, stored), n) / (spmv32_ms * 1e-3) / 1e9
+        M.set_format("auto")
+        M.format()
 
     if rank != 0:
         if dist:
@@ -741,7 +751,9 @@ def run_ours(args):
                                                         "fp64_pipe_active_frac"),
                      # the plain SpMV y = A x (cf_spmv_async, back to back)
                      "spmv_us": round(spmv_ms * 1e3, 2), "spmv_gbs": round(spmv_gbs, 1),
-                     "spmv_frac": round(spmv_gbs / peak, 4),
+                     "spmv_frac": round(spmv_gbs / peak, 4), "spmv_format": fmt,
+                     "spmv32_us": None if spmv32_ms is None else round(spmv32_ms * 1e3, 2),
+                     "spmv32_frac": None if spmv32_gbs is None else round(spmv32_gbs / peak, 4),
                      # the other two kernels of the CG step, CUDA events per launch
                      "cg_update_us": round(k2_ms * 1e3, 2), "cg_update_gbs": round(k2_gbs, 1),
                      "cg_prep_us": round(k0_ms * 1e3, 2), "cg_prep_gbs": round(k0_gbs, 1),
