@@ -493,16 +493,20 @@ __device__ __forceinline__ int32_t ld_stream(const int32_t *p, uint64_t pol)
     asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
     return v;
 }
-__device__ __forceinline__ uint32_t ld_stream(const uint8_t *p, uint64_t pol)
+// 8 bytes (8-byte aligned) as two words
+__device__ __forceinline__ uint2 ld_stream8(const uint8_t *p, uint64_t pol)
 {
-    uint32_t v;
-    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u8 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    uint2 v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+        : "=r"(v.x), "=r"(v.y)
+        : "l"(p), "l"(pol));
     return v;
 }
 
-// Column indices of a SELL-32 copy, read slot by slot.  SellCols32 holds
-// the 32-bit column of every slot.  SellCodes8 holds one byte per slot: an
-// index into a table of the pattern's distinct offsets col - row (at most
+// Column indices of a SELL-32 copy.  SellCols32 holds the 32-bit column of
+// every slot, entry-major like the values (slot t of lane l's row at element
+// b + 32 t + l of its slice).  SellCodes8 holds one byte per slot: an index
+// into a table of the pattern's distinct offsets col - row (at most
 // kMaxCodes; a 7-point stencil has 7, a 27-point one 27), so a slot costs 1
 // byte instead of 4: 9 instead of 12 bytes per FP64 entry, 5 instead of 8
 // per FP32 entry.  A padding slot holds offset 0 from its row base rb -- the
@@ -510,27 +514,52 @@ __device__ __forceinline__ uint32_t ld_stream(const uint8_t *p, uint64_t pol)
 // the column the 32-bit copy stores there, so both give the same gathers
 // and the same sums.
 //
-// Lane l keeps table entry l in a register and a code is decoded by a warp
-// shuffle (col(), called by all 32 lanes together).  Measured on GB300
-// against an L1-cached table load and a select tree over eight registers
-// (7-point systems): plain FP64 SpMV at 128^3 33.2 us (table 37.2, select
-// tree 36.4, 32-bit columns 35.7), FP32 MR step at 256^3 214 us (224, 228;
-// 237).  A row longer than 32 entries has more than 32 offsets, so
-// matrices with long rows keep 32-bit columns; col_div() (any lanes) reads
-// the table from memory.
+// The codes of a slice are stored lane-major (lane l's `len` codes at bytes
+// b + len l ... of the slice), so a lane fetches up to eight of them with
+// two aligned 8-byte loads: a load in flight holds a register until it
+// returns, and four registers for eight codes leave room for more loads in
+// flight than one register per one-byte load.  Lane l keeps table entry l
+// in a register and decodes by a warp shuffle (col(), called by all 32
+// lanes together).  Measured on GB300 against an L1-cached table load and a
+// select tree over eight registers (7-point systems, byte loads): plain FP64
+// SpMV at 128^3 33.2 us (table 37.2, select tree 36.4, 32-bit columns 35.7),
+// FP32 MR step at 256^3 214 us (224, 228; 237).  A row longer than 32
+// entries has more than 32 offsets, so matrices with long rows keep 32-bit
+// columns; col_div() (any lanes) reads the table from memory.
 constexpr int kMaxCodes = 32;
 
 struct SellCols32 {
-    using raw_t = int32_t;
     const int32_t *p;
-    __device__ __forceinline__ int32_t load(int64_t o, uint64_t pol) const { return ld_stream(p + o, pol); }
-    __device__ __forceinline__ int32_t plain(int64_t o) const { return p[o]; }
+    // the columns of slots t0 .. t0 + M - 1 of this lane's row (slice at b)
+    template <int M> struct Batch {
+        int32_t c[M];
+        __device__ __forceinline__ int32_t raw(int u) const { return c[u]; }
+    };
+    template <int M>
+    __device__ __forceinline__ Batch<M> load_batch(int64_t b, int lane, int, int t0, uint64_t pol) const
+    {
+        Batch<M> r;
+#pragma unroll
+        for (int u = 0; u < M; ++u) r.c[u] = ld_stream(p + b + lane + 32 * (t0 + u), pol);
+        return r;
+    }
+    // the same for the slots below len only (a batch may run past the row)
+    template <int M>
+    __device__ __forceinline__ Batch<M> load_guarded(int64_t b, int lane, int len, int t0, uint64_t pol) const
+    {
+        Batch<M> r;
+#pragma unroll
+        for (int u = 0; u < M; ++u)
+            if (t0 + u < len) r.c[u] = ld_stream(p + b + lane + 32 * (t0 + u), pol);
+        return r;
+    }
+    // slot t of row r of the slice (len slots)
+    __device__ __forceinline__ int32_t plain_slot(int64_t b, int, int r, int t) const { return p[b + r + (int64_t)32 * t]; }
     __device__ __forceinline__ int col(int32_t raw, int) const { return raw; }
     __device__ __forceinline__ int col_div(int32_t raw, int) const { return raw; }
     __device__ __forceinline__ const void *addr(int64_t o) const { return p + o; }
 };
 struct SellCodes8 {
-    using raw_t = uint32_t;
     const uint8_t *p;
     const int32_t *tab;  // offsets col - row (kMaxCodes entries, unused ones 0)
     int treg;            // tab[lane]
@@ -538,8 +567,41 @@ struct SellCodes8 {
         : p(p_), tab(tab_), treg(__ldg(tab_ + (threadIdx.x & 31)))
     {
     }
-    __device__ __forceinline__ uint32_t load(int64_t o, uint64_t pol) const { return ld_stream(p + o, pol); }
-    __device__ __forceinline__ uint32_t plain(int64_t o) const { return p[o]; }
+    // codes t0 .. t0 + M - 1 (M <= 8) of this lane, packed four to a word
+    template <int M> struct Batch {
+        uint32_t lo, hi;
+        __device__ __forceinline__ uint32_t raw(int u) const { return ((u < 4 ? lo : hi) >> (8 * (u & 3))) & 0xffu; }
+    };
+    // bytes b + len lane + t0 ... inside the 16 bytes from the 8-byte
+    // boundary below them (the array is padded, so the window may run past
+    // the slice)
+    template <int M>
+    __device__ __forceinline__ Batch<M> load_batch(int64_t b, int lane, int len, int t0, uint64_t pol) const
+    {
+        static_assert(M <= 8, "at most eight codes per batch");
+        const int64_t a = b + (int64_t)len * lane + t0;
+        const int64_t a0 = a & ~(int64_t)7;
+        const uint2 w01 = ld_stream8(p + a0, pol);
+        const uint2 w23 = ld_stream8(p + a0 + 8, pol);
+        const unsigned k = (unsigned)(a - a0);
+        const bool up = k >= 4;
+        const unsigned sh = 8u * (k & 3u);
+        const uint32_t x0 = up ? w01.y : w01.x, x1 = up ? w23.x : w01.y, x2 = up ? w23.y : w23.x;
+        Batch<M> r;
+        r.lo = __funnelshift_r(x0, x1, sh);   // codes t0 .. t0 + 3
+        r.hi = __funnelshift_r(x1, x2, sh);   // codes t0 + 4 .. t0 + 7
+        return r;
+    }
+    // (the 16-byte window stays inside the padded array for any t0 < len)
+    template <int M>
+    __device__ __forceinline__ Batch<M> load_guarded(int64_t b, int lane, int len, int t0, uint64_t pol) const
+    {
+        return load_batch<M>(b, lane, len, t0, pol);
+    }
+    __device__ __forceinline__ uint32_t plain_slot(int64_t b, int len, int r, int t) const
+    {
+        return p[b + (int64_t)len * r + t];
+    }
     __device__ __forceinline__ int col(uint32_t raw, int rb) const { return rb + __shfl_sync(kFull, treg, (int)raw); }
     __device__ __forceinline__ int col_div(uint32_t raw, int rb) const { return rb + __ldg(tab + raw); }
     __device__ __forceinline__ const void *addr(int64_t o) const { return p + o; }
@@ -575,36 +637,34 @@ __device__ __forceinline__ void sell_prefetch_first(int n_slices, const int32_t 
     }
 }
 
-// M entries of a SELL row (slots 32 elements apart, the first at element o
-// of the column and value arrays): all loads and gathers issued before the
-// first FMA, then one FMA chain in slot order.
+// Slots t0 .. t0 + M - 1 of this lane's row (slice at element b, len slots;
+// values 32 elements apart from vp = val + b + lane + 32 t0): all loads and
+// gathers issued before the first FMA, then one FMA chain in slot order.
 template <class V, int M, class C, class G>
-__device__ __forceinline__ void sell_batch(const C &cs, int64_t o, int rb, const V *vp, uint64_t pol, G g, V &acc)
+__device__ __forceinline__ void sell_batch(const C &cs, int64_t b, int lane, int len, int t0, int rb, const V *vp,
+                                           uint64_t pol, G g, V &acc)
 {
-    typename C::raw_t c[M];
     V v[M], x[M];
+    const auto c = cs.template load_batch<M>(b, lane, len, t0, pol);
 #pragma unroll
-    for (int u = 0; u < M; ++u) {
-        c[u] = cs.load(o + 32 * u, pol);
-        v[u] = ld_stream(vp + 32 * u, pol);
-    }
+    for (int u = 0; u < M; ++u) v[u] = ld_stream(vp + 32 * u, pol);
 #pragma unroll
-    for (int u = 0; u < M; ++u) x[u] = g(cs.col(c[u], rb));
+    for (int u = 0; u < M; ++u) x[u] = g(cs.col(c.raw(u), rb));
 #pragma unroll
     for (int u = 0; u < M; ++u) acc = fma_t(v[u], x[u], acc);
 }
 
 // the last r < B entries of a row as one exact batch
 template <class V, int B, class C, class G>
-__device__ __forceinline__ void sell_tail(int r, const C &cs, int64_t o, int rb, const V *vp, uint64_t pol, G g,
-                                          V &acc)
+__device__ __forceinline__ void sell_tail(int r, const C &cs, int64_t b, int lane, int len, int t0, int rb,
+                                          const V *vp, uint64_t pol, G g, V &acc)
 {
     if constexpr (B > 1) {
         if (r == B - 1) {
-            sell_batch<V, B - 1>(cs, o, rb, vp, pol, g, acc);
+            sell_batch<V, B - 1>(cs, b, lane, len, t0, rb, vp, pol, g, acc);
             return;
         }
-        sell_tail<V, B - 1>(r, cs, o, rb, vp, pol, g, acc);
+        sell_tail<V, B - 1>(r, cs, b, lane, len, t0, rb, vp, pol, g, acc);
     }
 }
 
@@ -612,10 +672,11 @@ __device__ __forceinline__ void sell_tail(int r, const C &cs, int64_t o, int rb,
 // `ro`) summed by the whole warp over their own slots, the bits of the CSR
 // passes (warp_row: lane j takes slots j, j + 32, ... as one FMA chain,
 // then the xor-shuffle tree); `acc` is this lane's sum, replaced for those
-// lanes.  b is the slice's first element, vp0 its first value.
+// lanes.  b is the slice's first element, slen its slots per row, vp0 its
+// first value.
 template <class V, class C, class G>
 __device__ __forceinline__ void sell_long_rows(int n, int s, const int32_t *__restrict__ ro, const C &cs,
-                                               int64_t b, const V *vp0, G g, V &acc)
+                                               int64_t b, int slen, const V *vp0, G g, V &acc)
 {
     const int lane = threadIdx.x & 31;
     const int row = s * 32 + lane;
@@ -626,7 +687,7 @@ __device__ __forceinline__ void sell_long_rows(int n, int s, const int32_t *__re
         const int rb = s * 32 + r;
         V a = V(0);
         for (int t = lane; t < len; t += 32)
-            a = fma_t(vp0[r + (int64_t)32 * t], g(cs.col_div(cs.plain(b + r + (int64_t)32 * t), rb)), a);
+            a = fma_t(vp0[r + (int64_t)32 * t], g(cs.col_div(cs.plain_slot(b, slen, r, t), rb)), a);
         const V v = warp_sum(a);
         if (lane == r) acc = v;
     }
@@ -653,13 +714,12 @@ __device__ __forceinline__ void sell_rows(int n, int n_slices, const int32_t *__
         const int len = (__ldg(off + s + 1) - b) >> 5;
         const int row = s * 32 + lane;
         const int rb = sell_row_base(row, n);
-        const int64_t o = (int64_t)b + lane;
-        const V *vp = val + o;
+        const V *vp = val + (int64_t)b + lane;
         V acc = V(0);
         int t0 = 0;
-        for (; t0 + B <= len; t0 += B) sell_batch<V, B>(cs, o + 32 * t0, rb, vp + 32 * t0, pol, g, acc);
-        sell_tail<V, B>(len - t0, cs, o + 32 * t0, rb, vp + 32 * t0, pol, g, acc);
-        if (has_long) sell_long_rows(n, s, ro, cs, b, val + b, g, acc);
+        for (; t0 + B <= len; t0 += B) sell_batch<V, B>(cs, b, lane, len, t0, rb, vp + 32 * t0, pol, g, acc);
+        sell_tail<V, B>(len - t0, cs, b, lane, len, t0, rb, vp + 32 * t0, pol, g, acc);
+        if (has_long) sell_long_rows(n, s, ro, cs, b, len, val + b, g, acc);
         if (row < n) f(row, acc);
     }
 }
@@ -683,19 +743,18 @@ __device__ __forceinline__ void sell_rows2(int n, int n_slices, const int32_t *_
         const V *vp2 = val2 + o;
         V a1 = V(0), a2 = V(0);
         for (int t0 = 0; t0 < len; t0 += B) {
-            typename C::raw_t c[B];
             V v1[B], v2[B], x1[B], x2[B];
+            const auto c = cs.template load_guarded<B>(b, lane, len, t0, pol);
 #pragma unroll
             for (int u = 0; u < B; ++u)
                 if (t0 + u < len) {
-                    c[u] = cs.load(o + 32 * (t0 + u), pol);
                     v1[u] = ld_stream(vp1 + 32 * (t0 + u), pol);
                     v2[u] = ld_stream(vp2 + 32 * (t0 + u), pol);
                 }
 #pragma unroll
             for (int u = 0; u < B; ++u)
                 if (t0 + u < len) {
-                    const int cc = cs.col(c[u], rb);
+                    const int cc = cs.col(c.raw(u), rb);
                     x1[u] = g1(cc);
                     x2[u] = g2(cc);
                 }
@@ -707,8 +766,8 @@ __device__ __forceinline__ void sell_rows2(int n, int n_slices, const int32_t *_
                 }
         }
         if (has_long) {
-            sell_long_rows(n, s, ro, cs, b, val1 + b, g1, a1);
-            sell_long_rows(n, s, ro, cs, b, val2 + b, g2, a2);
+            sell_long_rows(n, s, ro, cs, b, len, val1 + b, g1, a1);
+            sell_long_rows(n, s, ro, cs, b, len, val2 + b, g2, a2);
         }
         if (row < n) f(row, a1, a2);
     }

@@ -395,7 +395,8 @@ __global__ void k_csr_offsets(int n, const int32_t *__restrict__ ro, const int32
 }
 
 // each slot's code: the number of its offset (slot_code, by set position);
-// every offset is in the set, found within kCodeHash probes
+// every offset is in the set, found within kCodeHash probes.  A slice's
+// codes are stored lane-major: lane l's len codes at b + len l.
 __global__ void k_sell_encode(int n, int n_slices, const int32_t *__restrict__ soff,
                               const int32_t *__restrict__ scol, const int32_t *__restrict__ keys,
                               const uint8_t *__restrict__ slot_code, uint8_t *code)
@@ -405,11 +406,10 @@ __global__ void k_sell_encode(int n, int n_slices, const int32_t *__restrict__ s
         const int b = soff[s], len = (soff[s + 1] - b) >> 5;
         const int rb = sell_row_base(i, n);
         for (int t = 0; t < len; ++t) {
-            const int o = b + 32 * t + lane;
-            const int32_t d = scol[o] - rb;
+            const int32_t d = scol[b + 32 * t + lane] - rb;
             uint32_t h = offset_hash(d);
             for (int probe = 0; probe < kCodeHash && keys[h] != d; ++probe) h = (h + 1) & (kCodeHash - 1);
-            code[o] = slot_code[h];
+            code[b + len * lane + t] = slot_code[h];   // lane-major within the slice
         }
     }
 }
@@ -425,23 +425,26 @@ __global__ void k_sell_encode(int n, int n_slices, const int32_t *__restrict__ s
 #ifndef CF_PLAIN_SPMV_MINB
 #define CF_PLAIN_SPMV_MINB 5
 #endif
-#if CF_PLAIN_SPMV_MINB > 0
-#define CF_PLAIN_SPMV_BOUNDS __launch_bounds__(kBlock, CF_PLAIN_SPMV_MINB)
-#else
-#define CF_PLAIN_SPMV_BOUNDS __launch_bounds__(kBlock)
+// The same over the one-byte column codes, with its own constants: a batch
+// fetches its codes as one 16-byte window, so a 7-entry row is best one
+// batch.
+#ifndef CF_PLAIN_SPMV8_BATCH
+#define CF_PLAIN_SPMV8_BATCH 8
+#endif
+#ifndef CF_PLAIN_SPMV8_MINB
+#define CF_PLAIN_SPMV8_MINB 4
 #endif
 // (CODES: the columns from the one-byte codes and their offset table)
 template <bool CODES>
-__global__ void CF_PLAIN_SPMV_BOUNDS k_spmv_sell(int n, int n_slices, const int32_t *__restrict__ off,
-                                                 const int32_t *__restrict__ col, const uint8_t *__restrict__ code,
-                                                 const int32_t *__restrict__ tab, const double *__restrict__ val,
-                                                 const int32_t *__restrict__ ro, int has_long,
-                                                 const double *__restrict__ x, double *y)
+__global__ void __launch_bounds__(kBlock, CODES ? CF_PLAIN_SPMV8_MINB : (CF_PLAIN_SPMV_MINB > 0 ? CF_PLAIN_SPMV_MINB : 1))
+    k_spmv_sell(int n, int n_slices, const int32_t *__restrict__ off, const int32_t *__restrict__ col,
+                const uint8_t *__restrict__ code, const int32_t *__restrict__ tab, const double *__restrict__ val,
+                const int32_t *__restrict__ ro, int has_long, const double *__restrict__ x, double *y)
 {
     auto g = [&](int c) { return __ldg(x + c); };
     auto f = [&](int row, double v) { y[row] = v; };
     if constexpr (CODES)
-        sell_rows<double, CF_PLAIN_SPMV_BATCH>(n, n_slices, off, SellCodes8(code, tab), val, ro, has_long != 0, g, f);
+        sell_rows<double, CF_PLAIN_SPMV8_BATCH>(n, n_slices, off, SellCodes8(code, tab), val, ro, has_long != 0, g, f);
     else
         sell_rows<double, CF_PLAIN_SPMV_BATCH>(n, n_slices, off, SellCols32{col}, val, ro, has_long != 0, g, f);
 }
