@@ -959,23 +959,25 @@ def run_profile_mr(args):
     return 0
 
 
-def run_profile_batch(args):
+def run_profile_batch(args, small: bool = False):
     """A batched solve small enough for a full ncu capture: 256 lognormal
     7-point boxes with sides uniform in 16..40, rows permuted, 3 right-hand
-    sides, CG to 1e-8 in FP64 and in mixed precision, default schedule."""
+    sides, CG to 1e-8 in FP64 and in mixed precision, default schedule.
+    small: 32 boxes with sides 16..24 and at most 300 steps, short enough
+    launches for ncu's ~40 replay passes of the mixed kernel."""
     import torch
 
     import cufoam_gb300 as cf
     from cufoam_gb300 import workloads as W
     from cufoam_gb300.batch import BatchSolver, c4_systems
     ctx = cf.Context(0)
-    systems, _ = c4_systems(256, seed=4, lo=16, hi=40)
+    systems, _ = c4_systems(32, seed=4, lo=16, hi=24) if small else c4_systems(256, seed=4, lo=16, hi=40)
     B = BatchSolver(systems, n_rhs=3, context=ctx)
     rhs = [np.stack([W.uniform(10_000 + 3 * s + j, L.n) for j in range(3)])
            for s, L in enumerate(systems)]
     packed = torch.from_numpy(B.pack(rhs)).to("cuda")
     for prec in ("FP64", "mixed"):
-        _, res, ms = B.solve(packed, tolerance=1e-8, max_iter=5000, precision=prec)
+        _, res, ms = B.solve(packed, tolerance=1e-8, max_iter=300 if small else 5000, precision=prec)
         print(f"{prec}: {ms:.2f} ms, {sum(r['n_iterations'] for r in res)} iterations, "
               f"{sum(r['status'] == 0 for r in res)}/{len(res)} converged")
     B.close()
@@ -1132,8 +1134,8 @@ def _launch_bytes(N, F, nnz, S, slices):
             t[n2] = (formula.replace("Msell32", "Msell8_32"), val - Msell32 + Msell8_32)
         else:
             t[n2] = (formula.replace("Msell", "Msell8"), val - Msell + Msell8)
-    t["k_spmv_sell<SellCodes8>"] = ("Msell8 + 2V", Msell8 + 2 * V)
-    t["k_spmv_sell<SellCols32>"] = t["k_spmv_sell"]
+    t["k_spmv_sell<1>"] = ("Msell8 + 2V", Msell8 + 2 * V)     # over the one-byte codes
+    t["k_spmv_sell<0>"] = t["k_spmv_sell"]
     return t
 
 
@@ -1184,6 +1186,8 @@ def main():
                     help="skip the mixed-vs-FP64 and batched-vs-sequential comparisons")
     ap.add_argument("--profile", action="store_true",
                     help="short host-driven run for an ncu capture (prints no JSON)")
+    ap.add_argument("--profile-batch-small", action="store_true",
+                    help="the same with 32 systems of sides 16..24 and at most 300 steps (ncu --set full)")
     ap.add_argument("--profile-batch", action="store_true",
                     help="one FP64 and one mixed batched solve of 256 small systems, for ncu")
     ap.add_argument("--profile-all", action="store_true",
@@ -1207,8 +1211,8 @@ def main():
         return run_profile_mr(args)
     if args.profile_all:
         return run_profile_all(args)
-    if args.profile_batch:
-        return run_profile_batch(args)
+    if args.profile_batch or args.profile_batch_small:
+        return run_profile_batch(args, small=args.profile_batch_small)
     if args.profile:
         return run_profile(args)
     if args.impl == "reference":

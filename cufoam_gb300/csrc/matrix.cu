@@ -376,20 +376,31 @@ __global__ void k_offsets_clear(int32_t *keys, int32_t *count)
 }
 
 // every CSR entry's offset, and 0; stops early once more than kMaxCodes
-// distinct offsets are in the set (the codes cannot be used then)
+// distinct offsets are in the set (the codes cannot be used then).  Each
+// thread remembers the last eight offsets it inserted in registers, so a
+// stencil's few offsets reach the set (and its hot cache lines) once per
+// thread, not once per entry.
 __global__ void k_csr_offsets(int n, const int32_t *__restrict__ ro, const int32_t *__restrict__ col,
                               int32_t *keys, int32_t *count)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) offset_insert(keys, count, 0);
+    int32_t s0 = kNoOffset, s1 = kNoOffset, s2 = kNoOffset, s3 = kNoOffset;
+    int32_t s4 = kNoOffset, s5 = kNoOffset, s6 = kNoOffset, s7 = kNoOffset;
     CF_FOR_ELEMS(i, n) {
-        int32_t last = kNoOffset;
         const int re = ro[i + 1];
         for (int j = ro[i]; j < re; ++j) {
-            if (*(volatile int32_t *)count > kMaxCodes) return;
             const int32_t d = col[j] - i;
-            if (d == last) continue;
-            last = d;
+            if (d == s0 || d == s1 || d == s2 || d == s3 || d == s4 || d == s5 || d == s6 || d == s7) continue;
+            if (*(volatile int32_t *)count > kMaxCodes) return;
             offset_insert(keys, count, d);
+            s7 = s6;
+            s6 = s5;
+            s5 = s4;
+            s4 = s3;
+            s3 = s2;
+            s2 = s1;
+            s1 = s0;
+            s0 = d;
         }
     }
 }
