@@ -350,11 +350,14 @@ constexpr int32_t kNoOffset = INT32_MIN;     // empty slot (|d| < n < 2^31)
 
 __device__ __forceinline__ uint32_t offset_hash(int32_t d) { return ((uint32_t)d * 2654435761u) >> 22; }
 
-// d into the set; every probe sequence ends within kCodeHash steps
+// d into the set.  With at most kMaxCodes keys no probe sequence meets more
+// than kMaxCodes occupied slots, so one that meets more proves an overflow:
+// it marks the count past the limit (every thread then stops) instead of
+// walking a table that thousands of offsets filled.
 __device__ void offset_insert(int32_t *keys, int32_t *count, int32_t d)
 {
     uint32_t h = offset_hash(d);
-    for (int probe = 0; probe < kCodeHash; ++probe, h = (h + 1) & (kCodeHash - 1)) {
+    for (int probe = 0; probe <= kMaxCodes + 1; ++probe, h = (h + 1) & (kCodeHash - 1)) {
         const int32_t k = *(volatile int32_t *)(keys + h);
         if (k == d) return;
         if (k == kNoOffset) {
@@ -366,6 +369,7 @@ __device__ void offset_insert(int32_t *keys, int32_t *count, int32_t d)
             if (old == d) return;
         }
     }
+    atomicMax(count, kMaxCodes + 1);
 }
 
 // keys = empty, count = 0
