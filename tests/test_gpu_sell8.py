@@ -128,3 +128,52 @@ def test_codes_limit(ctx, n_strides):
         y = M.spmv(x, row_order="fast")
         M.set_format("sell")
         assert M.spmv(x, row_order="fast").tobytes() == y.tobytes()
+
+
+def _random_offset_ldu(seed):
+    """A random symmetric pattern whose couplings use a random set of 2..15
+    strides (offsets 0 and +-k: at most 31), with cells dropped from some
+    couplings, on a ragged size: uneven slices and rows of 1..31 entries."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(40, 3000))
+    strides = np.sort(rng.choice(np.arange(1, min(n - 1, 400)), size=int(rng.integers(2, 16)), replace=False))
+    la, ua = [], []
+    for k in strides:
+        keep = rng.random(n - k) < rng.uniform(0.3, 1.0)
+        cells = np.arange(n - k)[keep]
+        la.append(cells)
+        ua.append(cells + k)
+    la = np.concatenate(la).astype(np.int32)
+    ua = np.concatenate(ua).astype(np.int32)
+    order = np.lexsort((ua, la))
+    la, ua = la[order], ua[order]
+    w = rng.uniform(0.5, 1.5, size=len(la))
+    diag = np.ones(n)
+    np.add.at(diag, la, 2 * w)
+    np.add.at(diag, ua, 2 * w)
+    return O.LDU(n, diag, -w, -rng.uniform(0.5, 1.0) * w, la, ua)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_offset_sets_same_bits(ctx, seed):
+    """Random patterns within the codes' limit: the product over the codes
+    is bit-identical to the 32-bit columns and to CSR, for A and A^T, and a
+    fast-order MR solve takes the same steps to the same bits."""
+    L = _random_offset_ldu(seed)
+    A = O.ldu2csr(L)
+    assert len(np.unique(A.cols - np.repeat(np.arange(L.n), np.diff(A.row_offsets)))) <= 32
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    x = O.uniform(7 + seed, L.n)
+    b = O.uniform(3 + seed, L.n)
+    out = {}
+    for f in ("csr", "sell", "sell8"):
+        M.set_format(f)
+        assert M.format()[0] == f
+        out[f] = (M.spmv(x, row_order="fast").tobytes(), M.spmv(x, transpose=True, row_order="fast").tobytes())
+        if f != "csr":
+            out[f] += (_solve(M, "MR", b, {"reduction": "fast", "tolerance": 1e-9}, maxit=5000),)
+    assert out["csr"][:2] == out["sell"][:2] == out["sell8"][:2]
+    assert out["sell"][2] == out["sell8"][2]
+    ref = O.ref_spmv(A, x)
+    y = np.frombuffer(out["sell8"][0], dtype=np.float64)
+    assert np.allclose(y, ref, rtol=1e-14, atol=1e-14 * np.abs(ref).max())
