@@ -64,13 +64,21 @@ def sell8_matrix_bytes(n: int, stored: int) -> int:
     return 9 * stored + 4 * ((n + 31) // 32 + 1) + 4 * 32
 
 
+def sell16_matrix_bytes(n: int, stored: int) -> int:
+    """SELL-32 with 16-bit column deltas: 8 B value + 2 B delta per stored
+    entry, one int32 offset per slice."""
+    return 10 * stored + 4 * ((n + 31) // 32 + 1)
+
+
 def iter_matrix_bytes(fmt: str, n: int, nnz: int, stored: int, fp64_loop: bool = False) -> int:
     """FP64 matrix bytes per pass of the fast kernels in the format in use.
     fp64_loop: a pass of an FP64 solver loop, which reads the 32-bit columns
     when the codes exist by default (the codes serve the plain product and
     the FP32 sweeps)."""
-    if fmt == "sell8" and fp64_loop:
+    if fmt in ("sell8", "sell16") and fp64_loop:
         fmt = "sell"
+    if fmt == "sell16":
+        return sell16_matrix_bytes(n, stored)
     if fmt == "sell8":
         return sell8_matrix_bytes(n, stored)
     if fmt == "sell":
@@ -1081,6 +1089,8 @@ def _launch_bytes(N, F, nnz, S, slices):
     Msell32 = 8 * S + 4 * (slices + 1)
     Msell8 = 9 * S + 4 * (slices + 1) + 128           # one-byte column codes (format 2)
     Msell8_32 = 5 * S + 4 * (slices + 1) + 128
+    Msell16 = 10 * S + 4 * (slices + 1)               # 16-bit column deltas (format 3)
+    Msell16_32 = 6 * S + 4 * (slices + 1)
     t = {
         "k_pow_step": ("Mcsr + 2V", Mcsr + 2 * V), "k_pow_final": ("Mcsr + V", Mcsr + V),
         "k_bicg_spmv": ("Mcsr + 8nnz + 10V", Mcsr + 8 * nnz + 10 * V),
@@ -1121,20 +1131,24 @@ def _launch_bytes(N, F, nnz, S, slices):
     }
     # the same passes over the one-byte column codes: format 2 in the kernel
     # name, Msell8 (Msell8_32 for FP32 values) in place of Msell (Msell32)
+    # and over the 16-bit deltas: format 3, Msell16 (Msell16_32)
     for name, (formula, val) in list(t.items()):
         if not (name.startswith("k_f_") or name.startswith("k_mx_")) or "Msell" not in formula:
             continue
-        if name.startswith("k_mx_residual"):
-            n2 = name.replace("<1, ", "<2, ")
-        elif name.startswith("k_f_mr_spmv"):
-            n2 = name.replace(", 1>", ", 2>")
-        else:
-            n2 = name.replace("<1>", "<2>")
-        if "Msell32" in formula:
-            t[n2] = (formula.replace("Msell32", "Msell8_32"), val - Msell32 + Msell8_32)
-        else:
-            t[n2] = (formula.replace("Msell", "Msell8"), val - Msell + Msell8)
+        for fmt, m64, m32 in ((2, Msell8, Msell8_32), (3, Msell16, Msell16_32)):
+            lab = "Msell8" if fmt == 2 else "Msell16"
+            if name.startswith("k_mx_residual"):
+                n2 = name.replace("<1, ", f"<{fmt}, ")
+            elif name.startswith("k_f_mr_spmv"):
+                n2 = name.replace(", 1>", f", {fmt}>")
+            else:
+                n2 = name.replace("<1>", f"<{fmt}>")
+            if "Msell32" in formula:
+                t[n2] = (formula.replace("Msell32", lab + "_32"), val - Msell32 + m32)
+            else:
+                t[n2] = (formula.replace("Msell", lab), val - Msell + m64)
     t["k_spmv_sell<1>"] = ("Msell8 + 2V", Msell8 + 2 * V)     # over the one-byte codes
+    t["k_spmv_sell<2>"] = ("Msell16 + 2V", Msell16 + 2 * V)   # over the 16-bit deltas
     t["k_spmv_sell<0>"] = t["k_spmv_sell"]
     return t
 

@@ -201,14 +201,16 @@ class LduMatrix:
         self._lib.cf_matrix_shape(self._h, C.byref(n), C.byref(f), C.byref(z))
         return n.value, f.value, z.value
 
-    _FORMATS = {"auto": 0, "csr": 1, "sell": 2, "sell8": 3}
+    _FORMATS = {"auto": 0, "csr": 1, "sell": 2, "sell8": 3, "sell16": 4}
 
     def set_format(self, fmt: str) -> None:
         """Storage the fast kernels read: "auto" (SELL-32 when the padding
         stays within 20% of nnz, else CSR; SELL-32 with one-byte column
-        codes when the pattern has at most 32 distinct offsets col - row),
-        "csr", "sell" (32-bit columns) or "sell8" (one-byte codes; raises
-        for a pattern with more offsets)."""
+        codes when the pattern has at most 32 distinct offsets col - row,
+        else 16-bit column deltas when every |col - row| <= 32767), "csr",
+        "sell" (32-bit columns), "sell8" (one-byte codes; raises for a
+        pattern with more offsets) or "sell16" (16-bit deltas; raises for a
+        pattern with a larger offset)."""
         self.ctx.check(self._lib.cf_matrix_set_format(self._h, self._FORMATS[fmt]),
                        "cf_matrix_set_format")
 
@@ -216,7 +218,7 @@ class LduMatrix:
         """(format the fast kernels use, stored entries incl. padding)."""
         f, z = C.c_int32(), C.c_int64()
         self.ctx.check(self._lib.cf_matrix_format(self._h, C.byref(f), C.byref(z)), "cf_matrix_format")
-        return {1: "csr", 2: "sell", 3: "sell8"}[f.value], z.value
+        return {1: "csr", 2: "sell", 3: "sell8", 4: "sell16"}[f.value], z.value
 
     def update_values(self, diag, lower, upper) -> None:
         pd, m1, k1 = _ptr(diag, np.float64, "diag")

@@ -18,7 +18,7 @@ CF_MEM_HOST, CF_MEM_DEVICE = 0, 1
 CF_PREC_FP64, CF_PREC_MIXED = 0, 1
 CF_REDUCE_FAST, CF_REDUCE_REFERENCE, CF_REDUCE_AUTO = 0, 1, 2
 CF_NORM_REFERENCE_L2, CF_NORM_OPENFOAM_L1 = 0, 1
-CF_FORMAT_AUTO, CF_FORMAT_CSR, CF_FORMAT_SELL, CF_FORMAT_SELL_C8 = 0, 1, 2, 3
+CF_FORMAT_AUTO, CF_FORMAT_CSR, CF_FORMAT_SELL, CF_FORMAT_SELL_C8, CF_FORMAT_SELL_D16 = 0, 1, 2, 3, 4
 
 
 class cf_ldu_view(C.Structure):

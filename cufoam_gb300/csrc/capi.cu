@@ -482,7 +482,7 @@ cf_status cf_matrix_set_format(cf_matrix *m, int32_t format)
     if (!m || !m->owner) return CF_BAD_INPUT;
     return guarded(m->owner, [&] {
         cf::require(format == CF_FORMAT_AUTO || format == CF_FORMAT_CSR || format == CF_FORMAT_SELL ||
-                        format == CF_FORMAT_SELL_C8,
+                        format == CF_FORMAT_SELL_C8 || format == CF_FORMAT_SELL_D16,
                     CF_BAD_INPUT, "bad format");
         cf::Matrix *mi = m->impl;
         if (mi->format_request != format) {
@@ -500,7 +500,11 @@ cf_status cf_matrix_format(cf_matrix *m, int32_t *format, int64_t *stored_entrie
     return guarded(m->owner, [&] {
         const bool sell = cf::matrix_ensure_sell(m->impl, false, false);
         CF_CUDA(cudaStreamSynchronize(m->owner->impl->stream));
-        if (format) *format = !sell ? CF_FORMAT_CSR : (m->impl->n_codes > 0 ? CF_FORMAT_SELL_C8 : CF_FORMAT_SELL);
+        if (format)
+            *format = !sell                    ? CF_FORMAT_CSR
+                      : m->impl->n_codes > 0 ? CF_FORMAT_SELL_C8
+                      : m->impl->has_d16     ? CF_FORMAT_SELL_D16
+                                             : CF_FORMAT_SELL;
         if (stored_entries) *stored_entries = sell ? m->impl->sell_nnz : m->impl->nnz;
     });
 }

@@ -607,6 +607,56 @@ struct SellCodes8 {
     __device__ __forceinline__ const void *addr(int64_t o) const { return p + o; }
 };
 
+// 16-bit column deltas: a slot's column is its row base plus a signed
+// 16-bit delta (patterns whose offsets col - row all lie in [-32768, 32767]
+// but number more than kMaxCodes: unstructured meshes in a bandwidth-reducing
+// order).  Stored lane-major like the codes (lane l's len deltas at element
+// b + len l of the slice); a batch of up to eight comes from three aligned
+// 8-byte loads.  2 bytes per slot: 10 instead of 12 per FP64 entry, 6
+// instead of 8 per FP32 entry.
+struct SellDelta16 {
+    const int16_t *p;
+    template <int M> struct Batch {
+        uint32_t z[4];   // deltas t0 .. t0 + 7, two to a word
+        __device__ __forceinline__ int raw(int u) const { return (int)(int16_t)(z[u >> 1] >> (16 * (u & 1))); }
+    };
+    template <int M>
+    __device__ __forceinline__ Batch<M> load_batch(int64_t b, int lane, int len, int t0, uint64_t pol) const
+    {
+        static_assert(M <= 8, "at most eight deltas per batch");
+        const int64_t a = b + (int64_t)len * lane + t0;   // in deltas
+        const int64_t a0 = a & ~(int64_t)3;               // 8-byte boundary
+        const uint8_t *q = reinterpret_cast<const uint8_t *>(p + a0);
+        const uint2 w01 = ld_stream8(q, pol);
+        const uint2 w23 = ld_stream8(q + 8, pol);
+        const uint2 w45 = ld_stream8(q + 16, pol);
+        const unsigned k = (unsigned)(a - a0);            // 0..3 deltas into the window
+        const bool skip = k >= 2, half = k & 1u;
+        const uint32_t y0 = skip ? w01.y : w01.x, y1 = skip ? w23.x : w01.y, y2 = skip ? w23.y : w23.x;
+        const uint32_t y3 = skip ? w45.x : w23.y, y4 = skip ? w45.y : w45.x;
+        const unsigned sh = half ? 16u : 0u;
+        Batch<M> r;
+        r.z[0] = __funnelshift_r(y0, y1, sh);
+        r.z[1] = __funnelshift_r(y1, y2, sh);
+        r.z[2] = __funnelshift_r(y2, y3, sh);
+        r.z[3] = __funnelshift_r(y3, y4, sh);
+        return r;
+    }
+    // (the 24-byte window stays inside the padded array for any t0 < len)
+    template <int M>
+    __device__ __forceinline__ Batch<M> load_guarded(int64_t b, int lane, int len, int t0, uint64_t pol) const
+    {
+        return load_batch<M>(b, lane, len, t0, pol);
+    }
+    __device__ __forceinline__ int plain_slot(int64_t b, int len, int r, int t) const
+    {
+        return p[b + (int64_t)len * r + t];
+    }
+    __device__ __forceinline__ int col(int raw, int rb) const { return rb + raw; }
+    __device__ __forceinline__ int col_div(int raw, int rb) const { return rb + raw; }
+    __device__ __forceinline__ const void *addr(int64_t o) const { return p + o; }
+};
+
 // the row base a slot's code is relative to: the row, or 0 past n
 __device__ __forceinline__ int sell_row_base(int row, int n) { return row < n ? row : 0; }
 

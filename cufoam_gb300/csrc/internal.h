@@ -99,7 +99,8 @@ struct SolveArgs {
     const int32_t *s_off;      // [n_slices + 1] element offset of each slice
     const int32_t *s_col;
     const uint8_t *s_code;     // one-byte column codes of the same slots (null: none)
-    const int32_t *s_dtab;     // [256] offsets col - row the codes stand for
+    const int32_t *s_dtab;     // offsets col - row the codes stand for
+    const int16_t *s_d16;      // 16-bit column deltas col - row (null: none)
     const double *s_val;
     const double *s_valT;
     const float *s_val32;
@@ -196,7 +197,7 @@ struct Context {
     // scratch of the matrix builds (grow-only: a conversion after the first
     // allocates nothing) and the matrix of one-shot ldu2csr conversions
     DeviceBuffer scratch_flag, scratch_tmp, scratch_cnt, scratch_stats;
-    DeviceBuffer scratch_codes;   // offset set of the one-byte column codes (matrix.cu)
+    DeviceBuffer scratch_codes;   // offset set of the one-byte column codes, largest |offset| (matrix.cu)
     struct Matrix *ldu_scratch = nullptr;
 
     int fast_grid(const void *kernel, size_t dyn_smem) const;
@@ -257,6 +258,10 @@ struct Matrix {
     // col - row they index (n_codes distinct offsets; 0: 32-bit columns only)
     DeviceBuffer s_code, s_dtab;
     int32_t n_codes = 0;
+    // 16-bit column deltas col - row of the slots, when the codes cannot be
+    // used and every offset fits
+    DeviceBuffer s_d16;
+    bool has_d16 = false;
     bool have_sval = false, have_svalT = false, have_sval32 = false, have_svalT32 = false;
     // bumped by every change of the values, of 1/a_ii or of the format
     uint64_t gen = 1;

@@ -372,11 +372,39 @@ __device__ void offset_insert(int32_t *keys, int32_t *count, int32_t d)
     atomicMax(count, kMaxCodes + 1);
 }
 
-// keys = empty, count = 0
+// keys = empty, count = 0, largest |offset| = 0
 __global__ void k_offsets_clear(int32_t *keys, int32_t *count)
 {
     CF_FOR_ELEMS(i, kCodeHash) keys[i] = kNoOffset;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *count = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        count[0] = 0;
+        count[1] = 0;
+    }
+}
+
+// the largest |col - row| over the CSR entries (the 16-bit deltas' range)
+__global__ void k_csr_maxoff(int n, const int32_t *__restrict__ ro, const int32_t *__restrict__ col, int32_t *maxoff)
+{
+    int m = 0;
+    CF_FOR_ELEMS(i, n) {
+        const int re = ro[i + 1];
+        for (int j = ro[i]; j < re; ++j) m = max(m, abs(col[j] - i));
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(kFull, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(maxoff, m);
+}
+
+// the 16-bit delta of every slot, lane-major within the slice like the codes
+__global__ void k_sell_encode16(int n, int n_slices, const int32_t *__restrict__ soff,
+                                const int32_t *__restrict__ scol, int16_t *d16)
+{
+    CF_FOR_ELEMS(i, 32 * n_slices) {
+        const int s = i >> 5, lane = i & 31;
+        const int b = soff[s], len = (soff[s + 1] - b) >> 5;
+        const int rb = sell_row_base(i, n);
+        for (int t = 0; t < len; ++t) d16[b + len * lane + t] = (int16_t)(scol[b + 32 * t + lane] - rb);
+    }
 }
 
 // every CSR entry's offset, and 0; stops early once more than kMaxCodes
@@ -449,17 +477,21 @@ __global__ void k_sell_encode(int n, int n_slices, const int32_t *__restrict__ s
 #ifndef CF_PLAIN_SPMV8_MINB
 #define CF_PLAIN_SPMV8_MINB 4
 #endif
-// (CODES: the columns from the one-byte codes and their offset table)
-template <bool CODES>
-__global__ void __launch_bounds__(kBlock, CODES ? CF_PLAIN_SPMV8_MINB : (CF_PLAIN_SPMV_MINB > 0 ? CF_PLAIN_SPMV_MINB : 1))
+// (COLS: 0 the 32-bit columns, 1 the one-byte codes and their offset table,
+// 2 the 16-bit deltas)
+template <int COLS>
+__global__ void __launch_bounds__(kBlock, COLS ? CF_PLAIN_SPMV8_MINB : (CF_PLAIN_SPMV_MINB > 0 ? CF_PLAIN_SPMV_MINB : 1))
     k_spmv_sell(int n, int n_slices, const int32_t *__restrict__ off, const int32_t *__restrict__ col,
-                const uint8_t *__restrict__ code, const int32_t *__restrict__ tab, const double *__restrict__ val,
-                const int32_t *__restrict__ ro, int has_long, const double *__restrict__ x, double *y)
+                const uint8_t *__restrict__ code, const int32_t *__restrict__ tab, const int16_t *__restrict__ d16,
+                const double *__restrict__ val, const int32_t *__restrict__ ro, int has_long,
+                const double *__restrict__ x, double *y)
 {
     auto g = [&](int c) { return __ldg(x + c); };
     auto f = [&](int row, double v) { y[row] = v; };
-    if constexpr (CODES)
+    if constexpr (COLS == 1)
         sell_rows<double, CF_PLAIN_SPMV8_BATCH>(n, n_slices, off, SellCodes8(code, tab), val, ro, has_long != 0, g, f);
+    else if constexpr (COLS == 2)
+        sell_rows<double, CF_PLAIN_SPMV8_BATCH>(n, n_slices, off, SellDelta16{d16}, val, ro, has_long != 0, g, f);
     else
         sell_rows<double, CF_PLAIN_SPMV_BATCH>(n, n_slices, off, SellCols32{col}, val, ro, has_long != 0, g, f);
 }
@@ -580,9 +612,10 @@ static int grid_for(Context *ctx, int64_t work, int per_block = kBlock)
     return (int)g;
 }
 
-// The offset set of m's pattern (one-byte column codes) into the context's
-// scratch: keys [kCodeHash], count, then the slot -> code map [kCodeHash]
-// bytes.  Enqueued only; read back with the SELL-32 size.
+// The offset set of m's pattern (one-byte column codes) and its largest
+// |offset| (16-bit deltas) into the context's scratch: keys [kCodeHash],
+// count, largest |offset|, then the slot -> code map [kCodeHash] bytes.
+// Enqueued only; read back with the SELL-32 size.
 static void queue_offsets(Matrix *m)
 {
     Context *ctx = m->ctx;
@@ -593,6 +626,20 @@ static void queue_offsets(Matrix *m)
     k_csr_offsets<<<grid_for(ctx, m->n), kBlock, 0, ctx->stream>>>(m->n, m->ro.as<int32_t>(), m->col.as<int32_t>(),
                                                                   keys, keys + kCodeHash);
     CF_CHECK_LAUNCH();
+    k_csr_maxoff<<<grid_for(ctx, m->n), kBlock, 0, ctx->stream>>>(m->n, m->ro.as<int32_t>(), m->col.as<int32_t>(),
+                                                                 keys + kCodeHash + 1);
+    CF_CHECK_LAUNCH();
+}
+
+// The 16-bit column deltas of m's SELL-32 copy (every |offset| <= 32767).
+static void build_sell_d16(Matrix *m)
+{
+    Context *ctx = m->ctx;
+    m->s_d16.ensure(sizeof(int16_t) * ((size_t)m->sell_nnz + 32));
+    k_sell_encode16<<<grid_for(ctx, 32 * (int64_t)m->n_slices), kBlock, 0, ctx->stream>>>(
+        m->n, m->n_slices, m->s_off.as<int32_t>(), m->s_col.as<int32_t>(), m->s_d16.as<int16_t>());
+    CF_CHECK_LAUNCH();
+    m->has_d16 = true;
 }
 
 // The codes of m's SELL-32 copy from the offset set read back into hk /
@@ -1051,19 +1098,21 @@ bool matrix_ensure_sell(Matrix *m, bool transpose, bool fp32)
             k_sell_len<<<grid_for(ctx, (int64_t)ns + 1), kBlock, 0, ctx->stream>>>(
                 m->n, ns, m->ro.as<int32_t>(), slen.as<int32_t>(), tot.as<unsigned long long>());
             CF_CHECK_LAUNCH();
-            const bool want_codes = m->format_request != CF_FORMAT_SELL;
-            if (want_codes) queue_offsets(m);
+            const int req = m->format_request;
+            const bool want_codes = req == CF_FORMAT_AUTO || req == CF_FORMAT_SELL_C8;
+            const bool want_d16 = req == CF_FORMAT_AUTO || req == CF_FORMAT_SELL_D16;
+            if (want_codes || want_d16) queue_offsets(m);
             unsigned long long total = 0;
-            std::vector<int32_t> hk(want_codes ? kCodeHash + 1 : 0);
+            std::vector<int32_t> hk(want_codes || want_d16 ? kCodeHash + 2 : 0);
             CF_CUDA(cudaMemcpyAsync(&total, tot.ptr, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
-            if (want_codes)
-                CF_CUDA(cudaMemcpyAsync(hk.data(), ctx->scratch_codes.ptr, sizeof(int32_t) * (kCodeHash + 1),
+            if (want_codes || want_d16)
+                CF_CUDA(cudaMemcpyAsync(hk.data(), ctx->scratch_codes.ptr, sizeof(int32_t) * (kCodeHash + 2),
                                         cudaMemcpyDeviceToHost, ctx->stream));
             CF_CUDA(cudaStreamSynchronize(ctx->stream));
             const bool fits = total < (unsigned long long)INT32_MAX - 64;
             const bool good = fits && (double)total <= 1.2 * (double)m->nnz + 32.0 * 8 &&
                               m->nnz <= 32 * (int64_t)m->n;
-            const bool forced = m->format_request == CF_FORMAT_SELL || m->format_request == CF_FORMAT_SELL_C8;
+            const bool forced = req == CF_FORMAT_SELL || req == CF_FORMAT_SELL_C8 || req == CF_FORMAT_SELL_D16;
             require(!forced || fits, CF_UNSUPPORTED, "SELL-32 copy exceeds 2^31 entries");
             if (forced || good) {
                 exclusive_scan(ctx, ns + 1, slen.as<int32_t>(), m->s_off.as<int32_t>(), tmp);
@@ -1076,16 +1125,23 @@ bool matrix_ensure_sell(Matrix *m, bool transpose, bool fp32)
                 CF_CHECK_LAUNCH();
                 m->sell = 1;
                 m->n_codes = 0;
+                m->has_d16 = false;
+                const int32_t count = (want_codes || want_d16) ? hk[kCodeHash] : 0;
+                const int32_t maxoff = (want_codes || want_d16) ? hk[kCodeHash + 1] : INT32_MAX;
                 if (want_codes) {
-                    const int32_t count = hk[kCodeHash];
                     hk.resize(kCodeHash);
                     build_sell_codes(m, hk, count);
                 }
-                if (m->format_request == CF_FORMAT_SELL_C8 && m->n_codes == 0) {
+                if (want_d16 && m->n_codes == 0 && maxoff <= 32767) build_sell_d16(m);
+                if (req == CF_FORMAT_SELL_C8 && m->n_codes == 0) {
                     m->sell = -1;   // decided again (and refused again) by the next call
                     throw Error{CF_UNSUPPORTED,
                                 "one-byte column codes need at most " + std::to_string(kMaxCodes) +
                                     " distinct column offsets col - row"};
+                }
+                if (req == CF_FORMAT_SELL_D16 && !m->has_d16) {
+                    m->sell = -1;
+                    throw Error{CF_UNSUPPORTED, "16-bit column deltas need every |col - row| <= 32767"};
                 }
             }
         }
@@ -1160,13 +1216,14 @@ void spmv(Matrix *m, bool transpose, const double *x, double *y, bool ref_order)
             k_spmv_sell_ref<<<g, kBlock, 0, ctx->stream>>>(m->n, m->n_slices, m->s_off.as<int32_t>(),
                                                            m->s_col.as<int32_t>(), sv, m->ro.as<int32_t>(), x, y);
         } else {
-            const bool codes = m->n_codes > 0;
-            const void *kern = codes ? (const void *)k_spmv_sell<true> : (const void *)k_spmv_sell<false>;
-            const int g = ctx->fast_grid(kern, 0);
-            (codes ? k_spmv_sell<true> : k_spmv_sell<false>)<<<g, kBlock, 0, ctx->stream>>>(
-                m->n, m->n_slices, m->s_off.as<int32_t>(), m->s_col.as<int32_t>(),
-                codes ? m->s_code.as<uint8_t>() : nullptr, codes ? m->s_dtab.as<int32_t>() : nullptr, sv,
-                m->ro.as<int32_t>(), m->has_long ? 1 : 0, x, y);
+            const int cols = m->n_codes > 0 ? 1 : m->has_d16 ? 2 : 0;
+            auto kern = cols == 1 ? k_spmv_sell<1> : cols == 2 ? k_spmv_sell<2> : k_spmv_sell<0>;
+            const int g = ctx->fast_grid((const void *)kern, 0);
+            kern<<<g, kBlock, 0, ctx->stream>>>(m->n, m->n_slices, m->s_off.as<int32_t>(), m->s_col.as<int32_t>(),
+                                                cols == 1 ? m->s_code.as<uint8_t>() : nullptr,
+                                                cols == 1 ? m->s_dtab.as<int32_t>() : nullptr,
+                                                cols == 2 ? m->s_d16.as<int16_t>() : nullptr, sv,
+                                                m->ro.as<int32_t>(), m->has_long ? 1 : 0, x, y);
         }
         CF_CHECK_LAUNCH();
         return;

@@ -427,8 +427,9 @@ static Kernels inner_kernels_t(int solver)
 static Kernels inner_kernels(int solver, int format)
 {
     return format == kSellC ? inner_kernels_t<kSellC>(solver)
-           : format == kSell ? inner_kernels_t<kSell>(solver)
-                             : inner_kernels_t<kCsr>(solver);
+           : format == kSellD ? inner_kernels_t<kSellD>(solver)
+           : format == kSell  ? inner_kernels_t<kSell>(solver)
+                              : inner_kernels_t<kCsr>(solver);
 }
 
 template <int FMT>
@@ -504,8 +505,9 @@ MixedResult run_mixed(Context *ctx, Matrix *m, int solver, const cf_controls &c,
     const Kernels kk = inner_kernels(solver, fmt);
     const bool scaled = solver == CF_JMR;
     const void *k_residual = fmt == kSellC ? residual_kernel<kSellC>(scaled)
-                             : fmt == kSell ? residual_kernel<kSell>(scaled)
-                                            : residual_kernel<kCsr>(scaled);
+                             : fmt == kSellD ? residual_kernel<kSellD>(scaled)
+                             : fmt == kSell  ? residual_kernel<kSell>(scaled)
+                                             : residual_kernel<kCsr>(scaled);
     bool use_graph = use_graph_in;
     GraphEntry *ge = nullptr;
     if (use_graph) {

@@ -673,8 +673,9 @@ static Kernels fast_kernels(int solver)
 Kernels fast_body_kernels(int solver, int format)
 {
     return format == kSellC ? fast_kernels<kSellC>(solver)
-           : format == kSell ? fast_kernels<kSell>(solver)
-                             : fast_kernels<kCsr>(solver);
+           : format == kSellD ? fast_kernels<kSellD>(solver)
+           : format == kSell  ? fast_kernels<kSell>(solver)
+                              : fast_kernels<kCsr>(solver);
 }
 
 const void *fast_flush_kernel() { return (const void *)k_f_flush_x; }

@@ -684,14 +684,17 @@ void solve(Matrix *m, int solver, const cf_controls &c, const double *b_in, doub
         A.s_col = m->s_col.as<int32_t>();
         A.s_val = m->s_val.as<double>();
         A.s_valT = m->have_svalT ? m->s_valT.as<double>() : nullptr;
-        // one-byte column codes: read by the FP32 sweeps, and by the FP64
-        // fast passes when asked for (CF_FORMAT_SELL_C8).  Those passes are
+        // one-byte column codes (or 16-bit column deltas): read by the FP32
+        // sweeps, and by the FP64 fast passes when asked for
+        // (CF_FORMAT_SELL_C8, CF_FORMAT_SELL_D16).  Those passes are
         // bound by FP64 issue on GB300 (8 FP64 instructions per row of the CG
         // SpMV), so saving bytes does not shorten them (128^3 CG step 71.2 us
         // either way); the FP32 MR step at 256^3 drops from 237 to 214 us.
         if (m->n_codes > 0 && !ref && (mixed || m->format_request == CF_FORMAT_SELL_C8)) {
             A.s_code = m->s_code.as<uint8_t>();
             A.s_dtab = m->s_dtab.as<int32_t>();
+        } else if (m->has_d16 && !ref && (mixed || m->format_request == CF_FORMAT_SELL_D16)) {
+            A.s_d16 = m->s_d16.as<int16_t>();   // 16-bit column deltas, read by the same passes
         }
     }
     if (tr) {

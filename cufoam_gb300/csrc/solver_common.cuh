@@ -21,8 +21,9 @@ namespace cf {
 // row as one FMA chain in entry order.  for_rows calls f(row, sum_j a_ij g(j))
 // for every row; val is the CSR value array, sval its SELL-32 copy.
 // ---------------------------------------------------------------------------
-// kSellC: the SELL-32 copy with one-byte column codes (SellCodes8)
-enum { kCsr = 0, kSell = 1, kSellC = 2 };
+// kSellC: the SELL-32 copy with one-byte column codes (SellCodes8); kSellD:
+// with 16-bit column deltas (SellDelta16)
+enum { kCsr = 0, kSell = 1, kSellC = 2, kSellD = 3 };
 
 // SELL passes take CF_SELL_BATCH entries per thread per batch: all their
 // loads and gathers are issued before the first FMA, and a row's last
@@ -66,6 +67,9 @@ __device__ __forceinline__ void for_rows(const SolveArgs *a, const V *val, const
         constexpr int B = BATCH > 0 ? BATCH : (sizeof(V) == 4 ? kSellBatch32 : kSellBatch);
         sell_rows<V, B>(a->n, a->n_slices, a->s_off, SellCodes8(a->s_code, a->s_dtab), sval, a->ro,
                         a->has_long != 0, g, f);
+    } else if constexpr (FMT == kSellD) {
+        constexpr int B = BATCH > 0 ? BATCH : (sizeof(V) == 4 ? kSellBatch32 : kSellBatch);
+        sell_rows<V, B>(a->n, a->n_slices, a->s_off, SellDelta16{a->s_d16}, sval, a->ro, a->has_long != 0, g, f);
     } else {
         const int n = a->n, cap = a->stage_cap;
         CF_STAGE(V, cap);
@@ -90,6 +94,9 @@ __device__ __forceinline__ void for_rows2(const SolveArgs *a, const V *val1, con
     } else if constexpr (FMT == kSellC) {
         sell_rows2<V, 1>(a->n, a->n_slices, a->s_off, SellCodes8(a->s_code, a->s_dtab), sval1, sval2, a->ro,
                          a->has_long != 0, g1, g2, f);
+    } else if constexpr (FMT == kSellD) {
+        sell_rows2<V, 1>(a->n, a->n_slices, a->s_off, SellDelta16{a->s_d16}, sval1, sval2, a->ro,
+                         a->has_long != 0, g1, g2, f);
     } else {
         const int n = a->n, cap = a->stage_cap;
         CF_STAGE(V, cap);
@@ -111,6 +118,7 @@ __device__ __forceinline__ void sell_prefetch(const SolveArgs *a, const V *sval)
 {
     if constexpr (FMT == kSell) sell_prefetch_first(a->n_slices, a->s_off, SellCols32{a->s_col}, sval);
     if constexpr (FMT == kSellC) sell_prefetch_first(a->n_slices, a->s_off, SellCodes8(a->s_code, a->s_dtab), sval);
+    if constexpr (FMT == kSellD) sell_prefetch_first(a->n_slices, a->s_off, SellDelta16{a->s_d16}, sval);
 }
 
 // ---------------------------------------------------------------------------
@@ -396,12 +404,16 @@ static GraphEntry *loop_graph(Context *ctx, const Kernels &kk, int solver, int p
     return &(ctx->graphs[key] = ge);
 }
 
-// format: kCsr, kSell or kSellC (solve_format)
+// format: kCsr, kSell, kSellC or kSellD (solve_format)
 Kernels fast_body_kernels(int solver, int format);
 
 // The format of a solve's fast kernels from its arguments: CSR (no SELL-32
-// copy), SELL-32 with 32-bit columns, or with one-byte column codes.
-inline int solve_format(const SolveArgs &A) { return A.n_slices == 0 ? kCsr : (A.s_code ? kSellC : kSell); }
+// copy), SELL-32 with 32-bit columns, with one-byte column codes, or with
+// 16-bit column deltas.
+inline int solve_format(const SolveArgs &A)
+{
+    return A.n_slices == 0 ? kCsr : A.s_code ? kSellC : A.s_d16 ? kSellD : kSell;
+}
 const void *fast_flush_kernel();
 
 // ---------------------------------------------------------------------------

@@ -240,15 +240,19 @@ void cf_matrix_destroy(cf_matrix *m);
  * solver loops keep the 32-bit columns (GB300's FP64 issue rate, not HBM,
  * bounds them).  SELL and SELL_C8 may be asked for: SELL_C8 makes every
  * fast pass read the codes, and fails with CF_UNSUPPORTED on a pattern with
- * more offsets.  Every format
+ * more offsets.  A pattern with more offsets, all in [-32768, 32767] (an
+ * unstructured mesh in a bandwidth-reducing order), gets 16-bit column
+ * deltas instead (CF_FORMAT_SELL_D16: column = row + delta; 10 bytes per
+ * FP64 entry, 6 per FP32 entry), read where the codes would be; asked for
+ * on a pattern outside that range it fails with CF_UNSUPPORTED.  Every format
  * sums each row in entry order, so results do not depend on the choice.
  * The reference-order kernels read the 32-bit columns.  No reference
  * counterpart (the reference has CSR only). */
-enum { CF_FORMAT_AUTO = 0, CF_FORMAT_CSR = 1, CF_FORMAT_SELL = 2, CF_FORMAT_SELL_C8 = 3 };
+enum { CF_FORMAT_AUTO = 0, CF_FORMAT_CSR = 1, CF_FORMAT_SELL = 2, CF_FORMAT_SELL_C8 = 3, CF_FORMAT_SELL_D16 = 4 };
 cf_status cf_matrix_set_format(cf_matrix *m, int32_t format);
-/* The format the fast kernels use now (CF_FORMAT_CSR, CF_FORMAT_SELL or
- * CF_FORMAT_SELL_C8; decides AUTO first) and the stored entries including
- * padding. */
+/* The format the fast kernels use now (CF_FORMAT_CSR, CF_FORMAT_SELL,
+ * CF_FORMAT_SELL_C8 or CF_FORMAT_SELL_D16; decides AUTO first) and the
+ * stored entries including padding. */
 cf_status cf_matrix_format(cf_matrix *m, int32_t *format, int64_t *stored_entries);
 cf_status cf_matrix_shape(const cf_matrix *m, int32_t *n_rows, int32_t *n_faces, int64_t *nnz);
 /* CSR arrays of A (transpose = 0) or A^T (transpose = 1; the reference's

@@ -157,9 +157,10 @@ def test_spmv_formats_agree(ctx, case):
     32 entries as one FMA chain in entry order and each longer row with the
     whole warp in the same lane partition, so they agree exactly (zeros up
     to sign), for A and A^T, and after a value update.  AUTO takes the codes
-    when the pattern has at most 32 distinct offsets col - row (the grids);
-    the randomly permuted mesh has more and keeps 32-bit columns, and asking
-    for the codes there fails."""
+    when the pattern has at most 32 distinct offsets col - row (the grids),
+    else 16-bit deltas when the offsets fit (the randomly permuted mesh;
+    asking for the codes there fails); the star's and the skewed matrix's
+    long rows are summed by the whole warp over 16-bit deltas too."""
     L = SPMV_CASES[case]() if case != "ragged" else O.grid_lognormal(7, 5, 3, 9)  # 105 rows
     M = _matrix(ctx, L)
     fmt, stored = M.format()
@@ -169,13 +170,13 @@ def test_spmv_formats_agree(ctx, case):
     coded = len(np.union1d(offsets, [0])) <= 32
     if case in ("star", "skewed"):
         assert fmt == "csr" and stored == nnz      # padding to the long row: too much
-    else:
-        assert fmt == ("sell8" if coded else "sell") and nnz <= stored <= 1.2 * nnz + 256
+    else:   # the permuted mesh's offsets all fit 16 bits
+        assert fmt == ("sell8" if coded else "sell16") and nnz <= stored <= 1.2 * nnz + 256
     assert coded == (case not in ("permuted", "star", "skewed"))   # 1,627 / 5,999 / 13,845 offsets
     x = O.uniform(7, L.n)
     ref = O.ref_spmv(A, x)
     ys = {}
-    for f in ("csr", "sell", "sell8"):
+    for f in ("csr", "sell", "sell8", "sell16"):
         if f == "sell8" and not coded:
             with pytest.raises(cf.CufoamError, match="32 distinct column offsets"):
                 M.set_format(f)

@@ -1,11 +1,13 @@
-"""SELL-32 with one-byte column codes (CF_FORMAT_SELL_C8).
+"""SELL-32 with compact columns: one-byte codes (CF_FORMAT_SELL_C8) and
+16-bit deltas (CF_FORMAT_SELL_D16).
 
-The codes change only how the SELL-32 copy stores its columns: a slot's
-column is its row plus an entry of a table of the pattern's distinct offsets
-col - row.  Every fast-order kernel must therefore produce the same bits as
-with 32-bit columns -- iteration counts, residual histories, psi -- in FP64
-and in the mixed-precision FP32 sweeps, for A and A^T, on the 7-point grids
-and on a mesh whose offsets fill most of the table."""
+Both change only how the SELL-32 copy stores its columns: a slot's column is
+its row plus an entry of a table of the pattern's distinct offsets col - row
+(codes), or plus a signed 16-bit delta.  Every fast-order kernel must
+therefore produce the same bits as with 32-bit columns -- iteration counts,
+residual histories, psi -- in FP64 and in the mixed-precision FP32 sweeps,
+for A and A^T, on the 7-point grids, on meshes whose offsets fill most of the
+code table, and on random patterns."""
 import numpy as np
 import pytest
 
@@ -25,7 +27,7 @@ def _solve(M, name, b, opts, transpose=False, maxit=40000):
 
 def _both(M, name, b, opts, transpose=False):
     out = {}
-    for f in ("sell", "sell8"):
+    for f in ("sell", "sell8", "sell16"):
         M.set_format(f)
         out[f] = _solve(M, name, b, opts, transpose)
         assert M.format()[0] == f
@@ -40,7 +42,7 @@ def test_fp64_fast_order_same_bits(ctx, name):
     M = cf.LduMatrix.from_ldu(L, ctx)
     assert M.format()[0] == "sell8"
     out = _both(M, name, b, {"reduction": "fast"})
-    assert out["sell"] == out["sell8"]
+    assert out["sell"] == out["sell8"] == out["sell16"]
     assert out["sell"][0] > 5
 
 
@@ -53,7 +55,7 @@ def test_mixed_sweeps_same_bits(ctx, name, transpose):
     b = O.uniform(5, L.n)
     M = cf.LduMatrix.from_ldu(L, ctx)
     out = _both(M, name, b, {"precision": "mixed", "tolerance": 1e-10}, transpose)
-    assert out["sell"] == out["sell8"]
+    assert out["sell"] == out["sell8"] == out["sell16"]
     assert out["sell"][1] == 0
 
 
@@ -77,11 +79,11 @@ def test_many_offsets_and_value_update(ctx):
     b = O.uniform(3, L.n)
     for step in range(2):
         ys = {}
-        for f in ("sell", "sell8"):
+        for f in ("sell", "sell8", "sell16"):
             M.set_format(f)
             ys[f] = (M.spmv(x, row_order="fast").tobytes(), M.spmv(x, transpose=True, row_order="fast").tobytes(),
                      _solve(M, "CG", b, {"reduction": "fast"}))
-        assert ys["sell"] == ys["sell8"]
+        assert ys["sell"] == ys["sell8"] == ys["sell16"]
         ref = O.ref_spmv(O.ldu2csr(L), x)
         y = np.frombuffer(ys["sell8"][0], dtype=np.float64)
         assert np.allclose(y, ref, rtol=1e-14, atol=1e-14 * np.abs(ref).max())
@@ -122,12 +124,12 @@ def test_codes_limit(ctx, n_strides):
         M.set_format("sell8")
         with pytest.raises(cf.CufoamError, match="at most 32 distinct column offsets"):
             M.format()
-        M.set_format("sell")
-        assert M.format()[0] == "sell"
         M.set_format("csr")
         y = M.spmv(x, row_order="fast")
-        M.set_format("sell")
-        assert M.spmv(x, row_order="fast").tobytes() == y.tobytes()
+        for f in ("sell", "sell16"):   # rows of 33 entries: summed by the whole warp
+            M.set_format(f)
+            assert M.format()[0] == f
+            assert M.spmv(x, row_order="fast").tobytes() == y.tobytes()
 
 
 def _random_offset_ldu(seed):
@@ -166,14 +168,69 @@ def test_random_offset_sets_same_bits(ctx, seed):
     x = O.uniform(7 + seed, L.n)
     b = O.uniform(3 + seed, L.n)
     out = {}
-    for f in ("csr", "sell", "sell8"):
+    for f in ("csr", "sell", "sell8", "sell16"):
         M.set_format(f)
         assert M.format()[0] == f
         out[f] = (M.spmv(x, row_order="fast").tobytes(), M.spmv(x, transpose=True, row_order="fast").tobytes())
         if f != "csr":
             out[f] += (_solve(M, "MR", b, {"reduction": "fast", "tolerance": 1e-9}, maxit=5000),)
-    assert out["csr"][:2] == out["sell"][:2] == out["sell8"][:2]
-    assert out["sell"][2] == out["sell8"][2]
+    assert out["csr"][:2] == out["sell"][:2] == out["sell8"][:2] == out["sell16"][:2]
+    assert out["sell"][2] == out["sell8"][2] == out["sell16"][2]
     ref = O.ref_spmv(A, x)
     y = np.frombuffer(out["sell8"][0], dtype=np.float64)
     assert np.allclose(y, ref, rtol=1e-14, atol=1e-14 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_delta16_many_offsets_same_bits(ctx, seed):
+    """Patterns with more offsets than the codes' table but every |col - row|
+    within 16 bits take the deltas under AUTO (a mesh renumbered inside
+    windows of 64 rows: hundreds of offsets; a randomly permuted one): the
+    products and fast-order and mixed solves are bit-identical to 32-bit
+    columns."""
+    base = O.grid_lognormal(24, 20, 16 + seed, 6 + seed)
+    rng = np.random.default_rng(seed)
+    perm = np.arange(base.n)
+    w = 64 if seed % 2 == 0 else base.n
+    for s0 in range(0, base.n, w):
+        perm[s0:s0 + w] = rng.permutation(perm[s0:s0 + w])
+    L = O.permute_ldu(base, perm.astype(np.int32))
+    A = O.ldu2csr(L)
+    offs = A.cols - np.repeat(np.arange(L.n), np.diff(A.row_offsets))
+    assert len(np.unique(offs)) > 32 and np.abs(offs).max() <= 32767
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    fmt, stored = M.format()
+    assert fmt == ("sell16" if stored <= 1.2 * len(A.cols) + 256 else "csr")
+    x = O.uniform(7 + seed, L.n)
+    b = O.uniform(3 + seed, L.n)
+    out = {}
+    for f in ("sell", "sell16"):
+        M.set_format(f)
+        assert M.format()[0] == f
+        out[f] = (M.spmv(x, row_order="fast").tobytes(), M.spmv(x, transpose=True, row_order="fast").tobytes(),
+                  _solve(M, "CG", b, {"reduction": "fast"}),
+                  _solve(M, "MR", b, {"precision": "mixed", "tolerance": 1e-10}))
+    assert out["sell"] == out["sell16"]
+    assert out["sell"][3][1] == 0
+
+
+def test_delta16_range_limit(ctx):
+    """Offsets beyond 16 bits (a chain of 40,000 cells, cell i < 6,900 also
+    coupled to i + 33,000 + i mod 40: 83 distinct offsets up to 33,039): no
+    codes and no deltas under AUTO, and asking for the deltas fails."""
+    n = 40000
+    far = np.arange(6900)
+    la = np.concatenate([np.arange(n - 1), far]).astype(np.int32)
+    ua = np.concatenate([np.arange(1, n), far + 33000 + far % 40]).astype(np.int32)
+    order = np.lexsort((ua, la))
+    la, ua = la[order], ua[order]
+    w = np.full(len(la), 1.0)
+    diag = np.full(n, 4.0)
+    L = O.LDU(n, diag, -w, -w, la, ua)
+    M = cf.LduMatrix.from_ldu(L, ctx)
+    assert M.format()[0] == "sell"
+    M.set_format("sell16")
+    with pytest.raises(cf.CufoamError, match="16-bit column deltas"):
+        M.format()
+    M.set_format("auto")
+    assert M.format()[0] == "sell"
