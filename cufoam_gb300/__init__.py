@@ -299,10 +299,19 @@ class CsrMatrix(LduMatrix):
         self._h = h
         self.n = int(n)
         self.n_faces = -1
+        self._pattern = (row_offsets, cols)
         self._set_symmetry(lambda: _csr_symmetric(n, row_offsets, cols, vals))
 
     def update_values(self, diag, lower, upper) -> None:
-        raise NotImplementedError("a CSR matrix has no LDU coefficients")
+        raise NotImplementedError("a CSR matrix has no LDU coefficients (use update_csr_values)")
+
+    def update_csr_values(self, vals) -> None:
+        """New values on the same pattern (vals[nnz], host array or CUDA
+        tensor, in the entry order the matrix was created with)."""
+        pv, mv, kv = _ptr(vals, np.float64, "vals")
+        self.ctx.check(self._lib.cf_matrix_update_csr_values(self._h, pv, mv), "cf_matrix_update_csr_values")
+        ro, cols = self._pattern
+        self._set_symmetry(lambda: _csr_symmetric(self.n, ro, cols, kv))
 
 
 def _csr_symmetric(n, ro, cols, vals) -> bool:

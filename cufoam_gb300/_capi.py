@@ -126,6 +126,7 @@ def load(build_if_missing: bool = True):
                                         C.POINTER(C.c_int64)]),
         "cf_matrix_export_csr": (C.c_int32, [P, C.c_int32, P, P, P, C.c_int32]),
         "cf_matrix_set_format": (C.c_int32, [P, C.c_int32]),
+        "cf_matrix_update_csr_values": (C.c_int32, [P, P, C.c_int32]),
         "cf_matrix_create_csr": (C.c_int32, [P, C.c_int32, C.c_int64, P, P, P, C.c_int32, P]),
         "cf_csr_file_info": (C.c_int32, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                          C.POINTER(C.c_int64)]),

@@ -477,6 +477,15 @@ cf_status cf_matrix_update_values(cf_matrix *m, const double *diag, const double
     });
 }
 
+cf_status cf_matrix_update_csr_values(cf_matrix *m, const double *vals, int32_t memory)
+{
+    if (!m || !m->owner) return CF_BAD_INPUT;
+    return guarded(m->owner, [&] {
+        cf::require(memory == CF_MEM_HOST || memory == CF_MEM_DEVICE, CF_BAD_INPUT, "bad memory kind");
+        cf::matrix_update_csr_values(m->impl, vals, memory);
+    });
+}
+
 cf_status cf_matrix_set_format(cf_matrix *m, int32_t format)
 {
     if (!m || !m->owner) return CF_BAD_INPUT;

@@ -292,6 +292,7 @@ bool matrix_ensure_sell(Matrix *m, bool transpose, bool fp32);
 Matrix *matrix_from_csr(Context *ctx, int n, int64_t nnz, const int32_t *ro, const int32_t *col,
                         const double *val);
 void matrix_set_transpose_csr(Matrix *m, const int32_t *roT, const int32_t *colT, const double *valT);
+void matrix_update_csr_values(Matrix *m, const double *vals, int memory);
 void matrix_set_inverse_diagonal(Matrix *m, const double *dinv);
 void csr_transpose(Context *ctx, int n_rows, int n_cols, int64_t nnz, const int32_t *ro,
                    const int32_t *col, const double *val, int32_t *roT, int32_t *colT, double *valT);

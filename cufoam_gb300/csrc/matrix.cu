@@ -1039,6 +1039,28 @@ Matrix *matrix_from_csr(Context *ctx, int n, int64_t nnz, const int32_t *ro, con
     return m;
 }
 
+// New values on a CSR-built matrix's pattern: the diagonal and its derived
+// vectors are refreshed on the device, every other value copy is rebuilt
+// when next needed.
+void matrix_update_csr_values(Matrix *m, const double *vals, int memory)
+{
+    Context *ctx = m->ctx;
+    require(m->from_csr, CF_UNSUPPORTED,
+            "the matrix was created from LDU coefficients (its values change through cf_matrix_update_values)");
+    require(vals || m->nnz == 0, CF_BAD_INPUT, "null value array");
+    if (m->nnz > 0) upload(ctx, m->val.ptr, vals, sizeof(double) * (size_t)m->nnz, memory);
+    const int gc = grid_for(ctx, (int64_t)m->n + 1);
+    k_csr_diag<<<gc, kBlock, 0, ctx->stream>>>(m->n, m->ro.as<int32_t>(), m->col.as<int32_t>(), m->val.as<double>(),
+                                               m->diag.as<double>());
+    CF_CHECK_LAUNCH();
+    k_diag_derived<<<gc, kBlock, 0, ctx->stream>>>(m->n, m->diag.as<double>(), m->dinv.as<double>(),
+                                                   m->dinv_sqrt.as<double>());
+    CF_CHECK_LAUNCH();
+    m->have_valT = m->have_32 = m->have_T32 = m->have_dmin = false;
+    m->have_sval = m->have_svalT = m->have_sval32 = m->have_svalT32 = false;
+    ++m->gen;
+}
+
 // A^T values on A's pattern from a CSR A^T (given, or computed): the
 // patterns must coincide (true for every LDU matrix).
 void matrix_set_transpose_csr(Matrix *m, const int32_t *roT, const int32_t *colT, const double *valT)

@@ -37,6 +37,12 @@ def lib():
         L.mf_solve_reused_addressing.argtypes = [C.c_int] + list(L.mf_solve.argtypes)
         L.cuFoamGB300_matrix_builds.restype = C.c_long
         L.cuFoamGB300_matrix_builds.argtypes = []
+        L.cuFoamGB300_coupled_builds.restype = C.c_long
+        L.cuFoamGB300_coupled_builds.argtypes = []
+        # mf_solve_coupled without its processor flag, after a slot number
+        L.mf_solve_coupled_reused.restype = C.c_int
+        L.mf_solve_coupled_reused.argtypes = [C.c_int] + list(L.mf_solve_coupled.argtypes[:21]) + \
+            [C.c_void_p, C.c_char_p, C.c_int]
         L.mf_set_transport.restype = None
         L.mf_set_transport.argtypes = [C.c_void_p]
         L.mf_solve_decomposed.restype = C.c_int
@@ -53,6 +59,12 @@ def lib():
 def matrix_builds() -> int:
     """Device matrices the plugin has built so far (its cache misses)."""
     return int(lib().cuFoamGB300_matrix_builds())
+
+
+def coupled_builds() -> int:
+    """Coupled (cyclic-patch) matrices the plugin has built so far (the
+    misses of their cache)."""
+    return int(lib().cuFoamGB300_coupled_builds())
 
 
 class FoamError(RuntimeError):
@@ -99,12 +111,20 @@ def foam_solve(solver: str, ldu, source, psi, tolerance: float = 1e-6, rel_tol: 
         ca, cb = np.ascontiguousarray(ca, np.float64), np.ascontiguousarray(cb, np.float64)
         if not (fa.shape == fb.shape == ca.shape == cb.shape):
             raise ValueError("cyclic patch arrays must have one length")
-        rc = lib().mf_solve_coupled(solver.encode(), ldu.n, lo.shape[0], d.ctypes.data,
-                                    None if symmetric else lo.ctypes.data, up.ctypes.data,
-                                    la.ctypes.data, ua.ctypes.data, b.ctypes.data, psi.ctypes.data,
-                                    tolerance, rel_tol, max_iter, len(keys), ck, cv, int(fa.shape[0]),
-                                    fa.ctypes.data, fb.ctypes.data, ca.ctypes.data, cb.ctypes.data,
-                                    1 if processor_patch else 0, out.ctypes.data, err, 1024)
+        if reuse_addressing is not None and not processor_patch:
+            rc = lib().mf_solve_coupled_reused(int(reuse_addressing), solver.encode(), ldu.n, lo.shape[0],
+                                               d.ctypes.data, None if symmetric else lo.ctypes.data,
+                                               up.ctypes.data, la.ctypes.data, ua.ctypes.data, b.ctypes.data,
+                                               psi.ctypes.data, tolerance, rel_tol, max_iter, len(keys), ck,
+                                               cv, int(fa.shape[0]), fa.ctypes.data, fb.ctypes.data,
+                                               ca.ctypes.data, cb.ctypes.data, out.ctypes.data, err, 1024)
+        else:
+            rc = lib().mf_solve_coupled(solver.encode(), ldu.n, lo.shape[0], d.ctypes.data,
+                                        None if symmetric else lo.ctypes.data, up.ctypes.data,
+                                        la.ctypes.data, ua.ctypes.data, b.ctypes.data, psi.ctypes.data,
+                                        tolerance, rel_tol, max_iter, len(keys), ck, cv, int(fa.shape[0]),
+                                        fa.ctypes.data, fb.ctypes.data, ca.ctypes.data, cb.ctypes.data,
+                                        1 if processor_patch else 0, out.ctypes.data, err, 1024)
     if rc != 0:
         raise FoamError(err.value.decode())
     return {"initialResidual": out[0], "finalResidual": out[1], "nIterations": int(out[2]),

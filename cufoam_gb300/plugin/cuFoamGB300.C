@@ -12,6 +12,9 @@
  *              each call uploads the
  *              coefficients, converts them on the device, and runs
  *              normFactor + the solver inside one device-driven loop.
+ * Meshes with cyclic patches solve on a coupled matrix (the interface
+ * coefficients appended to their rows), kept in a cache of its own whose
+ * values are refreshed on every solve.
  * Fixed relative to the reference: the constructor forwards
  * interfaceBouCoeffs (the reference passes interfaceIntCoeffs twice,
  * cuFoamCG/cuFoamCG.C:30-31).
@@ -169,6 +172,28 @@ cf_matrix *deviceMatrix(const lduMatrix &M)   // under gb300Mutex()
     return hit->m;
 }
 
+// Coupled matrices (cyclic patches folded in), kept across solve() calls
+// like the device matrices: keyed on the addressing (as above) and on the
+// cyclic patches' face cells, all of them hashed.  Each entry holds, for
+// every CSR entry, where its value comes from in [diag | lower | upper | the
+// interface coefficients in patch and face order], so a repeat solve
+// gathers its values on the host and refreshes them on the device
+// (cf_matrix_update_csr_values): no conversion, no allocation, no SELL-32
+// layout rebuild.
+struct CoupledCacheEntry {
+    const void *lowerAddr = nullptr;
+    const void *upperAddr = nullptr;
+    label n = -1, nFaces = -1;
+    uint64_t fingerprint = 0, ifcFingerprint = 0;
+    uint64_t lastUse = 0;
+    cf_matrix *m = nullptr;
+    std::vector<int32_t> src;   // value source of each CSR entry
+    std::vector<double> vals;   // the gathered values
+};
+
+std::vector<CoupledCacheEntry> gCoupledCache;
+long gCoupledBuilds = 0;
+
 } // namespace
 
 static_assert(sizeof(label) == sizeof(int32_t), "cuFoamGB300 needs 32-bit labels");
@@ -210,11 +235,23 @@ cf_controls cuFoamGB300Solver::gb300Controls() const
     return c;
 }
 
-cf_matrix *cuFoamGB300Solver::coupledMatrix() const
+cf_matrix *cuFoamGB300Solver::coupledMatrix() const   // under gb300Mutex()
 {
-    // couplings of the cyclic patches: (faceCell, neighbour faceCell, -coeff)
-    std::vector<std::vector<std::pair<label, scalar>>> extra;
-    bool any = false;
+    // couplings of the cyclic patches: (faceCell, neighbour faceCell,
+    // -coeff), numbered in patch and face order
+    struct Extra {
+        label col;
+        int32_t e;
+    };
+    std::vector<std::vector<Extra>> extra;
+    std::vector<double> ext;   // -coeff of extra e
+    uint64_t ifp = 1469598103934665603ull;
+    auto mix = [&ifp](uint64_t v) {
+        for (int k = 0; k < 8; ++k) {
+            ifp ^= (v >> (8 * k)) & 0xffu;
+            ifp *= 1099511628211ull;
+        }
+    };
     const lduInterfaceFieldPtrsList &ifs = interfaces();
     for (label patchi = 0; patchi < ifs.size(); ++patchi) {
         if (!ifs.set(patchi)) continue;
@@ -235,57 +272,122 @@ cf_matrix *cuFoamGB300Solver::coupledMatrix() const
                                  << " does not match its neighbour" << exit(FatalError);
         }
         if (extra.empty()) extra.resize(matrix().diag().size());
-        for (label f = 0; f < fc.size(); ++f) extra[fc[f]].push_back({nfc[f], -coeffs[f]});
-        any = any || fc.size() > 0;
+        mix((uint64_t)patchi);
+        mix((uint64_t)fc.size());
+        for (label f = 0; f < fc.size(); ++f) {
+            mix((uint64_t)(uint32_t)fc[f]);
+            mix((uint64_t)(uint32_t)nfc[f]);
+            extra[fc[f]].push_back({nfc[f], (int32_t)ext.size()});
+            ext.push_back(-coeffs[f]);
+        }
     }
-    if (!any) return nullptr;
-    // the LDU part as the reference's CSR (device ldu2csr), then each row's
-    // interface entries after its own
+    if (ext.empty()) return nullptr;
     const lduMatrix &M = matrix();
     const lduAddressing &A = M.lduAddr();
     const label n = M.diag().size(), nf = A.lowerAddr().size();
-    cf_ldu_view v;
-    std::memset(&v, 0, sizeof(v));
-    v.n_cells = n;
-    v.n_faces = nf;
-    v.diag = M.diag().cdata();
-    v.lower = M.lower().cdata();
-    v.upper = M.upper().cdata();
-    v.lower_addr = A.lowerAddr().cdata();
-    v.upper_addr = A.upperAddr().cdata();
-    v.losort = A.losortAddr().cdata();
-    v.losort_start = A.losortStartAddr().cdata();
-    v.owner_start = A.ownerStartAddr().cdata();
-    v.memory = CF_MEM_HOST;
-    std::vector<int32_t> ro((size_t)n + 1), col((size_t)n + 2 * (size_t)nf);
-    std::vector<double> val(col.size());
+    const uint64_t fp = addressingFingerprint(A, n);
     cf_context *ctx = gb300Context();
-    cf_status st = cf_ldu2csr(ctx, &v, ro.data(), col.data(), val.data(), CF_MEM_HOST);
-    std::vector<int32_t> ro2((size_t)n + 1), col2;
-    std::vector<double> val2;
-    if (st == CF_OK) {
-        col2.reserve(col.size() + 2 * (size_t)n);
-        val2.reserve(col.size() + 2 * (size_t)n);
-        for (label i = 0; i < n; ++i) {
-            ro2[(size_t)i] = (int32_t)col2.size();
-            for (int32_t j = ro[(size_t)i]; j < ro[(size_t)i + 1]; ++j) {
-                col2.push_back(col[(size_t)j]);
-                val2.push_back(val[(size_t)j]);
+    CoupledCacheEntry *hit = nullptr, *slot = nullptr;
+    for (CoupledCacheEntry &e : gCoupledCache) {
+        if (e.lowerAddr == A.lowerAddr().cdata() && e.upperAddr == A.upperAddr().cdata() && e.n == n &&
+            e.nFaces == nf && e.fingerprint == fp && e.ifcFingerprint == ifp)
+            hit = &e;
+    }
+    cf_status st = CF_OK;
+    if (!hit) {
+        // the LDU part as the reference's CSR (device ldu2csr) on
+        // index-encoded values: each entry's value is its source position
+        std::vector<double> di((size_t)n), lo((size_t)nf), up((size_t)nf);
+        for (label i = 0; i < n; ++i) di[(size_t)i] = (double)i;
+        for (label f = 0; f < nf; ++f) {
+            lo[(size_t)f] = (double)(n + f);
+            up[(size_t)f] = (double)(n + nf + f);
+        }
+        cf_ldu_view v;
+        std::memset(&v, 0, sizeof(v));
+        v.n_cells = n;
+        v.n_faces = nf;
+        v.diag = di.data();
+        v.lower = lo.data();
+        v.upper = up.data();
+        v.lower_addr = A.lowerAddr().cdata();
+        v.upper_addr = A.upperAddr().cdata();
+        v.losort = A.losortAddr().cdata();
+        v.losort_start = A.losortStartAddr().cdata();
+        v.owner_start = A.ownerStartAddr().cdata();
+        v.memory = CF_MEM_HOST;
+        std::vector<int32_t> ro((size_t)n + 1), col((size_t)n + 2 * (size_t)nf);
+        std::vector<double> pos(col.size());
+        st = cf_ldu2csr(ctx, &v, ro.data(), col.data(), pos.data(), CF_MEM_HOST);
+        if (st == CF_OK) {
+            // then each row's interface entries after its own
+            if (gCoupledCache.size() < kMatrixCacheEntries) {
+                gCoupledCache.reserve(kMatrixCacheEntries);
+                gCoupledCache.emplace_back();
+                slot = &gCoupledCache.back();
+            } else {
+                slot = &gCoupledCache[0];
+                for (CoupledCacheEntry &e : gCoupledCache)
+                    if (e.lastUse < slot->lastUse) slot = &e;
             }
-            for (const auto &e : extra[(size_t)i]) {
-                col2.push_back(e.first);
-                val2.push_back(e.second);
+            if (slot->m) cf_matrix_destroy(slot->m);
+            *slot = CoupledCacheEntry();
+            std::vector<int32_t> ro2((size_t)n + 1), col2;
+            col2.reserve(col.size() + ext.size());
+            slot->src.reserve(col.size() + ext.size());
+            for (label i = 0; i < n; ++i) {
+                ro2[(size_t)i] = (int32_t)col2.size();
+                for (int32_t j = ro[(size_t)i]; j < ro[(size_t)i + 1]; ++j) {
+                    col2.push_back(col[(size_t)j]);
+                    slot->src.push_back((int32_t)pos[(size_t)j]);
+                }
+                for (const Extra &x : extra[(size_t)i]) {
+                    col2.push_back(x.col);
+                    slot->src.push_back((int32_t)(n + 2 * nf) + x.e);
+                }
+            }
+            ro2[(size_t)n] = (int32_t)col2.size();
+            slot->vals.resize(col2.size());
+            hit = slot;
+            ++gCoupledBuilds;
+            // values gathered below, then the matrix made from them
+            std::vector<int32_t>().swap(ro);
+            std::vector<int32_t>().swap(col);
+            slot->lowerAddr = A.lowerAddr().cdata();
+            slot->upperAddr = A.upperAddr().cdata();
+            slot->n = n;
+            slot->nFaces = nf;
+            slot->fingerprint = fp;
+            slot->ifcFingerprint = ifp;
+            const scalar *d = M.diag().cdata(), *l = M.lower().cdata(), *u = M.upper().cdata();
+            for (size_t j = 0; j < slot->src.size(); ++j) {
+                const int32_t q = slot->src[j];
+                slot->vals[j] = q < n ? d[q] : q < n + nf ? l[q - n] : q < n + 2 * nf ? u[q - n - nf]
+                                                                                  : ext[(size_t)(q - n - 2 * nf)];
+            }
+            st = cf_matrix_create_csr(ctx, n, (int64_t)col2.size(), ro2.data(), col2.data(), slot->vals.data(),
+                                      CF_MEM_HOST, &slot->m);
+            if (st != CF_OK) {
+                slot->m = nullptr;
+                *slot = CoupledCacheEntry();
             }
         }
-        ro2[(size_t)n] = (int32_t)col2.size();
-        cf_matrix *m = nullptr;
-        st = cf_matrix_create_csr(ctx, n, (int64_t)col2.size(), ro2.data(), col2.data(), val2.data(),
-                                  CF_MEM_HOST, &m);
-        if (st == CF_OK) return m;
+    } else {
+        // the same pattern: this call's coefficients in the cached order
+        const scalar *d = M.diag().cdata(), *l = M.lower().cdata(), *u = M.upper().cdata();
+        for (size_t j = 0; j < hit->src.size(); ++j) {
+            const int32_t q = hit->src[j];
+            hit->vals[j] = q < n ? d[q] : q < n + nf ? l[q - n] : q < n + 2 * nf ? u[q - n - nf]
+                                                                              : ext[(size_t)(q - n - 2 * nf)];
+        }
+        st = cf_matrix_update_csr_values(hit->m, hit->vals.data(), CF_MEM_HOST);
     }
-    FatalErrorInFunction << "cuFoamGB300: cannot load the coupled matrix: " << cf_status_string(st)
-                         << ": " << cf_context_last_error(ctx) << exit(FatalError);
-    return nullptr;
+    if (st != CF_OK || !hit || !hit->m) {
+        FatalErrorInFunction << "cuFoamGB300: cannot load the coupled matrix: " << cf_status_string(st)
+                             << ": " << cf_context_last_error(ctx) << exit(FatalError);
+    }
+    hit->lastUse = ++gMatrixClock;
+    return hit->m;
 }
 
 solverPerformance cuFoamGB300Solver::solve(scalarField &psi, const scalarField &source,
@@ -314,7 +416,6 @@ solverPerformance cuFoamGB300Solver::solve(scalarField &psi, const scalarField &
     } else {
         st = cf_solve(m, kind_, &c, source.cdata(), psi.data(), &perf);
     }
-    if (coupled) cf_matrix_destroy(coupled);
     if (st != CF_OK) {
         FatalErrorInFunction << type() << ": solve failed: " << cf_status_string(st) << ": "
                              << cf_context_last_error(gb300Context()) << exit(FatalError);
@@ -372,4 +473,12 @@ extern "C" long cuFoamGB300_matrix_builds()
 {
     std::lock_guard<std::mutex> lock(Foam::gb300Mutex());
     return Foam::gMatrixBuilds;
+}
+
+// Coupled (cyclic) matrices the plugin has built since the library was
+// loaded (a diagnostic for tests of their cache).
+extern "C" long cuFoamGB300_coupled_builds()
+{
+    std::lock_guard<std::mutex> lock(Foam::gb300Mutex());
+    return Foam::gCoupledBuilds;
 }

@@ -203,6 +203,25 @@ int mf_solve_coupled(const char *solver_name, int n, int n_faces, const double *
                rel_tol, max_iter, n_extra, keys, values, c, out, err, err_len);
 }
 
+/* mf_solve_coupled on the lduAddressing object of `slot` (0..3), kept
+ * between calls (see mf_solve_reused_addressing). */
+int mf_solve_coupled_reused(int slot, const char *solver_name, int n, int n_faces, const double *diag,
+                            const double *lower, const double *upper, const int *lower_addr,
+                            const int *upper_addr, const double *source, double *psi, double tolerance,
+                            double rel_tol, int max_iter, int n_extra, const char *const *keys,
+                            const char *const *values, int n_cyc, const int *fcA, const int *fcB,
+                            const double *coeffA, const double *coeffB, double *out, char *err, int err_len)
+{
+    Coupling c;
+    c.n_cyc = n_cyc;
+    c.fcA = fcA;
+    c.fcB = fcB;
+    c.coeffA = coeffA;
+    c.coeffB = coeffB;
+    return run(solver_name, n, n_faces, diag, lower, upper, lower_addr, upper_addr, source, psi, tolerance,
+               rel_tol, max_iter, n_extra, keys, values, c, out, err, err_len, slot);
+}
+
 /* The parallel run's transport (minifoam's Pstream): NULL ends the
  * parallel run.  The structure must stay valid while it is installed. */
 void mf_set_transport(const Foam::mfTransport *t)

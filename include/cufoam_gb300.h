@@ -225,6 +225,12 @@ cf_status cf_matrix_create_ldu(cf_context *ctx, const cf_ldu_view *ldu, cf_matri
 /* New coefficients, same addressing (time-step / Ux,Uy,Uz reuse). */
 cf_status cf_matrix_update_values(cf_matrix *m, const double *diag, const double *lower,
                                   const double *upper, int32_t memory);
+/* New values, same pattern, for a matrix made by cf_matrix_create_csr
+ * (vals[nnz] in its entry order; host or device memory).  No reference
+ * counterpart: the reference converts and uploads its CSR on every solve
+ * (cuFoamCG/cuFoamCG.C:48-62); the plugin uses this for the coupled
+ * matrices of meshes with cyclic patches. */
+cf_status cf_matrix_update_csr_values(cf_matrix *m, const double *vals, int32_t memory);
 void cf_matrix_destroy(cf_matrix *m);
 /* Storage the fast (CF_REDUCE_FAST) kernels read the matrix from.  AUTO
  * (the default) picks SELL-32 -- slices of 32 rows padded to their longest
