@@ -420,6 +420,24 @@ def suite_c2(ctx, device):
             k = perf.n_iterations
             res[key] = {"iters": k, "ms": round(perf.solve_ms, 2), "status": perf.status_name,
                         "gbs": round(per(mat, n) * k / (perf.solve_ms * 1e-3) / 1e9, 1)}
+        if case == "const":
+            # CG in FP64 and in mixed precision (FP32 sweeps over the one-byte
+            # column codes, FP64 refinement) to the same tolerance; the time
+            # and the true relative residual ||b - A x|| / normFactor of each
+            mx = {}
+            for prec in ("FP64", "mixed"):
+                psi = torch.zeros(n, dtype=torch.float64, device=dev)
+                c = {"tolerance": TOL, "maxIter": 400000, "precision": prec}
+                cf.cuFoamCG("p", M, dict(c, maxIter=8)).solve(psi, src)
+                psi.zero_()
+                torch.cuda.synchronize()
+                perf = cf.cuFoamCG("p", M, c).solve(psi, src)
+                torch.cuda.synchronize()
+                r = src - M.spmv(psi, row_order="fast")
+                mx[prec] = {"ms": round(perf.solve_ms, 2), "iters": perf.n_iterations, "status": perf.status_name,
+                            "true": float(f"{float(torch.linalg.norm(r)) / perf.norm_factor:.3g}")}
+            mx["speedup"] = round(mx["FP64"]["ms"] / mx["mixed"]["ms"], 3)
+            out["cg_mixed_vs_fp64"] = mx
         out[case] = res
         M.close()
     return out
@@ -477,7 +495,11 @@ def compact_suite(extras: dict) -> dict:
         out["c1_ldu2csr_us"] = c1["ldu2csr_us"]
     c2 = extras.get("c2")
     if isinstance(c2, dict) and "error" not in c2:
+        if "cg_mixed_vs_fp64" in c2:
+            out["c2_const_cg_mixed_vs_fp64"] = c2["cg_mixed_vs_fp64"]
         for case, res in c2.items():
+            if case == "cg_mixed_vs_fp64":
+                continue
             for k, r in res.items():
                 out[f"c2_{case}_{k}"] = {"iters": r["iters"], "ms": r["ms"], "gbs": r["gbs"],
                                          "status": r["status"]}
