@@ -35,3 +35,40 @@ def test_reference_arm_json_line():
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["config"]["workload"].startswith("poisson7_128^3")
     assert "unavailable" in d["reference_gpu_kernels"]
+
+
+def test_streamed_bytes_per_format():
+    """The algorithmic bytes bench.py credits each column format with: 12 B
+    per stored FP64 entry with 32-bit columns, 9 with one-byte codes (plus
+    the 128-byte offset table), 10 with 16-bit deltas; the FP64 solver loops
+    read the 32-bit columns whatever compact copy exists; every coded or
+    delta variant of a fast or mixed kernel in the launch table carries the
+    bytes of its own format."""
+    sys.path.insert(0, ROOT)
+    import bench
+    n, S = 2_097_152, 14_614_528
+    slices = (n + 31) // 32 + 1
+    assert bench.iter_matrix_bytes("sell", n, 0, S) == 12 * S + 4 * slices
+    assert bench.iter_matrix_bytes("sell8", n, 0, S) == 9 * S + 4 * slices + 128
+    assert bench.iter_matrix_bytes("sell16", n, 0, S) == 10 * S + 4 * slices
+    for fmt in ("sell8", "sell16"):
+        assert bench.iter_matrix_bytes(fmt, n, 0, S, fp64_loop=True) == 12 * S + 4 * slices
+    nnz = 14_581_760
+    assert bench.iter_matrix_bytes("csr", n, nnz, nnz) == 12 * nnz + 4 * (n + 1)
+    t = bench._launch_bytes(n, 6_242_304, nnz, S, 65_536)
+    for name, (formula, val) in t.items():
+        if "Msell" in formula and (name.startswith("k_f_") or name.startswith("k_mx_")):
+            # the format is the kernel's last template argument (the first for
+            # k_mx_residual)
+            if name.startswith("k_mx_residual"):
+                fmt1 = name.replace("<1, ", "<@, ")
+            elif name.startswith("k_f_mr_spmv"):
+                fmt1 = name[:-3] + "@>" if name.endswith(", 1>") else name
+            else:
+                fmt1 = name.replace("<1>", "<@>")
+            if "@" not in fmt1:
+                continue
+            for fmt, tag in (("2", "Msell8"), ("3", "Msell16")):
+                other = fmt1.replace("@", fmt)
+                assert other in t, other
+                assert tag in t[other][0] and t[other][1] < val
