@@ -63,7 +63,7 @@ def test_streamed_bytes_per_format():
             if name.startswith("k_mx_residual"):
                 fmt1 = name.replace("<1, ", "<@, ")
             elif name.startswith("k_f_mr_spmv"):
-                fmt1 = name[:-3] + "@>" if name.endswith(", 1>") else name
+                fmt1 = name[:-2] + "@>" if name.endswith(", 1>") else name
             else:
                 fmt1 = name.replace("<1>", "<@>")
             if "@" not in fmt1:
