@@ -658,7 +658,7 @@ def run_ours(args):
         m_e2e.update_values(h["diag"], h["lower"], h["upper"])
         return cf.cuFoamCG("p", m_e2e, ctrl).solve(hpsi, hb)
 
-    for _ in range(2):
+    for _ in range(max(args.warmup, 3)):
         e2e_step()
     if dist:
         dist.barrier()
