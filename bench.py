@@ -951,7 +951,9 @@ def batched_vs_sequential(ctx, device, n_systems: int = 512, tol: float = 1e-8,
 
 def run_profile(args):
     """A short run for ncu: the same 128^3 CG solve with host-driven
-    launches (every kernel a separate launch), then plain SpMVs."""
+    launches (every kernel a separate launch), then five plain SpMVs over the
+    one-byte column codes (k_spmv_sell<1>) and five over the 32-bit columns
+    (k_spmv_sell<0>)."""
     import torch
 
     import cufoam_gb300 as cf
@@ -966,8 +968,10 @@ def run_profile(args):
         psi.zero_()
         perf = s.solve(psi, src)
     x = torch.from_numpy(W.uniform(5, L.n)).cuda()
-    for _ in range(5):
-        M.spmv(x, row_order="fast")
+    for fmt in ("auto", "sell"):
+        M.set_format(fmt)
+        for _ in range(5):
+            M.spmv(x, row_order="fast")
     torch.cuda.synchronize()
     print(f"profile run ok: {perf.n_iterations} iterations")
     return 0
