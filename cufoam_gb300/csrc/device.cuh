@@ -554,7 +554,10 @@ struct SellCols32 {
         return r;
     }
     // slot t of row r of the slice (len slots)
-    __device__ __forceinline__ int32_t plain_slot(int64_t b, int, int r, int t) const { return p[b + r + (int64_t)32 * t]; }
+    __device__ __forceinline__ int32_t plain_slot(int64_t b, int, int r, int t) const
+    {
+        return p[b + r + (int64_t)32 * t];
+    }
     __device__ __forceinline__ int col(int32_t raw, int) const { return raw; }
     __device__ __forceinline__ int col_div(int32_t raw, int) const { return raw; }
     __device__ __forceinline__ const void *addr(int64_t o) const { return p + o; }

@@ -480,7 +480,8 @@ __global__ void k_sell_encode(int n, int n_slices, const int32_t *__restrict__ s
 // (COLS: 0 the 32-bit columns, 1 the one-byte codes and their offset table,
 // 2 the 16-bit deltas)
 template <int COLS>
-__global__ void __launch_bounds__(kBlock, COLS ? CF_PLAIN_SPMV8_MINB : (CF_PLAIN_SPMV_MINB > 0 ? CF_PLAIN_SPMV_MINB : 1))
+__global__ void
+__launch_bounds__(kBlock, COLS ? CF_PLAIN_SPMV8_MINB : (CF_PLAIN_SPMV_MINB > 0 ? CF_PLAIN_SPMV_MINB : 1))
     k_spmv_sell(int n, int n_slices, const int32_t *__restrict__ off, const int32_t *__restrict__ col,
                 const uint8_t *__restrict__ code, const int32_t *__restrict__ tab, const int16_t *__restrict__ d16,
                 const double *__restrict__ val, const int32_t *__restrict__ ro, int has_long,
