@@ -122,3 +122,35 @@ int main(void){printf("%zu %zu %zu %zu %zu\n", sizeof(cf_ldu_view), sizeof(cf_co
     assert sizes == [C.sizeof(_capi.cf_ldu_view), C.sizeof(_capi.cf_controls),
                      C.sizeof(_capi.cf_perf), C.sizeof(_capi.cf_device_info),
                      _capi.cf_controls.time_limit_s.offset]
+
+
+def test_header_enums_match_the_python_binding():
+    """Every CF_ enum constant of include/cufoam_gb300.h has the value the
+    ctypes binding uses (formats, memory kinds, statuses, solvers, ...)."""
+    import os
+    import re
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                            "cufoam_gb300.h")).read()
+    found = {}
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    hdr = re.sub(r"//[^\n]*", "", hdr)
+    for body in re.findall(r"enum\s*(?:\w+\s*)?\{([^}]*)\}", hdr):
+        nxt = 0
+        for item in body.split(","):
+            item = item.strip()
+            if not item:
+                continue
+            if "=" in item:
+                name, val = (t.strip() for t in item.split("=", 1))
+                nxt = int(val, 0)
+            else:
+                name = item
+            found[name] = nxt
+            nxt += 1
+    assert found["CF_FORMAT_SELL_C8"] == 3 and found["CF_FORMAT_SELL_D16"] == 4
+    checked = 0
+    for name, val in found.items():
+        if hasattr(_capi, name):
+            assert getattr(_capi, name) == val, name
+            checked += 1
+    assert checked >= 10
